@@ -1,0 +1,315 @@
+"""Benchmark of the GPU energy-packet transport: cell crossings/s.
+
+One step = one transport iteration of the clumpy 61^3 full-sphere nebula
+(lognormal nH, median 300 cm^-3, sigma_ln 1, 3-cell Gaussian correlation,
+seed 1; 60 kK blackbody star of 5e37 erg/s; 600 bins; 2e7 packets), FP32
+march with FP64 estimator sums.  A crossing is one pathSegment loop body
+ending in a full crossing or an interaction (source/photon_mod.f90:1517,
+:1817).
+
+  value   crossings / device time of the step, grid resident in HBM (the
+          estimators are zeroed inside the step, as iterateMC does)
+  e2e     the same metric through the drop-in call mc_transport_run with HOST
+          (pinned) buffers: grid upload, transport, estimator download
+  roofline  16 algorithmic bytes per crossing (4 B opacity + 4 B active +
+          8 B FP64 Jste) over the transport kernel's CUDA-event time, against
+          the measured HBM copy bandwidth
+  cpu_baseline  the FP32 oracle (a C++ restatement of the reference's Fortran
+          path, FP32 sums like the reference's `real` Jste) on the host cores,
+          on a bounded sample of the same workload
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "cell crossings/s"
+UNIT = "crossings/s"
+BYTES_PER_CROSSING = 16
+
+
+def workload(name):
+    from mocassin_gb300 import nebula
+    return {"clumpy61": nebula.clumpy61, "octant21": nebula.octant21, "dusty81": nebula.dusty81,
+            "twostar101": nebula.twostar101}[name]()
+
+
+def measured_peak():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_crossing():
+    """DRAM bytes per crossing from the committed ncu summary, if any."""
+    p = os.path.join(HERE, "profiles", "transport_plain_fp32_dram.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_crossing:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if len(s) >= 7 and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) >= 7 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 7 for i in range(4)
+                          if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(neb, seconds_target=15.0, threads=None):
+    """FP32 oracle on the host cores over a bounded packet sample."""
+    from oracle import runner
+    threads = threads or os.cpu_count() or 1
+    n = 20000
+    t0 = time.perf_counter()
+    _, _, _, st = runner.run(neb, n_packets=n, precision="fp32", seed=1, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = st["crossings"] / dt
+    # grow the sample to ~seconds_target of CPU work
+    n2 = int(min(max(n * seconds_target / max(dt, 1e-3), n), 2_000_000))
+    t0 = time.perf_counter()
+    _, _, _, st = runner.run(neb, n_packets=n2, precision="fp32", seed=2, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = st["crossings"] / dt
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d packets of the %d-packet step (%d crossings, %.1f s, FP32 march, FP64 sums)"
+                      % (n2, sum(neb.n_packets), st["crossings"], dt)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import runner
+    from mocassin_gb300 import nebula
+    neb = nebula.build(workload(args.config))
+    threads = os.cpu_count() or 1
+    n = args.ref_packets
+    for w in range(args.warmup):
+        runner.run(neb, n_packets=max(n // 10, 1000), precision="fp32", seed=100 + w, threads=threads)
+    cross, total = 0, 0.0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, _, st = runner.run(neb, n_packets=n, precision="fp32", seed=1 + k, threads=threads)
+        total += time.perf_counter() - t0
+        cross += st["crossings"]
+    value = cross / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": neb.spec.name, "cells": neb.ncells, "nbins": neb.nbins,
+                       "packets_per_step": n, "packets_per_iteration": sum(neb.n_packets),
+                       "note": "each step is a bounded packet sample of the iteration"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d packets per step x %d steps, FP32 oracle (C++ restatement of "
+                                       "photon_mod.f90; the Fortran reference has no compiler here)"
+                                       % (n, args.steps)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="clumpy61")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--packets", type=int, default=0, help="override packets per step")
+    ap.add_argument("--ref-packets", type=int, default=200000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    from mocassin_gb300 import build, nebula, transport
+    build.build()
+    spec = workload(args.config)
+    if args.packets:
+        spec.stars[0].n_packets = args.packets
+    neb = nebula.build(spec)
+    npk = sum(neb.n_packets)
+
+    ctx = transport.TransportContext(neb)
+    for w in range(args.warmup):
+        ctx.run(seed=1000 + w, iteration=1, precision=args.precision, zero_first=True)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(torch.cuda.current_device() if ws == 1 else local)
+    clocks.start()
+    # the library's kernels run on its own stream; its CUDA events bracket
+    # each step (zeroing + transport + counter read-back) and the call
+    # synchronises that stream before returning
+    stats = []
+    for k in range(args.steps):
+        stats.append(ctx.run(seed=1 + rank * 1000003 + k, iteration=1, precision=args.precision, zero_first=True))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = np.array([s["kernel_ms"] for s in stats])
+    cross = int(sum(s["crossings"] for s in stats))
+    t_dev = float(step_ms.sum()) / 1e3
+    if ws > 1:
+        t = torch.tensor([t_dev], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        c = torch.tensor([cross], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(c)
+        t_dev, cross_all = float(t.item()), float(c.item())
+    else:
+        cross_all = float(cross)
+    value = cross_all / t_dev
+    ctx.close()
+
+    # e2e: the drop-in call with host (pinned) buffers, copies inside the timed region
+    import ctypes as C
+    from mocassin_gb300 import abi
+    pinned = {}
+
+    def pin(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        pinned[id(a)] = t
+        return t
+
+    lib = transport.library()
+    m = abi.Marshalled(neb)
+    fields = [("opacity", neb.opacity), ("rec_pdf", neb.rec_pdf), ("total_lines", neb.total_lines),
+              ("x_axis", neb.x_axis), ("y_axis", neb.y_axis), ("z_axis", neb.z_axis), ("nu_array", neb.nu)]
+    h2d = 0
+    for name, arr in fields:
+        t = pin(arr.astype(np.float32))
+        setattr(m.grid, name, C.cast(t.data_ptr(), C.POINTER(C.c_float)))
+        h2d += t.numel() * 4
+    ta = pin(neb.active.astype(np.int32))
+    m.grid.active = C.cast(ta.data_ptr(), C.POINTER(C.c_int32))
+    h2d += ta.numel() * 4
+    if neb.sca_opac is not None:
+        t = pin(neb.sca_opac)
+        m.grid.sca_opac = C.cast(t.data_ptr(), C.POINTER(C.c_float))
+        h2d += t.numel() * 4
+    js = torch.zeros((neb.nbins, neb.ncells + 1), dtype=torch.float64).pin_memory()
+    es = torch.zeros((neb.nbins + 1, neb.ncells + 1), dtype=torch.float64).pin_memory()
+    d2h = (js.numel() + es.numel()) * 8
+    e2e_t, e2e_c = 0.0, 0
+    for k in range(args.e2e_steps + 1):
+        opts = abi.make_opts(seed=77 + k, iteration=1, precision=abi.MC_PREC_FP32 if args.precision == "fp32"
+                             else abi.MC_PREC_FP64)
+        st = abi.McStats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = lib.mc_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts),
+                                  C.cast(js.data_ptr(), C.POINTER(C.c_double)), None,
+                                  C.cast(es.data_ptr(), C.POINTER(C.c_double)), C.byref(st))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise transport.TransportError(rc, lib.mc_last_error().decode())
+        if k > 0:  # first call is a warm-up
+            e2e_t += dt
+            e2e_c += st.crossings
+    e2e = {"value": e2e_c / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "call": "mc_transport_run (host pinned buffers; includes device allocation, upload, CDF re-layout, "
+                   "transport, download)"}
+
+    peak, peak_kind = measured_peak()
+    achieved = cross / (t_dev if ws == 1 else float(step_ms.sum()) / 1e3) * BYTES_PER_CROSSING / 1e9
+    tpc = traffic_per_crossing()
+    per_launch_cross = cross / max(len(stats), 1)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (tpc * per_launch_cross) if tpc else None,
+            "kernel": "transport_plain_kernel<float>", "peak_kind": peak_kind + " hbm_gbs (copy)",
+            "algorithmic_bytes_per_crossing": BYTES_PER_CROSSING}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(step_ms.mean()), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision.replace("fp", "f"),
+            "data": "synthetic",
+            "config": {"workload": neb.spec.name, "grid": "%d^3" % neb.nx, "cells": neb.ncells, "nbins": neb.nbins,
+                       "packets_per_step": npk, "crossings_per_step": per_launch_cross,
+                       "march": args.precision, "estimators": "f64",
+                       "l2": "inputs larger than L2 (opacity %.0f MB, Jste %.0f MB)"
+                             % (neb.opacity.nbytes / 1e6, neb.opacity.size * 8 / 1e6),
+                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "roofline": roof, "e2e": e2e, "gpu_launches": len(stats), "clocks": clk}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(neb)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,204 @@
+/*
+ * mocassin_gpu.h -- C-ABI of the GB300 energy-packet transport library
+ * (libmcgpu.so).
+ *
+ * The library replaces mocassin's Monte Carlo packet loop:
+ *   subroutine energyPacketDriver(iStar, n, grid, gpLoc, cellLoc)
+ *     source/photon_mod.f90:26-285  (driver loop, re-emission loop :120-125)
+ *     source/photon_mod.f90:289-487 (energyPacketRun)
+ *     source/photon_mod.f90:768-1059 (newPhotonPacket), :491-684 (initPhotonPacket)
+ *     source/photon_mod.f90:720-764 (getNu2), :1061-2872 (pathSegment), :2875-3101 (hg)
+ *     source/vector_mod.f90:303-314 (randomUnitVector)
+ * called from iterateMC at source/iteration_mod.f90:488-493.
+ *
+ * Conventions
+ *  - Every array crossing this boundary is a plain pointer plus sizes.  Host
+ *    arrays keep the layout the Fortran side already has (column-major):
+ *      active(nx,ny,nz)          int32, x fastest       (common_mod.f90:258)
+ *      opacity(0:Nc,1:Nnu)       float, cell fastest    (common_mod.f90:290)
+ *      scaOpac, recPDF, dustPDF  same shape as opacity  (common_mod.f90:264,293,268)
+ *      totalLines(0:Nc)          float                  (common_mod.f90:295)
+ *      Jste/Jdif(0:Nc,1:Nnu)     double accumulators, cell fastest
+ *      escapedPackets(0:Nc,0:Nnu,0:nAngle) double, cell fastest
+ *    Grid indices (x,y,z cell indices, nuP) are 1-based as in the Fortran.
+ *  - Outputs are caller-allocated and are ACCUMULATED into (the caller zeroes
+ *    them once per iteration, as iteration_mod.f90:458-472 does).  The values
+ *    are the raw sums of dl*deltaE/dV of photon_mod.f90:1563-1574/1822-1833;
+ *    the caller still applies the x1e-9 and /8 of iteration_mod.f90:705-724.
+ *  - Every entry point returns an mc_status (0 = MC_OK).  The reference's
+ *    fatal "print*; stop" insanity checks become error codes; the text of the
+ *    last error of the calling thread is returned by mc_last_error().
+ *  - One host thread per process drives the library (the reference is one
+ *    thread per MPI rank).  Calls are not re-entrant on one context.
+ */
+#ifndef MOCASSIN_GPU_H
+#define MOCASSIN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MC_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum mc_status {
+  MC_OK = 0,
+  MC_ERR_ARG = 1,          /* bad pointer / size / flag combination          */
+  MC_ERR_CUDA = 2,         /* a CUDA runtime call failed                        */
+  MC_ERR_BOUNDS = 3,       /* a packet left the index range (pathSegment :1198) */
+  MC_ERR_NAN = 4,          /* NaN position/direction/opacity (photon_mod :1143) */
+  MC_ERR_REPLAY = 5,       /* replay draw stream exhausted                      */
+  MC_ERR_TIMEOUT = 6,      /* device watchdog budget ran out                    */
+  MC_ERR_UNSUPPORTED = 7,  /* option outside the built path (sub-grids, 1D ...) */
+  MC_ERR_NOMEM = 8,        /* device allocation failed                          */
+  MC_ERR_NO_DEVICE = 9     /* no CUDA device visible                            */
+} mc_status;
+
+/* ---- grid flags (the common_mod logicals that steer the transport) ----- */
+#define MC_FLAG_SYMMETRIC_XYZ (1u << 0) /* lgSymmetricXYZ                     */
+#define MC_FLAG_GAS           (1u << 1) /* lgGas                              */
+#define MC_FLAG_DUST          (1u << 2) /* lgDust                             */
+#define MC_FLAG_ISOTROPIC     (1u << 3) /* lgIsotropic (dust scattering)      */
+#define MC_FLAG_DEBUG         (1u << 4) /* lgDebug: diffuse packets go to Jdif */
+#define MC_FLAG_MULTISTARS    (1u << 5) /* lgMultistars: no octant folding    */
+
+/* Precision of the march (mc_run_opts_t.precision). */
+#define MC_PREC_FP32 0  /* FP32 march, cell-local coordinates, FP64 sums      */
+#define MC_PREC_FP64 1  /* FP64 march, reference order of operations (replay) */
+
+/* Random-draw source (mc_run_opts_t.rng). */
+#define MC_RNG_PHILOX 0 /* Philox4x32-10 keyed by (seed, iteration, star)    */
+#define MC_RNG_REPLAY 1 /* draws read from a caller buffer, one row per packet */
+
+/* Run flags (mc_run_opts_t.run_flags). */
+#define MC_RUN_ZERO_FIRST 1 /* zero the device estimators inside the call, before
+                               the transport (iteration_mod.f90:458-472)      */
+
+/* Read-only description of one (mother) grid for one iteration.  All
+ * pointers are HOST pointers owned by the caller; they are read during the
+ * call only. */
+typedef struct mc_grid {
+  int32_t nx, ny, nz;      /* grid%nx, grid%ny, grid%nz                       */
+  int32_t ncells;          /* grid%nCells = Nc; arrays carry rows 0..Nc       */
+  int32_t nbins;           /* nbins = Nnu                                     */
+  int32_t n_angle;         /* nAngleBins; only 0 is supported (bin 0 only)    */
+  const float *x_axis;     /* [nx] cm                                         */
+  const float *y_axis;     /* [ny] cm                                         */
+  const float *z_axis;     /* [nz] cm                                         */
+  const int32_t *active;   /* [nx*ny*nz], x fastest; 0 = inactive (row 0)     */
+  const float *opacity;    /* [(Nc+1)*Nnu], cell fastest, 1/cm                */
+  const float *sca_opac;   /* [(Nc+1)*Nnu] or NULL when no dust               */
+  const float *rec_pdf;    /* [(Nc+1)*Nnu] cumulative, or NULL without gas    */
+  const float *total_lines;/* [Nc+1] line fraction, or NULL without gas       */
+  const float *dust_pdf;   /* [(Nc+1)*Nnu] cumulative, or NULL                */
+  const float *nu_array;   /* [Nnu] Ryd                                       */
+  const float *g_sca;      /* [Nnu] HG asymmetry, or NULL                     */
+  float geo_corr[3];       /* grid%geoCorrX/Y/Z (grid_mod.f90:807-820)        */
+  float r_out;             /* R_out (0 = no outer radius)                     */
+  float ion_edge1;         /* ionEdge(1), Ryd                                 */
+  uint32_t flags;          /* MC_FLAG_*                                       */
+} mc_grid_t;
+
+/* One ionising source: one call of energyPacketDriver(iStar, n, ...). */
+typedef struct mc_source {
+  int32_t istar;           /* iStar (1-based), keys the random stream         */
+  int32_t cell[3];         /* starIndeces(iStar,1:3), 1-based                 */
+  int64_t n_packets;       /* n                                               */
+  double delta_e;          /* deltaE(iStar) [1e36 erg/s]                      */
+  float pos[3];            /* starPosition(iStar) [cm]                        */
+  const float *spec_cdf;   /* inSpectrumProbDen(iStar,1:Nnu) (host pointer)   */
+} mc_source_t;
+
+/* Per-call options. */
+typedef struct mc_run_opts {
+  uint64_t seed;           /* Philox key word                                 */
+  uint32_t iteration;      /* nIterateMC; second key word with the star index */
+  int32_t precision;       /* MC_PREC_*                                       */
+  int32_t rng;             /* MC_RNG_*                                        */
+  int32_t recursion_limit; /* recursionLimit (constants_mod.f90:56), 0 = 5000 */
+  int32_t safe_limit;      /* pathSegment safeLimit (:1190), 0 = 500000       */
+  int32_t run_flags;       /* MC_RUN_*                                        */
+  const double *replay;    /* MC_RNG_REPLAY: [n_total * replay_stride] draws in
+                              [0,1), row p = packet p of the concatenated
+                              sources, consumed in the reference draw order   */
+  int64_t replay_stride;   /* draws per packet row                            */
+} mc_run_opts_t;
+
+/* Counters of one call (read back after the transport). */
+typedef struct mc_stats {
+  int64_t crossings;       /* pathSegment loop bodies ending in a full crossing
+                              (:1817) or an interaction (:1517)               */
+  int64_t absorptions;     /* absInt: gas/dust absorptions (:1702, :1803)     */
+  int64_t scatterings;     /* scaInt: dust scatterings (:1720)                */
+  int64_t escaped;         /* packets that reached escapedPackets             */
+  int64_t lines;           /* re-emissions as line packets (:927)             */
+  int64_t trapped;         /* histories that hit recursionLimit (:126)        */
+  int64_t silent_exits;    /* wall-sitting returns without escape (:1276)     */
+  int64_t safe_limit_hits; /* pathSegment safeLimit exhaustion (:2838)        */
+  double qphot;            /* Qphot (:859-861)                                */
+  double kernel_ms;        /* device time of the call's device work (CUDA events
+                              on the library stream: zeroing when requested,
+                              the transport kernel, the counter read-back)    */
+  int32_t error_code;      /* first device-side error (mc_status), 0 if none  */
+  int32_t error_packet;    /* packet index of that error, -1 if none          */
+} mc_stats_t;
+
+/* ---- library ----------------------------------------------------------- */
+
+/* ABI version (MC_ABI_VERSION). */
+int mc_abi_version(void);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *mc_last_error(void);
+
+/* Replaces the whole of energyPacketDriver for nsrc sources
+ * (photon_mod.f90:26-285, the star loop of iteration_mod.f90:474-496).
+ * HOST pointers in, HOST accumulators out: uploads the grid, runs all packets
+ * of all sources on the GPU and adds the estimators into jste / jdif /
+ * escaped.  jdif may be NULL unless MC_FLAG_DEBUG; escaped may be NULL. */
+mc_status mc_transport_run(const mc_grid_t *grid, const mc_source_t *src,
+                           int32_t nsrc, const mc_run_opts_t *opts,
+                           double *jste, double *jdif, double *escaped,
+                           mc_stats_t *stats);
+
+/* ---- resident context: the grid stays in HBM across iterations --------- */
+typedef struct mc_ctx mc_ctx_t;
+
+/* Uploads a grid to the current CUDA device and re-lays it out for the
+ * kernels.  Replaces nothing in the reference (the reference keeps the grid
+ * in host memory); it splits mc_transport_run so a caller that iterates keeps
+ * the grid on the device.  The device estimators start at zero. */
+mc_status mc_ctx_create(const mc_grid_t *grid, mc_ctx_t **out);
+
+/* Re-uploads the per-iteration arrays (opacity, sca_opac, rec_pdf,
+ * total_lines, dust_pdf, g_sca) of an existing context; geometry and sizes
+ * must match the grid the context was created with. */
+mc_status mc_ctx_update(mc_ctx_t *ctx, const mc_grid_t *grid);
+
+/* Zeroes the device estimators (iteration_mod.f90:458-472). */
+mc_status mc_ctx_zero(mc_ctx_t *ctx);
+
+/* Runs the packets of nsrc sources on the resident grid, accumulating into
+ * the device estimators.  spec_cdf pointers of src are host pointers. */
+mc_status mc_ctx_run(mc_ctx_t *ctx, const mc_source_t *src, int32_t nsrc,
+                     const mc_run_opts_t *opts, mc_stats_t *stats);
+
+/* Copies the device estimators into host arrays (adds into them when
+ * accumulate != 0, else overwrites).  Any pointer may be NULL. */
+mc_status mc_ctx_download(mc_ctx_t *ctx, double *jste, double *jdif,
+                          double *escaped, int32_t accumulate);
+
+/* Device pointers of the estimators (Jste, Jdif, escaped), for callers that
+ * consume them on the device (the cell update).  Any out pointer may be NULL. */
+mc_status mc_ctx_device_estimators(mc_ctx_t *ctx, double **jste, double **jdif,
+                                   double **escaped);
+
+void mc_ctx_destroy(mc_ctx_t *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOCASSIN_GPU_H */

@@ -1,0 +1,141 @@
+"""ctypes mirror of include/mocassin_gpu.h and marshalling from a Nebula.
+
+The structs here are byte-for-byte the C-ABI structs; a Fortran caller would
+declare the same layout with ``bind(C)`` derived types.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+MC_OK = 0
+MC_PREC_FP32 = 0
+MC_PREC_FP64 = 1
+MC_RNG_PHILOX = 0
+MC_RNG_REPLAY = 1
+
+STATUS_NAMES = {0: "MC_OK", 1: "MC_ERR_ARG", 2: "MC_ERR_CUDA", 3: "MC_ERR_BOUNDS", 4: "MC_ERR_NAN",
+                5: "MC_ERR_REPLAY", 6: "MC_ERR_TIMEOUT", 7: "MC_ERR_UNSUPPORTED", 8: "MC_ERR_NOMEM",
+                9: "MC_ERR_NO_DEVICE"}
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int32)
+_dp = C.POINTER(C.c_double)
+
+
+class McGrid(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("ncells", C.c_int32),
+                ("nbins", C.c_int32), ("n_angle", C.c_int32),
+                ("x_axis", _fp), ("y_axis", _fp), ("z_axis", _fp), ("active", _ip),
+                ("opacity", _fp), ("sca_opac", _fp), ("rec_pdf", _fp), ("total_lines", _fp),
+                ("dust_pdf", _fp), ("nu_array", _fp), ("g_sca", _fp),
+                ("geo_corr", C.c_float * 3), ("r_out", C.c_float), ("ion_edge1", C.c_float),
+                ("flags", C.c_uint32)]
+
+
+class McSource(C.Structure):
+    _fields_ = [("istar", C.c_int32), ("cell", C.c_int32 * 3), ("n_packets", C.c_int64),
+                ("delta_e", C.c_double), ("pos", C.c_float * 3), ("spec_cdf", _fp)]
+
+
+class McRunOpts(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("iteration", C.c_uint32), ("precision", C.c_int32),
+                ("rng", C.c_int32), ("recursion_limit", C.c_int32), ("safe_limit", C.c_int32),
+                ("run_flags", C.c_int32), ("replay", _dp), ("replay_stride", C.c_int64)]
+
+
+class McStats(C.Structure):
+    _fields_ = [("crossings", C.c_int64), ("absorptions", C.c_int64), ("scatterings", C.c_int64),
+                ("escaped", C.c_int64), ("lines", C.c_int64), ("trapped", C.c_int64),
+                ("silent_exits", C.c_int64), ("safe_limit_hits", C.c_int64), ("qphot", C.c_double),
+                ("kernel_ms", C.c_double), ("error_code", C.c_int32), ("error_packet", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _ptr(a, ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Marshalled:
+    """Keeps the numpy buffers alive while the structs point at them."""
+
+    def __init__(self, neb, n_packets=None, delta_e=None):
+        self.keep = []
+
+        def f(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            self.keep.append(a)
+            return a
+
+        act = np.ascontiguousarray(neb.active, dtype=np.int32)
+        self.keep.append(act)
+        g = McGrid()
+        g.nx, g.ny, g.nz = neb.nx, neb.ny, neb.nz
+        g.ncells, g.nbins, g.n_angle = neb.ncells, neb.nbins, 0
+        g.x_axis = _ptr(f(neb.x_axis), C.c_float)
+        g.y_axis = _ptr(f(neb.y_axis), C.c_float)
+        g.z_axis = _ptr(f(neb.z_axis), C.c_float)
+        g.active = _ptr(act, C.c_int32)
+        g.opacity = _ptr(f(neb.opacity), C.c_float)
+        g.sca_opac = _ptr(f(neb.sca_opac), C.c_float)
+        g.rec_pdf = _ptr(f(neb.rec_pdf), C.c_float)
+        g.total_lines = _ptr(f(neb.total_lines), C.c_float)
+        g.dust_pdf = _ptr(None, C.c_float)
+        g.nu_array = _ptr(f(neb.nu), C.c_float)
+        g.g_sca = _ptr(f(neb.g_sca), C.c_float)
+        for i in range(3):
+            g.geo_corr[i] = float(neb.geo_corr[i])
+        g.r_out = float(neb.r_out)
+        g.ion_edge1 = float(neb.ion_edge1)
+        g.flags = int(neb.flags)
+        self.grid = g
+        ns = len(neb.star_pos)
+        self.sources = (McSource * ns)()
+        for s in range(ns):
+            src = self.sources[s]
+            src.istar = s + 1
+            for i in range(3):
+                src.cell[i] = int(neb.star_cell[s][i])
+                src.pos[i] = float(neb.star_pos[s][i])
+            npk = neb.n_packets[s] if n_packets is None else (n_packets[s] if hasattr(n_packets, "__len__") else n_packets)
+            src.n_packets = int(npk)
+            de = neb.delta_e[s] if delta_e is None else delta_e[s]
+            src.delta_e = float(de)
+            src.spec_cdf = _ptr(f(neb.spec_cdf[s]), C.c_float)
+        self.nsrc = ns
+        self.total_packets = sum(int(self.sources[s].n_packets) for s in range(ns))
+
+
+def make_opts(seed=1, iteration=1, precision=MC_PREC_FP64, replay=None, recursion_limit=0, safe_limit=0,
+              run_flags=0):
+    o = McRunOpts()
+    o.run_flags = run_flags
+    o.seed = seed
+    o.iteration = iteration
+    o.precision = precision
+    o.recursion_limit = recursion_limit
+    o.safe_limit = safe_limit
+    if replay is not None:
+        replay = np.ascontiguousarray(replay, dtype=np.float64)
+        o.rng = MC_RNG_REPLAY
+        o.replay = replay.ctypes.data_as(_dp)
+        o.replay_stride = replay.shape[1]
+        o._keep = replay
+    else:
+        o.rng = MC_RNG_PHILOX
+        o.replay = C.cast(None, _dp)
+        o.replay_stride = 0
+    return o
+
+
+def estimator_arrays(neb):
+    """Zeroed host accumulators: Jste, Jdif (nbins, Nc+1), escaped (nbins+1, Nc+1)."""
+    nc1 = neb.ncells + 1
+    return (np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins + 1, nc1)))

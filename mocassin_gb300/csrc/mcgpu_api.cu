@@ -1,0 +1,452 @@
+// mcgpu_api.cu -- the C-ABI of libmcgpu.so (include/mocassin_gpu.h).
+//
+// Host side of the drop-in for energyPacketDriver (source/photon_mod.f90:26-285):
+// validates the Fortran-layout arrays, keeps a resident copy of the grid in
+// HBM, launches the transport and hands the estimators back.  All errors are
+// returned as mc_status with a message for mc_last_error(); nothing here
+// aborts the process (the reference's "print*; stop" sites become codes).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mocassin_gpu.h"
+#include "mc_device.cuh"
+#include "mc_launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+mc_status set_error(mc_status code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define MC_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return set_error(e_ == cudaErrorMemoryAllocation ? MC_ERR_NOMEM : MC_ERR_CUDA,        \
+                       "%s failed: %s", #call, cudaGetErrorString(e_));                    \
+  } while (0)
+
+// Device buffer owned by a context.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { if (p) cudaFree(p); }
+  cudaError_t alloc(size_t b) {
+    bytes = b;
+    return cudaMalloc(&p, b ? b : 16);
+  }
+  template <typename T> T *as() const { return (T *)p; }
+};
+
+}  // namespace
+
+namespace mcg {
+
+// Transposes a [nb][nc1] cell-fastest CDF into [nc1][nb] rows and applies a
+// running maximum along each row.  Block: 32 cells; tiles of 32 bins go
+// through shared memory so both the read and the write are coalesced.
+__global__ void cdf_transpose_kernel(const float *__restrict__ in, float *__restrict__ out, int nc1, int nb) {
+  __shared__ float tile[32][33];
+  const int c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  float run = -INFINITY;                         // running max of cell c0+tx (owned by ty == 0 lanes)
+  for (int v0 = 0; v0 < nb; v0 += 32) {
+    for (int k = ty; k < 32; k += 8) {
+      const int v = v0 + k, c = c0 + tx;
+      tile[k][tx] = (v < nb && c < nc1) ? in[(long long)v * nc1 + c] : 0.f;
+    }
+    __syncthreads();
+    if (ty == 0) {
+      for (int k = 0; k < 32; ++k) {
+        run = fmaxf(run, tile[k][tx]);
+        tile[k][tx] = run;
+      }
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+      const int c = c0 + k, v = v0 + tx;
+      if (c < nc1 && v < nb) out[(long long)c * nb + v] = tile[tx][k];
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_cdf_transpose(const float *in, float *out, int nc1, int nb, cudaStream_t stream) {
+  dim3 block(32, 8);
+  dim3 grid((nc1 + 31) / 32);
+  cdf_transpose_kernel<<<grid, block, 0, stream>>>(in, out, nc1, nb);
+  return cudaGetLastError();
+}
+
+}  // namespace mcg
+
+struct mc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int nx = 0, ny = 0, nz = 0, nc = 0, nb = 0;
+  uint32_t flags = 0;
+  DBuf xa, ya, za, active, opacity, sca, rec_raw, rec_cdf, dust_raw, dust_cdf, tlines, nu, gsca;
+  DBuf dx32, dy32, dz32, dx64, dy64, dz64;
+  DBuf jste, jdif, esc;
+  DBuf counters, src_cdf, replay;
+  mcg::DevGrid g{};
+};
+
+namespace {
+
+mc_status check_grid(const mc_grid_t *g) {
+  if (!g) return set_error(MC_ERR_ARG, "grid is NULL");
+  if (g->nx < 2 || g->ny < 2 || g->nz < 2)
+    return set_error(MC_ERR_UNSUPPORTED, "nx, ny, nz must be >= 2 (1D grids are not supported): %d %d %d",
+                     g->nx, g->ny, g->nz);
+  if (g->ncells < 0 || g->nbins < 3) return set_error(MC_ERR_ARG, "bad ncells/nbins %d/%d", g->ncells, g->nbins);
+  if (g->n_angle != 0) return set_error(MC_ERR_UNSUPPORTED, "nAngleBins > 0 is not supported");
+  if (!g->x_axis || !g->y_axis || !g->z_axis || !g->active || !g->opacity || !g->nu_array)
+    return set_error(MC_ERR_ARG, "grid axes/active/opacity/nu_array must be non-NULL");
+  const bool gas = g->flags & MC_FLAG_GAS, dust = g->flags & MC_FLAG_DUST;
+  if (!gas && !dust) return set_error(MC_ERR_ARG, "grid has neither gas nor dust");
+  if (gas && (!g->rec_pdf || !g->total_lines)) return set_error(MC_ERR_ARG, "gas grid needs rec_pdf and total_lines");
+  if (dust && !g->sca_opac) return set_error(MC_ERR_ARG, "dust grid needs sca_opac");
+  if (dust && !gas && !g->dust_pdf) return set_error(MC_ERR_ARG, "dust-only grid needs dust_pdf");
+  if (dust && !(g->flags & MC_FLAG_ISOTROPIC) && !g->g_sca)
+    return set_error(MC_ERR_ARG, "anisotropic dust scattering needs g_sca");
+  const int64_t ncell3 = (int64_t)g->nx * g->ny * g->nz;
+  for (int64_t i = 0; i < ncell3; ++i) {
+    const int a = g->active[i];
+    if (a < 0) return set_error(MC_ERR_UNSUPPORTED, "active < 0 (sub-grid pointer) at %lld", (long long)i);
+    if (a > g->ncells) return set_error(MC_ERR_ARG, "active %d exceeds ncells %d", a, g->ncells);
+  }
+  return MC_OK;
+}
+
+template <typename T> void widths(const float *ax, int n, bool sym, std::vector<T> &w) {
+  // photon_mod.f90:1469-1512, divided by 1e15 (the FP32 literal)
+  w.resize(n);
+  for (int p = 1; p <= n; ++p) {
+    T d;
+    auto A = [&](int i) { return (T)ax[i - 1]; };
+    if (p > 1 && p < n) d = std::fabs(A(p + 1) - A(p - 1)) / (T)2;
+    else if (p == 1) d = sym ? std::fabs(A(p + 1) - A(p)) / (T)2 : std::fabs(A(p + 1) - A(p));
+    else d = std::fabs(A(p) - A(p - 1));
+    w[p - 1] = d / (T)1.e15f;
+  }
+}
+
+mc_status upload(DBuf &b, const void *host, size_t bytes, cudaStream_t s) {
+  MC_CUDA(b.alloc(bytes));
+  if (host && bytes) MC_CUDA(cudaMemcpyAsync(b.p, host, bytes, cudaMemcpyHostToDevice, s));
+  return MC_OK;
+}
+
+mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first) {
+  const int nc1 = g->ncells + 1, nb = g->nbins;
+  const size_t plane = (size_t)nc1 * nb * sizeof(float);
+  cudaStream_t s = c->stream;
+  mc_status st;
+  auto put = [&](DBuf &b, const void *h, size_t bytes) -> mc_status {
+    if (first || !b.p) return upload(b, h, bytes, s);
+    if (h) {
+      cudaError_t e = cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
+    }
+    return MC_OK;
+  };
+  if ((st = put(c->opacity, g->opacity, plane))) return st;
+  if (g->sca_opac && (st = put(c->sca, g->sca_opac, plane))) return st;
+  if (g->total_lines && (st = put(c->tlines, g->total_lines, (size_t)nc1 * sizeof(float)))) return st;
+  if (g->g_sca && (st = put(c->gsca, g->g_sca, (size_t)nb * sizeof(float)))) return st;
+  if (g->rec_pdf) {
+    if ((st = put(c->rec_raw, g->rec_pdf, plane))) return st;
+    if (!c->rec_cdf.p) MC_CUDA(c->rec_cdf.alloc(plane));
+    MC_CUDA(mcg::launch_cdf_transpose(c->rec_raw.as<float>(), c->rec_cdf.as<float>(), nc1, nb, s));
+  }
+  if (g->dust_pdf) {
+    if ((st = put(c->dust_raw, g->dust_pdf, plane))) return st;
+    if (!c->dust_cdf.p) MC_CUDA(c->dust_cdf.alloc(plane));
+    MC_CUDA(mcg::launch_cdf_transpose(c->dust_raw.as<float>(), c->dust_cdf.as<float>(), nc1, nb, s));
+  }
+  return MC_OK;
+}
+
+mc_status make_sources(mc_ctx *c, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                       mcg::DevSources &S) {
+  if (nsrc < 1 || nsrc > mcg::kMaxSources)
+    return set_error(MC_ERR_ARG, "nsrc must be 1..%d (got %d)", mcg::kMaxSources, nsrc);
+  std::vector<float> cdfs((size_t)nsrc * c->nb);
+  S.nsrc = nsrc;
+  long long base = 0;
+  for (int i = 0; i < nsrc; ++i) {
+    const mc_source_t &x = src[i];
+    if (!x.spec_cdf) return set_error(MC_ERR_ARG, "source %d has no spec_cdf", i);
+    if (x.n_packets < 0) return set_error(MC_ERR_ARG, "source %d has negative n_packets", i);
+    if (x.cell[0] < 1 || x.cell[0] > c->nx || x.cell[1] < 1 || x.cell[1] > c->ny || x.cell[2] < 1 ||
+        x.cell[2] > c->nz)
+      return set_error(MC_ERR_BOUNDS, "source %d cell (%d,%d,%d) outside the grid", i, x.cell[0], x.cell[1],
+                       x.cell[2]);
+    float run = -INFINITY;  // running max: binary search == getNu2's scan
+    for (int k = 0; k < c->nb; ++k) {
+      run = std::fmax(run, x.spec_cdf[k]);
+      cdfs[(size_t)i * c->nb + k] = run;
+    }
+    mcg::DevSource &d = S.s[i];
+    d.cell[0] = x.cell[0]; d.cell[1] = x.cell[1]; d.cell[2] = x.cell[2];
+    d.pos[0] = x.pos[0]; d.pos[1] = x.pos[1]; d.pos[2] = x.pos[2];
+    d.delta_e = x.delta_e;
+    d.k0 = (uint32_t)o->seed;
+    d.k1 = (uint32_t)(o->seed >> 32) ^ ((o->iteration & 0xFFFFFFu) << 8) ^ ((uint32_t)x.istar & 0xFFu);
+    d.n = x.n_packets;
+    d.base = base;
+    base += x.n_packets;
+  }
+  S.total = base;
+  const size_t bytes = cdfs.size() * sizeof(float);
+  if (c->src_cdf.bytes < bytes) {
+    if (c->src_cdf.p) { cudaFree(c->src_cdf.p); c->src_cdf.p = nullptr; }
+    MC_CUDA(c->src_cdf.alloc(bytes));
+  }
+  MC_CUDA(cudaMemcpyAsync(c->src_cdf.p, cdfs.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+  for (int i = 0; i < nsrc; ++i) S.s[i].cdf = c->src_cdf.as<float>() + (size_t)i * c->nb;
+  return MC_OK;
+}
+
+double kernel_budget_ns() {
+  const char *e = getenv("MC_KERNEL_BUDGET_S");
+  double s = e ? atof(e) : 120.0;
+  if (!(s > 0)) s = 120.0;
+  return s * 1e9;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mc_abi_version(void) { return MC_ABI_VERSION; }
+
+const char *mc_last_error(void) { return g_last_error.c_str(); }
+
+mc_status mc_ctx_create(const mc_grid_t *g, mc_ctx_t **out) {
+  if (!out) return set_error(MC_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  mc_status st = check_grid(g);
+  if (st) return st;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(MC_ERR_NO_DEVICE, "no CUDA device");
+  mc_ctx *c = new mc_ctx();
+  auto fail = [&](mc_status s) { delete c; return s; };
+  if (cudaGetDevice(&c->device) != cudaSuccess) return fail(set_error(MC_ERR_CUDA, "cudaGetDevice failed"));
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
+    return fail(set_error(MC_ERR_CUDA, "stream/event creation failed"));
+  c->nx = g->nx; c->ny = g->ny; c->nz = g->nz; c->nc = g->ncells; c->nb = g->nbins; c->flags = g->flags;
+  const bool sym = g->flags & MC_FLAG_SYMMETRIC_XYZ;
+  const size_t n3 = (size_t)g->nx * g->ny * g->nz;
+  if ((st = upload(c->xa, g->x_axis, g->nx * sizeof(float), c->stream)) ||
+      (st = upload(c->ya, g->y_axis, g->ny * sizeof(float), c->stream)) ||
+      (st = upload(c->za, g->z_axis, g->nz * sizeof(float), c->stream)) ||
+      (st = upload(c->active, g->active, n3 * sizeof(int32_t), c->stream)) ||
+      (st = upload(c->nu, g->nu_array, g->nbins * sizeof(float), c->stream)))
+    return fail(st);
+  std::vector<float> w32;
+  std::vector<double> w64;
+  const float *ax[3] = {g->x_axis, g->y_axis, g->z_axis};
+  const int na[3] = {g->nx, g->ny, g->nz};
+  DBuf *b32[3] = {&c->dx32, &c->dy32, &c->dz32};
+  DBuf *b64[3] = {&c->dx64, &c->dy64, &c->dz64};
+  for (int k = 0; k < 3; ++k) {
+    widths<float>(ax[k], na[k], sym, w32);
+    widths<double>(ax[k], na[k], sym, w64);
+    if ((st = upload(*b32[k], w32.data(), w32.size() * sizeof(float), c->stream))) return fail(st);
+    if ((st = upload(*b64[k], w64.data(), w64.size() * sizeof(double), c->stream))) return fail(st);
+    // the host vectors are reused: finish the copy first
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(set_error(MC_ERR_CUDA, "sync failed"));
+  }
+  if ((st = upload_arrays(c, g, true))) return fail(st);
+  const size_t nj = (size_t)(g->ncells + 1) * g->nbins, ne = (size_t)(g->ncells + 1) * (g->nbins + 1);
+  if (c->jste.alloc(nj * sizeof(double)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "Jste alloc"));
+  if ((g->flags & MC_FLAG_DEBUG) && c->jdif.alloc(nj * sizeof(double)) != cudaSuccess)
+    return fail(set_error(MC_ERR_NOMEM, "Jdif alloc"));
+  if (c->esc.alloc(ne * sizeof(double)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "escaped alloc"));
+  if (c->counters.alloc(sizeof(mcg::DevCounters)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "counters"));
+
+  mcg::DevGrid &d = c->g;
+  d.nx = g->nx; d.ny = g->ny; d.nz = g->nz; d.nc = g->ncells; d.nb = g->nbins;
+  d.xa = c->xa.as<float>(); d.ya = c->ya.as<float>(); d.za = c->za.as<float>();
+  d.active = c->active.as<int32_t>();
+  d.opacity = c->opacity.as<float>();
+  d.sca = c->sca.as<float>();
+  d.rec_cdf = c->rec_cdf.as<float>();
+  d.dust_cdf = c->dust_cdf.as<float>();
+  d.total_lines = c->tlines.as<float>();
+  d.nu = c->nu.as<float>();
+  d.gsca = c->gsca.as<float>();
+  d.dx32 = c->dx32.as<float>(); d.dy32 = c->dy32.as<float>(); d.dz32 = c->dz32.as<float>();
+  d.dx64 = c->dx64.as<double>(); d.dy64 = c->dy64.as<double>(); d.dz64 = c->dz64.as<double>();
+  d.gc[0] = g->geo_corr[0]; d.gc[1] = g->geo_corr[1]; d.gc[2] = g->geo_corr[2];
+  d.rout = g->r_out;
+  d.ion_edge1 = g->ion_edge1;
+  d.flags = g->flags;
+  d.jste = c->jste.as<double>();
+  d.jdif = c->jdif.as<double>();
+  d.esc = c->esc.as<double>();
+  mc_status z = mc_ctx_zero(c);
+  if (z) return fail(z);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return fail(set_error(MC_ERR_CUDA, "upload failed: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = c;
+  return MC_OK;
+}
+
+mc_status mc_ctx_update(mc_ctx_t *c, const mc_grid_t *g) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  mc_status st = check_grid(g);
+  if (st) return st;
+  if (g->nx != c->nx || g->ny != c->ny || g->nz != c->nz || g->ncells != c->nc || g->nbins != c->nb ||
+      g->flags != c->flags)
+    return set_error(MC_ERR_ARG, "grid shape/flags differ from the context's");
+  if ((st = upload_arrays(c, g, false))) return st;
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+mc_status mc_ctx_zero(mc_ctx_t *c) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  MC_CUDA(cudaMemsetAsync(c->jste.p, 0, c->jste.bytes, c->stream));
+  if (c->jdif.p) MC_CUDA(cudaMemsetAsync(c->jdif.p, 0, c->jdif.bytes, c->stream));
+  MC_CUDA(cudaMemsetAsync(c->esc.p, 0, c->esc.bytes, c->stream));
+  return MC_OK;
+}
+
+mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                     mc_stats_t *stats) {
+  if (!c || !src || !o) return set_error(MC_ERR_ARG, "ctx/src/opts is NULL");
+  if (o->precision != MC_PREC_FP32 && o->precision != MC_PREC_FP64)
+    return set_error(MC_ERR_ARG, "precision must be MC_PREC_FP32 or MC_PREC_FP64");
+  if (o->rng != MC_RNG_PHILOX && o->rng != MC_RNG_REPLAY) return set_error(MC_ERR_ARG, "unknown rng");
+  mcg::DevSources S{};
+  mc_status st = make_sources(c, src, nsrc, o, S);
+  if (st) return st;
+  mcg::DevReplay rp{nullptr, 0};
+  if (o->rng == MC_RNG_REPLAY) {
+    if (!o->replay || o->replay_stride <= 0) return set_error(MC_ERR_ARG, "replay needs draws and a stride");
+    const size_t bytes = (size_t)S.total * o->replay_stride * sizeof(double);
+    if (c->replay.bytes < bytes) {
+      if (c->replay.p) { cudaFree(c->replay.p); c->replay.p = nullptr; }
+      MC_CUDA(c->replay.alloc(bytes));
+    }
+    MC_CUDA(cudaMemcpyAsync(c->replay.p, o->replay, bytes, cudaMemcpyHostToDevice, c->stream));
+    rp.draws = c->replay.as<double>();
+    rp.stride = o->replay_stride;
+  }
+  mcg::DevGrid g = c->g;
+  g.recursion_limit = o->recursion_limit > 0 ? o->recursion_limit : 5000;
+  g.safe_limit = o->safe_limit > 0 ? o->safe_limit : 500000;
+  mcg::DevCounters h{};
+  h.error_packet = -1;
+  h.budget_ns = (unsigned long long)kernel_budget_ns();
+  MC_CUDA(cudaEventRecord(c->ev0, c->stream));
+  if (o->run_flags & MC_RUN_ZERO_FIRST) {
+    mc_status z = mc_ctx_zero(c);
+    if (z) return z;
+  }
+  MC_CUDA(cudaMemcpyAsync(c->counters.p, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
+  if (S.total > 0) {
+    cudaError_t e = o->precision == MC_PREC_FP64
+                        ? mcg::launch_plain_fp64(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream)
+                        : mcg::launch_plain_fp32(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "transport launch failed: %s", cudaGetErrorString(e));
+  }
+  MC_CUDA(cudaEventRecord(c->ev1, c->stream));
+  MC_CUDA(cudaMemcpyAsync(&h, c->counters.p, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  if (stats) {
+    stats->crossings = (int64_t)h.crossings;
+    stats->absorptions = (int64_t)h.absorptions;
+    stats->scatterings = (int64_t)h.scatterings;
+    stats->escaped = (int64_t)h.escaped;
+    stats->lines = (int64_t)h.lines;
+    stats->trapped = (int64_t)h.trapped;
+    stats->silent_exits = (int64_t)h.silent;
+    stats->safe_limit_hits = (int64_t)h.safe_hits;
+    stats->qphot = h.qphot;
+    stats->kernel_ms = ms;
+    stats->error_code = h.error_code;
+    stats->error_packet = h.error_packet;
+  }
+  if (h.error_code != 0)
+    return set_error((mc_status)h.error_code, "device error %d in packet %d", h.error_code, h.error_packet);
+  return MC_OK;
+}
+
+mc_status mc_ctx_download(mc_ctx_t *c, double *jste, double *jdif, double *escaped, int32_t accumulate) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  struct Item { double *h; DBuf *d; } items[3] = {{jste, &c->jste}, {jdif, &c->jdif}, {escaped, &c->esc}};
+  for (auto &it : items) {
+    if (!it.h || !it.d->p) continue;
+    const size_t n = it.d->bytes / sizeof(double);
+    if (!accumulate) {
+      MC_CUDA(cudaMemcpyAsync(it.h, it.d->p, it.d->bytes, cudaMemcpyDeviceToHost, c->stream));
+      MC_CUDA(cudaStreamSynchronize(c->stream));
+    } else {
+      std::vector<double> tmp(n);
+      MC_CUDA(cudaMemcpyAsync(tmp.data(), it.d->p, it.d->bytes, cudaMemcpyDeviceToHost, c->stream));
+      MC_CUDA(cudaStreamSynchronize(c->stream));
+      for (size_t i = 0; i < n; ++i) it.h[i] += tmp[i];
+    }
+  }
+  return MC_OK;
+}
+
+mc_status mc_ctx_device_estimators(mc_ctx_t *c, double **jste, double **jdif, double **escaped) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  if (jste) *jste = c->jste.as<double>();
+  if (jdif) *jdif = c->jdif.as<double>();
+  if (escaped) *escaped = c->esc.as<double>();
+  return MC_OK;
+}
+
+void mc_ctx_destroy(mc_ctx_t *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  cudaStream_t s = c->stream;
+  delete c;  // frees the device buffers
+  if (s) cudaStreamDestroy(s);
+}
+
+mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                           double *jste, double *jdif, double *escaped, mc_stats_t *stats) {
+  if (!jste) return set_error(MC_ERR_ARG, "jste is NULL");
+  if (g && (g->flags & MC_FLAG_DEBUG) && !jdif) return set_error(MC_ERR_ARG, "debug grid needs jdif");
+  mc_ctx_t *c = nullptr;
+  mc_status st = mc_ctx_create(g, &c);
+  if (st) return st;
+  st = mc_ctx_run(c, src, nsrc, o, stats);
+  if (st == MC_OK) st = mc_ctx_download(c, jste, jdif, escaped, 1);
+  mc_ctx_destroy(c);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+"""Host-side mirror of mocassin's transport interface over libmcgpu.so.
+
+``energy_packet_driver`` is the call the Fortran ``iterateMC`` makes
+(``call energyPacketDriver(iStar, load, grid(1:nGrids))``,
+source/iteration_mod.f90:488-493): it runs all packets of the given stars and
+adds the path-length estimators into Jste (and escapedPackets).  Errors are
+raised as ``TransportError`` carrying the C-ABI status and message, the
+counterpart of the reference's fatal ``print*; stop`` insanity checks.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+visible, the call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libmcgpu.so")
+
+
+class TransportError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+def library():
+    """Loads libmcgpu.so (built by mocassin_gb300.build); raises if absent."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise TransportError(2, "libmcgpu.so is not built (%s); run mocassin_gb300.build.build()" % LIB_PATH)
+        lib = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        lib.mc_abi_version.restype = C.c_int
+        lib.mc_last_error.restype = C.c_char_p
+        lib.mc_transport_run.restype = C.c_int
+        lib.mc_transport_run.argtypes = [C.POINTER(abi.McGrid), C.POINTER(abi.McSource), C.c_int32,
+                                         C.POINTER(abi.McRunOpts), dp, dp, dp, C.POINTER(abi.McStats)]
+        lib.mc_ctx_create.restype = C.c_int
+        lib.mc_ctx_create.argtypes = [C.POINTER(abi.McGrid), C.POINTER(C.c_void_p)]
+        lib.mc_ctx_update.restype = C.c_int
+        lib.mc_ctx_update.argtypes = [C.c_void_p, C.POINTER(abi.McGrid)]
+        lib.mc_ctx_zero.restype = C.c_int
+        lib.mc_ctx_zero.argtypes = [C.c_void_p]
+        lib.mc_ctx_run.restype = C.c_int
+        lib.mc_ctx_run.argtypes = [C.c_void_p, C.POINTER(abi.McSource), C.c_int32, C.POINTER(abi.McRunOpts),
+                                   C.POINTER(abi.McStats)]
+        lib.mc_ctx_download.restype = C.c_int
+        lib.mc_ctx_download.argtypes = [C.c_void_p, dp, dp, dp, C.c_int32]
+        lib.mc_ctx_device_estimators.restype = C.c_int
+        lib.mc_ctx_device_estimators.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
+        lib.mc_ctx_destroy.restype = None
+        lib.mc_ctx_destroy.argtypes = [C.c_void_p]
+        if lib.mc_abi_version() != 1:
+            raise TransportError(1, "ABI version mismatch")
+        _LIB = lib
+    return _LIB
+
+
+def _check(status):
+    if status != 0:
+        raise TransportError(status, library().mc_last_error().decode())
+
+
+def _dptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None,
+                         jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0):
+    """Runs every packet of every star of ``neb`` through the GPU transport.
+
+    Accumulates into ``jste`` / ``jdif`` / ``escaped`` (created zeroed when not
+    given; shapes ``(nbins, Nc+1)`` and ``(nbins+1, Nc+1)``, i.e. Fortran
+    ``(0:Nc, 1:nbins)`` cell fastest) and returns ``(jste, jdif, escaped,
+    stats)``.
+    """
+    lib = library()
+    m = abi.Marshalled(neb, n_packets=n_packets)
+    prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
+    opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
+                         recursion_limit=recursion_limit, safe_limit=safe_limit)
+    js0, jd0, es0 = abi.estimator_arrays(neb)
+    jste = js0 if jste is None else jste
+    escaped = es0 if escaped is None else escaped
+    if jdif is None and (neb.flags & abi_flag_debug()):
+        jdif = jd0
+    st = abi.McStats()
+    _check(lib.mc_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), _dptr(jste), _dptr(jdif),
+                                _dptr(escaped), C.byref(st)))
+    return jste, jdif, escaped, st.as_dict()
+
+
+def abi_flag_debug():
+    return 1 << 4
+
+
+class TransportContext:
+    """A grid resident in HBM across iterations (mc_ctx_* entry points)."""
+
+    def __init__(self, neb):
+        self.lib = library()
+        self.neb = neb
+        self._m = abi.Marshalled(neb)
+        h = C.c_void_p()
+        _check(self.lib.mc_ctx_create(C.byref(self._m.grid), C.byref(h)))
+        self.handle = h
+
+    def update(self, neb):
+        m = abi.Marshalled(neb)
+        _check(self.lib.mc_ctx_update(self.handle, C.byref(m.grid)))
+        self.neb, self._m = neb, m
+
+    def zero(self):
+        _check(self.lib.mc_ctx_zero(self.handle))
+
+    def run(self, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None, recursion_limit=0,
+            safe_limit=0, zero_first=False):
+        m = abi.Marshalled(self.neb, n_packets=n_packets)
+        prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
+        opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
+                             recursion_limit=recursion_limit, safe_limit=safe_limit,
+                             run_flags=1 if zero_first else 0)
+        st = abi.McStats()
+        _check(self.lib.mc_ctx_run(self.handle, m.sources, m.nsrc, C.byref(opts), C.byref(st)))
+        return st.as_dict()
+
+    def download(self, jste=None, jdif=None, escaped=None, accumulate=False):
+        js0, jd0, es0 = abi.estimator_arrays(self.neb)
+        jste = js0 if jste is None else jste
+        escaped = es0 if escaped is None else escaped
+        _check(self.lib.mc_ctx_download(self.handle, _dptr(jste), _dptr(jdif), _dptr(escaped), int(accumulate)))
+        return jste, jdif, escaped
+
+    def device_estimators(self):
+        j, d, e = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+        _check(self.lib.mc_ctx_device_estimators(self.handle, C.byref(j), C.byref(d), C.byref(e)))
+        addr = lambda p: C.cast(p, C.c_void_p).value or 0
+        return addr(j), addr(d), addr(e)
+
+    def close(self):
+        if self.handle:
+            self.lib.mc_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,141 @@
+"""Parity of the GPU transport (through the C-ABI) with the CPU oracle.
+
+FP64 march: the GPU consumes the same draws as the oracle (Philox streams or
+a replay buffer) and must reproduce every counter exactly and Jste /
+escapedPackets to 1e-12 relative.  FP32 march: stochastic agreement with the
+FP64 oracle within 4 sigma of packet noise.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from mocassin_gb300 import nebula, transport
+from oracle import runner
+from tests import helpers
+from tests.golden import make_golden
+
+pytestmark = pytest.mark.gpu
+
+CASES = nebula.small_cases()
+KEYS = ("crossings", "absorptions", "scatterings", "escaped", "lines", "trapped", "silent_exits")
+GOLDEN = np.load(os.path.join(os.path.dirname(__file__), "golden", "transport_small_fp64.npz"))
+RTOL = 1e-12
+
+
+def _compare(g, o):
+    js, _, es, st = g
+    ojs, _, oes, ost = o
+    for k in KEYS:
+        assert st[k] == ost[k], (k, st[k], ost[k])
+    assert helpers.rel_err(js, ojs) < RTOL
+    assert helpers.rel_err(es, oes) < RTOL
+    assert abs(st["qphot"] - ost["qphot"]) <= 1e-12 * max(abs(ost["qphot"]), 1e-300)
+
+
+@pytest.mark.parametrize("spec", CASES, ids=lambda s: s.name)
+def test_fp64_philox_parity(gpu_lib, spec):
+    neb = nebula.build(spec)
+    g = transport.energy_packet_driver(neb, precision="fp64", seed=17)
+    o = runner.run(neb, precision="fp64", seed=17)
+    _compare(g, o)
+
+
+@pytest.mark.parametrize("spec", CASES[:4], ids=lambda s: s.name)
+def test_fp64_replay_parity(gpu_lib, spec):
+    neb = nebula.build(spec)
+    n = 800
+    draws = np.random.default_rng(99).random((n * len(neb.n_packets), 2048))
+    g = transport.energy_packet_driver(neb, n_packets=n, precision="fp64", replay=draws)
+    o = runner.run(neb, n_packets=n, precision="fp64", replay=draws)
+    _compare(g, o)
+
+
+@pytest.mark.parametrize("spec", CASES, ids=lambda s: s.name)
+def test_fp64_matches_golden(gpu_lib, spec):
+    neb = nebula.build(spec)
+    js, _, es, st = transport.energy_packet_driver(neb, precision="fp64", seed=make_golden.SEED)
+    counts = np.array([st[k] for k in make_golden.KEYS])
+    np.testing.assert_array_equal(counts, GOLDEN[spec.name + "/counts"])
+    np.testing.assert_allclose(js.sum(0), GOLDEN[spec.name + "/j_cell"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(es.sum(1), GOLDEN[spec.name + "/esc_nu"], rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("spec", [CASES[1], CASES[3]], ids=lambda s: s.name)
+def test_fp32_march_agrees_with_fp64_oracle(gpu_lib, spec):
+    """Band-integrated J per cell: GPU FP32 vs oracle FP64 over 8 seeds each;
+    the difference of the means stays within 4 sigma (batch means) for the
+    grid total and for >= 97% of well-sampled cells."""
+    neb = nebula.build(spec)
+    g, o = [], []
+    for seed in range(1, 9):
+        g.append(transport.energy_packet_driver(neb, n_packets=3000, precision="fp32", seed=seed)[0].sum(0))
+        o.append(runner.run(neb, n_packets=3000, precision="fp64", seed=100 + seed)[0].sum(0))
+    g, o = np.array(g), np.array(o)
+    sig = np.sqrt(g.var(0, ddof=1) / len(g) + o.var(0, ddof=1) / len(o))
+    d = np.abs(g.mean(0) - o.mean(0))
+    tot_sig = np.sqrt(g.sum(1).var(ddof=1) / len(g) + o.sum(1).var(ddof=1) / len(o))
+    assert abs(g.sum(1).mean() - o.sum(1).mean()) < 4 * tot_sig
+    ok = sig > 0.02 * o.mean(0).clip(1e-300)
+    frac = float(np.mean(d[ok] < 4 * sig[ok]))
+    assert frac >= 0.97, frac
+
+
+def test_vacuum_known_answer_on_gpu(gpu_lib):
+    spec = nebula.NebulaSpec("vac", 9, 3.0e18, True, [nebula.Star(40000.0, 10.0, (0, 0, 0), 200000)],
+                             nh_median=100.0, r_in=0.0)
+    neb = helpers.vacuum(nebula.build(spec))
+    for prec in ("fp64", "fp32"):
+        js, _, es, st = transport.energy_packet_driver(neb, precision=prec, seed=3)
+        path = (js.sum(0) * helpers.cell_volumes(neb)).sum() / (neb.delta_e[0] * neb.n_packets[0])
+        mu, sd = helpers.octant_path_expectation(3.0e18)
+        assert abs(path - mu) < 4 * sd / np.sqrt(neb.n_packets[0]) + 1e-3 * mu, prec
+        assert st["escaped"] == neb.n_packets[0]
+
+
+def test_zero_packets_and_errors(gpu_lib):
+    neb = nebula.build(CASES[0])
+    js, _, es, st = transport.energy_packet_driver(neb, n_packets=0, precision="fp32")
+    assert st["crossings"] == 0 and js.sum() == 0 and es.sum() == 0
+    bad = nebula.build(CASES[0])
+    bad.star_cell = [(0, 1, 1)]
+    with pytest.raises(transport.TransportError) as e:
+        transport.energy_packet_driver(bad, n_packets=10)
+    assert e.value.status == 3  # MC_ERR_BOUNDS
+    # replay stream too short: MC_ERR_REPLAY, reported by the device, no fault
+    draws = np.full((10, 3), 0.5)
+    with pytest.raises(transport.TransportError) as e:
+        transport.energy_packet_driver(neb, n_packets=10, precision="fp64", replay=draws)
+    assert e.value.status == 5
+    # the library stays usable after device-side errors
+    js, _, es, st = transport.energy_packet_driver(neb, n_packets=100, precision="fp64", seed=1)
+    assert st["escaped"] + st["lines"] == 100
+
+
+def test_watchdog_returns_timeout_status(gpu_lib, monkeypatch):
+    """A kernel budget of ~0 makes every thread give up after its first
+    check: the call returns MC_ERR_TIMEOUT and the context stays usable."""
+    neb = nebula.build(nebula.octant21(20000))
+    monkeypatch.setenv("MC_KERNEL_BUDGET_S", "1e-9")
+    with pytest.raises(transport.TransportError) as e:
+        transport.energy_packet_driver(neb, precision="fp32")
+    assert e.value.status == 6
+    monkeypatch.delenv("MC_KERNEL_BUDGET_S")
+    js, _, es, st = transport.energy_packet_driver(neb, precision="fp32")
+    assert st["escaped"] + st["lines"] == 20000
+
+
+def test_resident_context_accumulates(gpu_lib):
+    neb = nebula.build(CASES[1])
+    ctx = transport.TransportContext(neb)
+    s1 = ctx.run(seed=5, precision="fp64")
+    s2 = ctx.run(seed=6, precision="fp64")
+    js, _, es = ctx.download()
+    a = runner.run(neb, precision="fp64", seed=5)
+    b = runner.run(neb, precision="fp64", seed=6)
+    assert helpers.rel_err(js, a[0] + b[0]) < RTOL
+    ctx.zero()
+    js0, _, _ = ctx.download()
+    assert js0.sum() == 0
+    ctx.close()
+    assert s1["crossings"] == a[3]["crossings"] and s2["crossings"] == b[3]["crossings"]
