@@ -180,9 +180,12 @@ def main():
     ap.add_argument("--config", default="clumpy61")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--packets", type=int, default=0, help="override packets per step")
+    ap.add_argument("--grid", type=int, default=0, help="override the grid size n (odd for full grids)")
     ap.add_argument("--ref-packets", type=int, default=200000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--form", default="wave", choices=["wave", "plain"])
+    ap.add_argument("--plain-steps", type=int, default=2)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -201,12 +204,14 @@ def main():
     spec = workload(args.config)
     if args.packets:
         spec.stars[0].n_packets = args.packets
+    if args.grid:
+        spec.n = args.grid
     neb = nebula.build(spec)
     npk = sum(neb.n_packets)
 
     ctx = transport.TransportContext(neb)
     for w in range(args.warmup):
-        ctx.run(seed=1000 + w, iteration=1, precision=args.precision, zero_first=True)
+        ctx.run(seed=1000 + w, iteration=1, precision=args.precision, zero_first=True, form=args.form)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -217,7 +222,8 @@ def main():
     # synchronises that stream before returning
     stats = []
     for k in range(args.steps):
-        stats.append(ctx.run(seed=1 + rank * 1000003 + k, iteration=1, precision=args.precision, zero_first=True))
+        stats.append(ctx.run(seed=1 + rank * 1000003 + k, iteration=1, precision=args.precision, zero_first=True,
+                             form=args.form))
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = np.array([s["kernel_ms"] for s in stats])
@@ -232,6 +238,17 @@ def main():
     else:
         cross_all = float(cross)
     value = cross_all / t_dev
+    march_ms = np.array([s["march_ms"] for s in stats])
+    plain = None
+    if args.form == "wave" and args.plain_steps > 0:
+        ctx.run(seed=999, iteration=1, precision=args.precision, zero_first=True, form="plain")
+        ps = [ctx.run(seed=2 + k, iteration=1, precision=args.precision, zero_first=True, form="plain")
+              for k in range(args.plain_steps)]
+        pms = np.array([s["kernel_ms"] for s in ps])
+        pc = sum(s["crossings"] for s in ps)
+        plain = {"value": pc / (pms.sum() / 1e3), "unit": UNIT, "ms_per_step": float(pms.mean()),
+                 "steps": args.plain_steps, "kernel": "transport_plain_kernel<float>",
+                 "roofline_frac": pc * BYTES_PER_CROSSING / (pms.sum() / 1e3) / 1e9 / measured_peak()[0]}
     ctx.close()
 
     # e2e: the drop-in call with host (pinned) buffers, copies inside the timed region
@@ -266,7 +283,7 @@ def main():
     e2e_t, e2e_c = 0.0, 0
     for k in range(args.e2e_steps + 1):
         opts = abi.make_opts(seed=77 + k, iteration=1, precision=abi.MC_PREC_FP32 if args.precision == "fp32"
-                             else abi.MC_PREC_FP64)
+                             else abi.MC_PREC_FP64, run_flags=abi.MC_RUN_FORM_PLAIN if args.form == "plain" else 0)
         st = abi.McStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -279,17 +296,19 @@ def main():
         if k > 0:  # first call is a warm-up
             e2e_t += dt
             e2e_c += st.crossings
-    e2e = {"value": e2e_c / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+    e2e = {"value": e2e_c / e2e_t if e2e_t > 0 else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "call": "mc_transport_run (host pinned buffers; includes device allocation, upload, CDF re-layout, "
                    "transport, download)"}
 
     peak, peak_kind = measured_peak()
-    achieved = cross / (t_dev if ws == 1 else float(step_ms.sum()) / 1e3) * BYTES_PER_CROSSING / 1e9
+    # dominant kernel: the march (its own CUDA events on the library stream)
+    achieved = cross / (float(march_ms.sum()) / 1e3) * BYTES_PER_CROSSING / 1e9
     tpc = traffic_per_crossing()
     per_launch_cross = cross / max(len(stats), 1)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (tpc * per_launch_cross) if tpc else None,
-            "kernel": "transport_plain_kernel<float>", "peak_kind": peak_kind + " hbm_gbs (copy)",
+            "kernel": "wave_march_kernel<float,true>" if args.form == "wave" else "transport_plain_kernel<float>",
+            "kernel_ms_per_launch": float(march_ms.mean()), "peak_kind": peak_kind + " hbm_gbs (copy)",
             "algorithmic_bytes_per_crossing": BYTES_PER_CROSSING}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(step_ms.mean()), "higher_is_better": True,
@@ -297,11 +316,14 @@ def main():
             "data": "synthetic",
             "config": {"workload": neb.spec.name, "grid": "%d^3" % neb.nx, "cells": neb.ncells, "nbins": neb.nbins,
                        "packets_per_step": npk, "crossings_per_step": per_launch_cross,
-                       "march": args.precision, "estimators": "f64",
+                       "march": args.precision, "estimators": "f64", "form": args.form,
                        "l2": "inputs larger than L2 (opacity %.0f MB, Jste %.0f MB)"
                              % (neb.opacity.nbytes / 1e6, neb.opacity.size * 8 / 1e6),
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
-            "roofline": roof, "e2e": e2e, "gpu_launches": len(stats), "clocks": clk}
+            "roofline": roof, "e2e": e2e, "gpu_launches": len(stats) * (4 if args.form == "wave" else 1),
+            "clocks": clk}
+    if plain:
+        line["plain_form"] = plain
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(neb)
     if rank == 0:

@@ -75,6 +75,8 @@ typedef enum mc_status {
 /* Run flags (mc_run_opts_t.run_flags). */
 #define MC_RUN_ZERO_FIRST 1 /* zero the device estimators inside the call, before
                                the transport (iteration_mod.f90:458-472)      */
+#define MC_RUN_FORM_PLAIN 2 /* one thread per packet history (the plain form)
+                               instead of the frequency-sorted persistent march */
 
 /* Read-only description of one (mother) grid for one iteration.  All
  * pointers are HOST pointers owned by the caller; they are read during the
@@ -143,6 +145,8 @@ typedef struct mc_stats {
                               the transport kernel, the counter read-back)    */
   int32_t error_code;      /* first device-side error (mc_status), 0 if none  */
   int32_t error_packet;    /* packet index of that error, -1 if none          */
+  double march_ms;         /* device time of the march kernel(s) alone        */
+  int64_t rounds;          /* march rounds (re-emission generations) run      */
 } mc_stats_t;
 
 /* ---- library ----------------------------------------------------------- */

@@ -52,7 +52,7 @@ def _stale(target, deps):
 def build(verbose=False, force=False):
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(OBJDIR, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".inc"))]
     headers.append(os.path.join(os.path.dirname(ROOT), "include", "mocassin_gpu.h"))
     jobs, objs = [], []
     for src, extra in UNITS:

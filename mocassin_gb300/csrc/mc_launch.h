@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "mc_device.cuh"
+#include "wave_types.cuh"
 
 namespace mcg {
 
@@ -14,6 +15,27 @@ cudaError_t launch_plain_fp32(const DevGrid &g, const DevSources &s, const DevRe
                               DevCounters *cnt, int num_sms, cudaStream_t stream);
 cudaError_t launch_plain_fp64(const DevGrid &g, const DevSources &s, const DevReplay &rp,
                               DevCounters *cnt, int num_sms, cudaStream_t stream);
+
+// Chosen form (wavefront rounds), per precision: the frequency sampling of
+// round 0 (stellar) and of later rounds (re-emission), the emission of the
+// sorted queue, and the persistent march.
+cudaError_t launch_wave_sample_stellar_fp32(const WaveLaunch &L);
+cudaError_t launch_wave_sample_stellar_fp64(const WaveLaunch &L);
+cudaError_t launch_wave_sample_reemit_fp32(const WaveLaunch &L, unsigned int n_abs);
+cudaError_t launch_wave_sample_reemit_fp64(const WaveLaunch &L, unsigned int n_abs);
+cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round);
+cudaError_t launch_wave_emit_fp64(const WaveLaunch &L, int round);
+cudaError_t launch_wave_march_fp32(const WaveLaunch &L);
+cudaError_t launch_wave_march_fp64(const WaveLaunch &L);
+
+// Scan of the per-bin counts and scatter of the round's n entries into the
+// frequency-sorted queue; fold of march-indexed estimators into rows;
+// expansion of a cell-fastest array into march order (non-identity grids).
+cudaError_t launch_wave_sort(const WaveLaunch &L, unsigned int n);
+cudaError_t launch_wave_fold(const double *src, double *dst, const int32_t *lin2cell, long long ncell3, int nc1,
+                             int nb, cudaStream_t stream);
+cudaError_t launch_wave_expand(const float *src, float *dst, const int32_t *lin2cell, long long ncell3, int nc1,
+                               int nb, cudaStream_t stream);
 
 // Re-layout of the emission CDF rows: [nb][nc+1] (cell fastest) ->
 // [nc+1][nb] (one row per cell) with a running maximum along each row.

@@ -17,6 +17,7 @@
 #include "../../include/mocassin_gpu.h"
 #include "mc_device.cuh"
 #include "mc_launch.h"
+#include "wave_types.cuh"
 
 namespace {
 
@@ -88,6 +89,8 @@ __global__ void cdf_transpose_kernel(const float *__restrict__ in, float *__rest
   }
 }
 
+#include "wave_util.inc"
+
 cudaError_t launch_cdf_transpose(const float *in, float *out, int nc1, int nb, cudaStream_t stream) {
   dim3 block(32, 8);
   dim3 grid((nc1 + 31) / 32);
@@ -108,6 +111,17 @@ struct mc_ctx {
   DBuf dx32, dy32, dz32, dx64, dy64, dz64;
   DBuf jste, jdif, esc;
   DBuf counters, src_cdf, replay;
+  // chosen form: march-indexed views and the sorted packet queue
+  int identity = 1;
+  long long ncell3 = 0;
+  DBuf lin2cell, opac_m, sca_m, jste_m, jdif_m, bins;
+  DBuf s_nu, s_words, queue, q_id, q_cell, q_words, q_meta, q_origin, q_r, q_v, q_pass;
+  DBuf a_id, a_cell, a_words, a_run, a_r;
+  size_t queue_cap = 0;
+  int refill_min = 8;
+  int inner_steps = 4;
+  int rounds = 0;
+  cudaEvent_t evm0 = nullptr, evm1 = nullptr;
   mcg::DevGrid g{};
 };
 
@@ -172,6 +186,17 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first) {
   };
   if ((st = put(c->opacity, g->opacity, plane))) return st;
   if (g->sca_opac && (st = put(c->sca, g->sca_opac, plane))) return st;
+  if (!c->identity) {
+    const size_t mplane = (size_t)c->ncell3 * nb * sizeof(float);
+    if (!c->opac_m.p) MC_CUDA(c->opac_m.alloc(mplane));
+    MC_CUDA(mcg::launch_wave_expand(c->opacity.as<float>(), c->opac_m.as<float>(), c->lin2cell.as<int32_t>(),
+                                    c->ncell3, nc1, nb, s));
+    if (g->sca_opac) {
+      if (!c->sca_m.p) MC_CUDA(c->sca_m.alloc(mplane));
+      MC_CUDA(mcg::launch_wave_expand(c->sca.as<float>(), c->sca_m.as<float>(), c->lin2cell.as<int32_t>(),
+                                      c->ncell3, nc1, nb, s));
+    }
+  }
   if (g->total_lines && (st = put(c->tlines, g->total_lines, (size_t)nc1 * sizeof(float)))) return st;
   if (g->g_sca && (st = put(c->gsca, g->g_sca, (size_t)nb * sizeof(float)))) return st;
   if (g->rec_pdf) {
@@ -254,6 +279,8 @@ mc_status mc_ctx_create(const mc_grid_t *g, mc_ctx_t **out) {
   auto fail = [&](mc_status s) { delete c; return s; };
   if (cudaGetDevice(&c->device) != cudaSuccess) return fail(set_error(MC_ERR_CUDA, "cudaGetDevice failed"));
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (const char *rm = getenv("MC_REFILL_MIN")) c->refill_min = atoi(rm) > 0 ? atoi(rm) : 8;
+  if (const char *is = getenv("MC_INNER_STEPS")) c->inner_steps = atoi(is) > 0 ? atoi(is) : 4;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
     return fail(set_error(MC_ERR_CUDA, "stream/event creation failed"));
@@ -280,12 +307,38 @@ mc_status mc_ctx_create(const mc_grid_t *g, mc_ctx_t **out) {
     // the host vectors are reused: finish the copy first
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(set_error(MC_ERR_CUDA, "sync failed"));
   }
+  {
+    // march order lin = (z-1) + nz*((y-1) + ny*(x-1)) -> active value
+    c->ncell3 = (long long)g->nx * g->ny * g->nz;
+    std::vector<int32_t> l2c((size_t)c->ncell3);
+    c->identity = 1;
+    for (int x = 1; x <= g->nx; ++x)
+      for (int y = 1; y <= g->ny; ++y)
+        for (int z = 1; z <= g->nz; ++z) {
+          const long long lin = (z - 1) + (long long)g->nz * ((y - 1) + (long long)g->ny * (x - 1));
+          const int a = g->active[(x - 1) + (long long)g->nx * ((y - 1) + (long long)g->ny * (z - 1))];
+          l2c[lin] = a;
+          if (a != lin + 1) c->identity = 0;
+        }
+    if ((st = upload(c->lin2cell, l2c.data(), l2c.size() * sizeof(int32_t), c->stream))) return fail(st);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(set_error(MC_ERR_CUDA, "sync failed"));
+    if (cudaEventCreate(&c->evm0) != cudaSuccess || cudaEventCreate(&c->evm1) != cudaSuccess)
+      return fail(set_error(MC_ERR_CUDA, "event creation failed"));
+    if (c->bins.alloc((size_t)g->nbins * 2 * sizeof(unsigned int) + 32) != cudaSuccess)
+      return fail(set_error(MC_ERR_NOMEM, "bins"));
+  }
   if ((st = upload_arrays(c, g, true))) return fail(st);
   const size_t nj = (size_t)(g->ncells + 1) * g->nbins, ne = (size_t)(g->ncells + 1) * (g->nbins + 1);
   if (c->jste.alloc(nj * sizeof(double)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "Jste alloc"));
   if ((g->flags & MC_FLAG_DEBUG) && c->jdif.alloc(nj * sizeof(double)) != cudaSuccess)
     return fail(set_error(MC_ERR_NOMEM, "Jdif alloc"));
   if (c->esc.alloc(ne * sizeof(double)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "escaped alloc"));
+  if (!c->identity) {
+    const size_t nm = (size_t)c->ncell3 * g->nbins * sizeof(double);
+    if (c->jste_m.alloc(nm) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "march Jste alloc"));
+    if ((g->flags & MC_FLAG_DEBUG) && c->jdif_m.alloc(nm) != cudaSuccess)
+      return fail(set_error(MC_ERR_NOMEM, "march Jdif alloc"));
+  }
   if (c->counters.alloc(sizeof(mcg::DevCounters)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "counters"));
 
   mcg::DevGrid &d = c->g;
@@ -336,6 +389,120 @@ mc_status mc_ctx_zero(mc_ctx_t *c) {
   return MC_OK;
 }
 
+namespace {
+
+mc_status wave_buffers(mc_ctx_t *c, size_t n) {
+  if (n <= c->queue_cap) return MC_OK;
+  struct B { DBuf *b; size_t per; } bs[] = {
+      {&c->s_nu, 2},     {&c->s_words, 4}, {&c->queue, 4},   {&c->q_id, 4},     {&c->q_cell, 4},
+      {&c->q_words, 4},  {&c->q_meta, 4},  {&c->q_origin, 4}, {&c->q_r, 24},    {&c->q_v, 24},
+      {&c->q_pass, 8},   {&c->a_id, 4},    {&c->a_cell, 4},  {&c->a_words, 4},  {&c->a_run, 2},
+      {&c->a_r, 24}};
+  for (auto &x : bs)
+    if (x.b->p) { cudaFree(x.b->p); x.b->p = nullptr; x.b->bytes = 0; }
+  for (auto &x : bs) MC_CUDA(x.b->alloc(n * x.per));
+  c->queue_cap = n;
+  return MC_OK;
+}
+
+mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S, const mcg::DevReplay &rp,
+                   int precision, float *march_ms, int *rounds_out) {
+  if (S.total > 0xFFFFFFFFll) return set_error(MC_ERR_ARG, "more than 2^32-1 packets in one call");
+  if (g.nb > 0xFFFF) return set_error(MC_ERR_UNSUPPORTED, "nbins above 65535");
+  if (c->nx > 1023 || c->ny > 1023 || c->nz > 1023) return set_error(MC_ERR_UNSUPPORTED, "grid axes above 1023");
+  mc_status st = wave_buffers(c, (size_t)S.total);
+  if (st) return st;
+  mcg::WaveLaunch L{};
+  L.g = g;
+  L.S = S;
+  L.rp = rp;
+  L.cnt = c->counters.as<mcg::DevCounters>();
+  L.num_sms = c->num_sms;
+  L.stream = c->stream;
+  mcg::WaveGrid &w = L.w;
+  w.identity = c->identity;
+  if (c->identity) {
+    w.opac = c->opacity.as<float>();
+    w.sca = c->sca.as<float>();
+    w.jste = c->jste.as<double>();
+    w.jdif = c->jdif.as<double>();
+    w.S = c->nc + 1;
+    w.off = 1;
+  } else {
+    w.opac = c->opac_m.as<float>();
+    w.sca = c->sca_m.as<float>();
+    w.jste = c->jste_m.as<double>();
+    w.jdif = c->jdif_m.as<double>();
+    w.S = c->ncell3;
+    w.off = 0;
+    MC_CUDA(cudaMemsetAsync(c->jste_m.p, 0, c->jste_m.bytes, c->stream));
+    if (c->jdif_m.p) MC_CUDA(cudaMemsetAsync(c->jdif_m.p, 0, c->jdif_m.bytes, c->stream));
+  }
+  w.lin2cell = c->lin2cell.as<int32_t>();
+  w.refill_min = c->refill_min;
+  w.inner_steps = c->inner_steps;
+  w.s_nu = c->s_nu.as<uint16_t>();
+  w.s_words = c->s_words.as<uint32_t>();
+  w.bin_count = c->bins.as<unsigned int>();
+  w.bin_cursor = w.bin_count + c->nb;
+  w.qhead = (unsigned long long *)(((uintptr_t)(w.bin_cursor + c->nb) + 7) & ~(uintptr_t)7);
+  w.a_count = (unsigned int *)(w.qhead + 1);
+  w.queue = c->queue.as<uint32_t>();
+  w.q_id = c->q_id.as<uint32_t>();
+  w.q_cell = c->q_cell.as<uint32_t>();
+  w.q_words = c->q_words.as<uint32_t>();
+  w.q_meta = c->q_meta.as<uint32_t>();
+  w.q_origin = c->q_origin.as<int32_t>();
+  w.q_r = c->q_r.p;
+  w.q_v = c->q_v.p;
+  w.q_pass = c->q_pass.p;
+  w.a_id = c->a_id.as<uint32_t>();
+  w.a_cell = c->a_cell.as<uint32_t>();
+  w.a_words = c->a_words.as<uint32_t>();
+  w.a_run = c->a_run.as<uint16_t>();
+  w.a_r = c->a_r.p;
+  const bool f64 = precision == MC_PREC_FP64;
+  unsigned int n_abs = 0;
+  float total_ms = 0.f;
+  int round = 0;
+  for (;; ++round) {
+    MC_CUDA(cudaMemsetAsync(c->bins.p, 0, (size_t)c->nb * 2 * sizeof(unsigned int), c->stream));
+    cudaError_t e;
+    if (round == 0) e = f64 ? mcg::launch_wave_sample_stellar_fp64(L) : mcg::launch_wave_sample_stellar_fp32(L);
+    else e = f64 ? mcg::launch_wave_sample_reemit_fp64(L, n_abs) : mcg::launch_wave_sample_reemit_fp32(L, n_abs);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "sample launch failed: %s", cudaGetErrorString(e));
+    MC_CUDA(mcg::launch_wave_sort(L, round == 0 ? (unsigned int)S.total : n_abs));
+    e = f64 ? mcg::launch_wave_emit_fp64(L, round) : mcg::launch_wave_emit_fp32(L, round);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "emit launch failed: %s", cudaGetErrorString(e));
+    MC_CUDA(cudaEventRecord(c->evm0, c->stream));
+    e = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "march launch failed: %s", cudaGetErrorString(e));
+    MC_CUDA(cudaEventRecord(c->evm1, c->stream));
+    struct { unsigned int a_count; int err; } hb{};
+    MC_CUDA(cudaMemcpyAsync(&hb.a_count, w.a_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    MC_CUDA(cudaMemcpyAsync(&hb.err, &L.cnt->error_code, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MC_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->evm0, c->evm1);
+    total_ms += ms;
+    n_abs = hb.a_count;
+    if (n_abs == 0 || hb.err != 0) break;
+    if (round > g.recursion_limit + 1) return set_error(MC_ERR_BOUNDS, "re-emission rounds exceeded recursionLimit");
+  }
+  if (!c->identity) {
+    MC_CUDA(mcg::launch_wave_fold(c->jste_m.as<double>(), c->jste.as<double>(), w.lin2cell, c->ncell3, c->nc + 1,
+                                  c->nb, c->stream));
+    if (c->jdif_m.p)
+      MC_CUDA(mcg::launch_wave_fold(c->jdif_m.as<double>(), c->jdif.as<double>(), w.lin2cell, c->ncell3,
+                                    c->nc + 1, c->nb, c->stream));
+  }
+  *march_ms = total_ms;
+  *rounds_out = round + 1;
+  return MC_OK;
+}
+
+}  // namespace
+
 mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
                      mc_stats_t *stats) {
   if (!c || !src || !o) return set_error(MC_ERR_ARG, "ctx/src/opts is NULL");
@@ -369,17 +536,32 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
     if (z) return z;
   }
   MC_CUDA(cudaMemcpyAsync(c->counters.p, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
+  const bool plain = o->run_flags & MC_RUN_FORM_PLAIN;
+  float wave_ms = 0.f;
   if (S.total > 0) {
-    cudaError_t e = o->precision == MC_PREC_FP64
-                        ? mcg::launch_plain_fp64(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream)
-                        : mcg::launch_plain_fp32(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream);
-    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "transport launch failed: %s", cudaGetErrorString(e));
+    if (plain) {
+      MC_CUDA(cudaEventRecord(c->evm0, c->stream));
+      cudaError_t e = o->precision == MC_PREC_FP64
+                          ? mcg::launch_plain_fp64(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream)
+                          : mcg::launch_plain_fp32(g, S, rp, c->counters.as<mcg::DevCounters>(), c->num_sms, c->stream);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "transport launch failed: %s", cudaGetErrorString(e));
+      MC_CUDA(cudaEventRecord(c->evm1, c->stream));
+    } else {
+      mc_status ws = run_wave(c, g, S, rp, o->precision, &wave_ms, &c->rounds);
+      if (ws) return ws;
+    }
+  } else {
+    MC_CUDA(cudaEventRecord(c->evm0, c->stream));
+    MC_CUDA(cudaEventRecord(c->evm1, c->stream));
   }
   MC_CUDA(cudaEventRecord(c->ev1, c->stream));
   MC_CUDA(cudaMemcpyAsync(&h, c->counters.p, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+
   MC_CUDA(cudaStreamSynchronize(c->stream));
-  float ms = 0.f;
+  float ms = 0.f, mms = 0.f;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  if (plain || S.total == 0) cudaEventElapsedTime(&mms, c->evm0, c->evm1);
+  else mms = wave_ms;
   if (stats) {
     stats->crossings = (int64_t)h.crossings;
     stats->absorptions = (int64_t)h.absorptions;
@@ -393,6 +575,8 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
     stats->kernel_ms = ms;
     stats->error_code = h.error_code;
     stats->error_packet = h.error_packet;
+    stats->march_ms = mms;
+    stats->rounds = plain ? 1 : c->rounds;
   }
   if (h.error_code != 0)
     return set_error((mc_status)h.error_code, "device error %d in packet %d", h.error_code, h.error_packet);
@@ -431,6 +615,8 @@ void mc_ctx_destroy(mc_ctx_t *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->evm0) cudaEventDestroy(c->evm0);
+  if (c->evm1) cudaEventDestroy(c->evm1);
   cudaStream_t s = c->stream;
   delete c;  // frees the device buffers
   if (s) cudaStreamDestroy(s);

@@ -18,3 +18,62 @@ cudaError_t launch_plain_fp32(const DevGrid &g, const DevSources &s, const DevRe
 }
 
 }  // namespace mcg
+
+#include "transport_wave.cuh"
+
+namespace mcg {
+
+static const int kGridPerSm = 4;
+
+template <bool Replay> static cudaError_t sample_stellar_impl(const WaveLaunch &L) {
+  auto k = wave_sample_stellar_kernel<float, Replay>;
+  const size_t sh = (size_t)L.g.nb * (1 + L.S.nsrc) * sizeof(unsigned int);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  if (e != cudaSuccess) return e;
+  k<<<L.num_sms * kGridPerSm, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, L.cnt);
+  return cudaGetLastError();
+}
+cudaError_t launch_wave_sample_stellar_fp32(const WaveLaunch &L) {
+  return L.rp.draws ? sample_stellar_impl<true>(L) : sample_stellar_impl<false>(L);
+}
+
+template <bool Replay> static cudaError_t sample_reemit_impl(const WaveLaunch &L, unsigned int n) {
+  auto k = wave_sample_reemit_kernel<float, Replay>;
+  const size_t sh = (size_t)L.g.nb * sizeof(unsigned int);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  if (e != cudaSuccess) return e;
+  const unsigned int blocks = (unsigned int)min((long long)L.num_sms * kGridPerSm, (n + 255ll) / 256 + 1);
+  k<<<blocks, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, n, L.cnt);
+  return cudaGetLastError();
+}
+cudaError_t launch_wave_sample_reemit_fp32(const WaveLaunch &L, unsigned int n) {
+  return L.rp.draws ? sample_reemit_impl<true>(L, n) : sample_reemit_impl<false>(L, n);
+}
+
+template <bool Replay> static cudaError_t emit_impl(const WaveLaunch &L, int round) {
+  wave_emit_kernel<float, Replay><<<L.num_sms * kGridPerSm, 256, 0, L.stream>>>(L.g, L.S, L.rp, L.w, round, L.cnt);
+  return cudaGetLastError();
+}
+cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round) {
+  return L.rp.draws ? emit_impl<true>(L, round) : emit_impl<false>(L, round);
+}
+
+template <bool Dust, bool Replay> static cudaError_t march_impl(const WaveLaunch &L) {
+  auto k = wave_march_kernel<float, true, Dust, Replay>;
+  const size_t sh = march_smem_bytes<float>(L.g.nx, L.g.ny, L.g.nz, 256 / 32);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, sh);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  k<<<L.num_sms * per_sm, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, L.cnt);
+  return cudaGetLastError();
+}
+cudaError_t launch_wave_march_fp32(const WaveLaunch &L) {
+  const bool dust = L.g.flags & MC_FLAG_DUST;
+  if (L.rp.draws) return dust ? march_impl<true, true>(L) : march_impl<false, true>(L);
+  return dust ? march_impl<true, false>(L) : march_impl<false, false>(L);
+}
+
+}  // namespace mcg

@@ -425,6 +425,7 @@ template <typename Real> struct History {
   }
 
   __device__ void run(long long p) {
+    if (global_ns() - t0 > cnt->budget_ns) { fail(MC_ERR_TIMEOUT); return; }
     int ptype = STELLAR;
     R3<Real> position{(Real)src.pos[0], (Real)src.pos[1], (Real)src.pos[2]};
     int cell[3] = {src.cell[0], src.cell[1], src.cell[2]};

@@ -72,20 +72,27 @@ def _dptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _flags(form, zero_first=False):
+    if form not in ("wave", "plain"):
+        raise ValueError("form must be 'wave' or 'plain'")
+    return (abi.MC_RUN_FORM_PLAIN if form == "plain" else 0) | (abi.MC_RUN_ZERO_FIRST if zero_first else 0)
+
+
 def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None,
-                         jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0):
+                         jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0, form="wave"):
     """Runs every packet of every star of ``neb`` through the GPU transport.
 
     Accumulates into ``jste`` / ``jdif`` / ``escaped`` (created zeroed when not
     given; shapes ``(nbins, Nc+1)`` and ``(nbins+1, Nc+1)``, i.e. Fortran
     ``(0:Nc, 1:nbins)`` cell fastest) and returns ``(jste, jdif, escaped,
-    stats)``.
+    stats)``.  ``form`` selects the frequency-sorted persistent march
+    ("wave", the default) or one thread per history ("plain").
     """
     lib = library()
     m = abi.Marshalled(neb, n_packets=n_packets)
     prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
     opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
-                         recursion_limit=recursion_limit, safe_limit=safe_limit)
+                         recursion_limit=recursion_limit, safe_limit=safe_limit, run_flags=_flags(form))
     js0, jd0, es0 = abi.estimator_arrays(neb)
     jste = js0 if jste is None else jste
     escaped = es0 if escaped is None else escaped
@@ -121,12 +128,12 @@ class TransportContext:
         _check(self.lib.mc_ctx_zero(self.handle))
 
     def run(self, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None, recursion_limit=0,
-            safe_limit=0, zero_first=False):
+            safe_limit=0, zero_first=False, form="wave"):
         m = abi.Marshalled(self.neb, n_packets=n_packets)
         prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
         opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
                              recursion_limit=recursion_limit, safe_limit=safe_limit,
-                             run_flags=1 if zero_first else 0)
+                             run_flags=_flags(form, zero_first))
         st = abi.McStats()
         _check(self.lib.mc_ctx_run(self.handle, m.sources, m.nsrc, C.byref(opts), C.byref(st)))
         return st.as_dict()

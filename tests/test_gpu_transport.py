@@ -33,43 +33,51 @@ def _compare(g, o):
     assert abs(st["qphot"] - ost["qphot"]) <= 1e-12 * max(abs(ost["qphot"]), 1e-300)
 
 
+FORMS = ("wave", "plain")
+
+
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("spec", CASES, ids=lambda s: s.name)
-def test_fp64_philox_parity(gpu_lib, spec):
+def test_fp64_philox_parity(gpu_lib, spec, form):
     neb = nebula.build(spec)
-    g = transport.energy_packet_driver(neb, precision="fp64", seed=17)
+    g = transport.energy_packet_driver(neb, precision="fp64", seed=17, form=form)
     o = runner.run(neb, precision="fp64", seed=17)
     _compare(g, o)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("spec", CASES[:4], ids=lambda s: s.name)
-def test_fp64_replay_parity(gpu_lib, spec):
+def test_fp64_replay_parity(gpu_lib, spec, form):
     neb = nebula.build(spec)
     n = 800
     draws = np.random.default_rng(99).random((n * len(neb.n_packets), 2048))
-    g = transport.energy_packet_driver(neb, n_packets=n, precision="fp64", replay=draws)
+    g = transport.energy_packet_driver(neb, n_packets=n, precision="fp64", replay=draws, form=form)
     o = runner.run(neb, n_packets=n, precision="fp64", replay=draws)
     _compare(g, o)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("spec", CASES, ids=lambda s: s.name)
-def test_fp64_matches_golden(gpu_lib, spec):
+def test_fp64_matches_golden(gpu_lib, spec, form):
     neb = nebula.build(spec)
-    js, _, es, st = transport.energy_packet_driver(neb, precision="fp64", seed=make_golden.SEED)
+    js, _, es, st = transport.energy_packet_driver(neb, precision="fp64", seed=make_golden.SEED, form=form)
     counts = np.array([st[k] for k in make_golden.KEYS])
     np.testing.assert_array_equal(counts, GOLDEN[spec.name + "/counts"])
     np.testing.assert_allclose(js.sum(0), GOLDEN[spec.name + "/j_cell"], rtol=RTOL, atol=0)
     np.testing.assert_allclose(es.sum(1), GOLDEN[spec.name + "/esc_nu"], rtol=RTOL, atol=0)
 
 
-@pytest.mark.parametrize("spec", [CASES[1], CASES[3]], ids=lambda s: s.name)
-def test_fp32_march_agrees_with_fp64_oracle(gpu_lib, spec):
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("spec", [CASES[1], CASES[2], CASES[3], CASES[4]], ids=lambda s: s.name)
+def test_fp32_march_agrees_with_fp64_oracle(gpu_lib, spec, form):
     """Band-integrated J per cell: GPU FP32 vs oracle FP64 over 8 seeds each;
     the difference of the means stays within 4 sigma (batch means) for the
     grid total and for >= 97% of well-sampled cells."""
     neb = nebula.build(spec)
     g, o = [], []
     for seed in range(1, 9):
-        g.append(transport.energy_packet_driver(neb, n_packets=3000, precision="fp32", seed=seed)[0].sum(0))
+        g.append(transport.energy_packet_driver(neb, n_packets=3000, precision="fp32", seed=seed,
+                                                form=form)[0].sum(0))
         o.append(runner.run(neb, n_packets=3000, precision="fp64", seed=100 + seed)[0].sum(0))
     g, o = np.array(g), np.array(o)
     sig = np.sqrt(g.var(0, ddof=1) / len(g) + o.var(0, ddof=1) / len(o))
@@ -81,47 +89,50 @@ def test_fp32_march_agrees_with_fp64_oracle(gpu_lib, spec):
     assert frac >= 0.97, frac
 
 
-def test_vacuum_known_answer_on_gpu(gpu_lib):
+@pytest.mark.parametrize("form", FORMS)
+def test_vacuum_known_answer_on_gpu(gpu_lib, form):
     spec = nebula.NebulaSpec("vac", 9, 3.0e18, True, [nebula.Star(40000.0, 10.0, (0, 0, 0), 200000)],
                              nh_median=100.0, r_in=0.0)
     neb = helpers.vacuum(nebula.build(spec))
     for prec in ("fp64", "fp32"):
-        js, _, es, st = transport.energy_packet_driver(neb, precision=prec, seed=3)
+        js, _, es, st = transport.energy_packet_driver(neb, precision=prec, seed=3, form=form)
         path = (js.sum(0) * helpers.cell_volumes(neb)).sum() / (neb.delta_e[0] * neb.n_packets[0])
         mu, sd = helpers.octant_path_expectation(3.0e18)
         assert abs(path - mu) < 4 * sd / np.sqrt(neb.n_packets[0]) + 1e-3 * mu, prec
         assert st["escaped"] == neb.n_packets[0]
 
 
-def test_zero_packets_and_errors(gpu_lib):
+@pytest.mark.parametrize("form", FORMS)
+def test_zero_packets_and_errors(gpu_lib, form):
     neb = nebula.build(CASES[0])
-    js, _, es, st = transport.energy_packet_driver(neb, n_packets=0, precision="fp32")
+    js, _, es, st = transport.energy_packet_driver(neb, n_packets=0, precision="fp32", form=form)
     assert st["crossings"] == 0 and js.sum() == 0 and es.sum() == 0
     bad = nebula.build(CASES[0])
     bad.star_cell = [(0, 1, 1)]
     with pytest.raises(transport.TransportError) as e:
-        transport.energy_packet_driver(bad, n_packets=10)
+        transport.energy_packet_driver(bad, n_packets=10, form=form)
     assert e.value.status == 3  # MC_ERR_BOUNDS
     # replay stream too short: MC_ERR_REPLAY, reported by the device, no fault
     draws = np.full((10, 3), 0.5)
     with pytest.raises(transport.TransportError) as e:
-        transport.energy_packet_driver(neb, n_packets=10, precision="fp64", replay=draws)
+        transport.energy_packet_driver(neb, n_packets=10, precision="fp64", replay=draws, form=form)
     assert e.value.status == 5
     # the library stays usable after device-side errors
-    js, _, es, st = transport.energy_packet_driver(neb, n_packets=100, precision="fp64", seed=1)
+    js, _, es, st = transport.energy_packet_driver(neb, n_packets=100, precision="fp64", seed=1, form=form)
     assert st["escaped"] + st["lines"] == 100
 
 
-def test_watchdog_returns_timeout_status(gpu_lib, monkeypatch):
+@pytest.mark.parametrize("form", FORMS)
+def test_watchdog_returns_timeout_status(gpu_lib, monkeypatch, form):
     """A kernel budget of ~0 makes every thread give up after its first
     check: the call returns MC_ERR_TIMEOUT and the context stays usable."""
     neb = nebula.build(nebula.octant21(20000))
     monkeypatch.setenv("MC_KERNEL_BUDGET_S", "1e-9")
     with pytest.raises(transport.TransportError) as e:
-        transport.energy_packet_driver(neb, precision="fp32")
+        transport.energy_packet_driver(neb, precision="fp32", form=form)
     assert e.value.status == 6
     monkeypatch.delenv("MC_KERNEL_BUDGET_S")
-    js, _, es, st = transport.energy_packet_driver(neb, precision="fp32")
+    js, _, es, st = transport.energy_packet_driver(neb, precision="fp32", form=form)
     assert st["escaped"] + st["lines"] == 20000
 
 
@@ -139,3 +150,19 @@ def test_resident_context_accumulates(gpu_lib):
     assert js0.sum() == 0
     ctx.close()
     assert s1["crossings"] == a[3]["crossings"] and s2["crossings"] == b[3]["crossings"]
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_grey_absorber_known_answer_on_gpu(gpu_lib, form, prec, symmetric):
+    """First-flight path length with a grey absorber: E[(1 - exp(-kappa s)) / kappa]
+    over isotropic directions, s the distance to the march boundary."""
+    spec = nebula.NebulaSpec("grey", 11, 3.0e18, symmetric, [nebula.Star(40000.0, 10.0, (0, 0, 0), 200000)],
+                             nh_median=100.0, r_in=0.0)
+    neb = helpers.vacuum(nebula.build(spec), kappa=6.0e-19, debug=True)
+    js, jd, es, st = transport.energy_packet_driver(neb, precision=prec, seed=21, form=form)
+    path = (js.sum(0) * helpers.cell_volumes(neb)).sum() / (neb.delta_e[0] * neb.n_packets[0])
+    mu, sd = helpers.octant_path_expectation(3.0e18, kappa=6.0e-19)
+    assert abs(path - mu) < 4 * sd / np.sqrt(neb.n_packets[0]) + 2e-4 * mu
+    assert st["escaped"] + st["lines"] + st["trapped"] == neb.n_packets[0]
