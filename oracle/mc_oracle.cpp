@@ -27,6 +27,12 @@
 //
 // Parallel over packet histories with OpenMP (the reference is MPI over
 // packets, iteration_mod.f90:477-493); estimators are summed with atomics.
+//
+// Parity unpinned: the reference (Fortran 90 + MPI) cannot be built in this
+// image and ships no tests or golden vectors, so this restatement is pinned
+// only by the published Philox known-answer vectors and by analytic known
+// answers of the transport (vacuum and grey-absorber path lengths, packet
+// and energy conservation) in tests/test_oracle_pinning.py.
 
 #include <atomic>
 #include <cmath>
