@@ -201,6 +201,27 @@ mc_status mc_ctx_device_estimators(mc_ctx_t *ctx, double **jste, double **jdif,
 
 void mc_ctx_destroy(mc_ctx_t *ctx);
 
+/* ---- allocation-free transport ------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a code that only hands over device memory it already manages, or a loop
+ * where an allocation could block or fail): runs the one-thread-per-history
+ * transport on DEVICE arrays the caller owns and allocates nothing.  Every
+ * pointer of `grid` (axes, active, opacity, ..., with rec_pdf / dust_pdf in
+ * the Fortran layout above), each spec_cdf of `src`, opts->replay and the
+ * jste / jdif / escaped accumulators are device pointers; `src`, `opts` and
+ * `stats` are host structs.  Its scratch (counters, first error, cell-width
+ * tables) is one fixed device array of about 37 KB that every GPU loading
+ * the library holds until exit; grids above 1024 cells along an axis or
+ * more than 16 sources are rejected with MC_ERR_UNSUPPORTED.  All calls
+ * share that array, so calls that overlap on the GPU race: serialise them.
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture.  `stream` is a cudaStream_t (NULL: default stream);
+ * the call returns after the stream has finished its work.  Results equal
+ * mc_transport_run with MC_RUN_FORM_PLAIN on the same inputs and draws. */
+mc_status mc_transport_run_noalloc(const mc_grid_t *grid, const mc_source_t *src, int32_t nsrc,
+                                   const mc_run_opts_t *opts, double *jste, double *jdif,
+                                   double *escaped, mc_stats_t *stats, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@ UNITS = [
     ("mcgpu_api.cu", []),
     ("transport_fp32.cu", []),
     ("transport_fp64.cu", ["-fmad=false"]),
+    ("transport_noalloc.cu", ["-fmad=false"]),
 ]
 
 

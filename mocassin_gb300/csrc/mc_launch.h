@@ -37,6 +37,9 @@ cudaError_t launch_wave_fold(const double *src, double *dst, const int32_t *lin2
 cudaError_t launch_wave_expand(const float *src, float *dst, const int32_t *lin2cell, long long ncell3, int nc1,
                                int nb, cudaStream_t stream);
 
+// Sets the text returned by mc_last_error() on the calling thread.
+void set_last_error_text(const char *msg);
+
 // Re-layout of the emission CDF rows: [nb][nc+1] (cell fastest) ->
 // [nc+1][nb] (one row per cell) with a running maximum along each row.
 cudaError_t launch_cdf_transpose(const float *in, float *out, int nc1, int nb, cudaStream_t stream);

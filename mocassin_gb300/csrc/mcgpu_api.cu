@@ -60,6 +60,8 @@ struct DBuf {
 
 namespace mcg {
 
+void set_last_error_text(const char *msg) { g_last_error = msg; }
+
 // Transposes a [nb][nc1] cell-fastest CDF into [nc1][nb] rows and applies a
 // running maximum along each row.  Block: 32 cells; tiles of 32 bins go
 // through shared memory so both the read and the write are coalesced.

@@ -52,7 +52,11 @@ struct LocalCounts {
   double qphot = 0.0;
 };
 
-template <typename Real> struct History {
+// Layout 0: emission CDF rows are contiguous per cell and monotone (the
+// context's re-laid-out copy), sampled by binary search.  Layout 1: the
+// caller's Fortran arrays recPDF(0:Nc, 1:nbins) (cell fastest), sampled by
+// getNu2's own linear scan over a strided row.
+template <typename Real, int Layout = 0> struct History {
   const DevGrid &g;
   const DevSource &src;
   DevCounters *cnt;
@@ -82,7 +86,7 @@ template <typename Real> struct History {
 
   // getNu2 on a monotone CDF row: the count c of leading entries <= random
   // gives nuP = max(c, 1), then +1 when below nbins-1.
-  __device__ int getNu2(const float *row) {
+  __device__ int getNu2(const float *row, long long stride) {
     Real random = rnd();
     int i;
     for (i = 1; i <= 10000; ++i) {
@@ -90,13 +94,21 @@ template <typename Real> struct History {
       else break;
     }
     if (i >= 10000) { fail(MC_ERR_BOUNDS); return 0; }
-    int lo = 0, hi = g.nb;  // first index with row[idx] > random
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (random >= (Real)__ldg(row + mid)) lo = mid + 1;
-      else hi = mid;
+    int nuP = 1;
+    if constexpr (Layout == 0) {
+      int lo = 0, hi = g.nb;  // first index with row[idx] > random
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (random >= (Real)__ldg(row + mid)) lo = mid + 1;
+        else hi = mid;
+      }
+      nuP = lo < 1 ? 1 : lo;
+    } else {
+      for (int is = 1; is <= g.nb; ++is) {  // photon_mod.f90:746-753
+        if (random >= (Real)__ldg(row + (long long)(is - 1) * stride)) nuP = is;
+        else break;
+      }
     }
-    int nuP = lo < 1 ? 1 : lo;
     if (nuP < g.nb - 1) nuP = nuP + 1;
     return nuP;
   }
@@ -393,7 +405,7 @@ template <typename Real> struct History {
     Pk<Real> pk;
     const R3<Real> zero{(Real)0, (Real)0, (Real)0};
     if (ptype == STELLAR) {
-      const int nuP = getNu2(src.cdf);
+      const int nuP = getNu2(src.cdf, 1);
       if (failed || nuP >= g.nb || nuP < 1) { fail(MC_ERR_BOUNDS); return false; }
       if (!initPacket(pk, nuP, position, zero, false, true, cell[0], cell[1], cell[2], false)) return false;
       if (pk.nu > (Real)1) lc.qphot += (double)(deltaE / ((Real)2.1799153e-11f * pk.nu));
@@ -405,12 +417,14 @@ template <typename Real> struct History {
         if (random <= (Real)__ldg(g.total_lines + a)) {
           if (!initPacket(pk, 0, position, zero, true, false, cell[0], cell[1], cell[2], false)) return false;
         } else {
-          const int nuP = getNu2(g.rec_cdf + (long long)a * g.nb);
+          const int nuP = Layout == 0 ? getNu2(g.rec_cdf + (long long)a * g.nb, 1)
+                                      : getNu2(g.rec_cdf + a, (long long)g.nc + 1);
           if (failed || nuP >= g.nb || nuP < 1) { fail(MC_ERR_BOUNDS); return false; }
           if (!initPacket(pk, nuP, position, zero, false, false, cell[0], cell[1], cell[2], false)) return false;
         }
       } else {
-        const int nuP = getNu2(g.dust_cdf + (long long)a * g.nb);
+        const int nuP = Layout == 0 ? getNu2(g.dust_cdf + (long long)a * g.nb, 1)
+                                    : getNu2(g.dust_cdf + a, (long long)g.nc + 1);
         if (failed || nuP >= g.nb || nuP < 1) { fail(MC_ERR_BOUNDS); return false; }
         if (!initPacket(pk, nuP, position, zero, false, false, cell[0], cell[1], cell[2], false)) return false;
       }
@@ -470,7 +484,7 @@ __device__ __forceinline__ void flush_counts(DevCounters *c, LocalCounts &lc) {
 }
 
 // Persistent grid-stride kernel over all packets of all sources.
-template <typename Real>
+template <typename Real, int Layout = 0>
 __global__ void __launch_bounds__(256) transport_plain_kernel(const __grid_constant__ DevGrid g,
                                                              const __grid_constant__ DevSources S,
                                                              const __grid_constant__ DevReplay rp,
@@ -483,7 +497,7 @@ __global__ void __launch_bounds__(256) transport_plain_kernel(const __grid_const
     int s = 0;
     while (s + 1 < S.nsrc && gp >= S.s[s + 1].base) ++s;
     const DevSource &src = S.s[s];
-    History<Real> h(g, src, cnt, lc);
+    History<Real, Layout> h(g, src, cnt, lc);
     h.gpacket = gp;
     h.t0 = t0;
     h.st.init(src.k0, src.k1, (unsigned long long)(gp - src.base), rp, gp);
