@@ -308,7 +308,7 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (tpc * per_launch_cross) if tpc else None,
             "kernel": "wave_march_kernel<float,true>" if args.form == "wave" else "transport_plain_kernel<float>",
-            "kernel_ms_per_launch": float(march_ms.mean()), "peak_kind": peak_kind + " hbm_gbs (copy)",
+            "kernel_ms_per_step": float(march_ms.mean()), "peak_kind": peak_kind + " hbm_gbs (copy)",
             "algorithmic_bytes_per_crossing": BYTES_PER_CROSSING}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(step_ms.mean()), "higher_is_better": True,
@@ -320,7 +320,10 @@ def main():
                        "l2": "inputs larger than L2 (opacity %.0f MB, Jste %.0f MB)"
                              % (neb.opacity.nbytes / 1e6, neb.opacity.size * 8 / 1e6),
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
-            "roofline": roof, "e2e": e2e, "gpu_launches": len(stats) * (4 if args.form == "wave" else 1),
+            # per step and round: sample, scan, scatter, emit, march (wave form) or one kernel (plain)
+            "roofline": roof, "e2e": e2e,
+            "gpu_launches": int(sum(s["rounds"] for s in stats) * (5 if args.form == "wave" else 1)),
+            "rounds_per_step": float(np.mean([s["rounds"] for s in stats])),
             "clocks": clk}
     if plain:
         line["plain_form"] = plain

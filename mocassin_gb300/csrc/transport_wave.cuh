@@ -380,11 +380,12 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   uint32_t id;
   Real absTau, passProb;
   bool stellar, valid;
+  bool pend;  // absorbed: the entry for the next round is written after the step
   RStream<Replay> st;
 
   __device__ Marcher(const DevGrid &g_, const DevSources &S_, const DevReplay &rp_, const WaveGrid &w_,
                      const Tables<Real> &T_, DevCounters *c_, LocalCounts &lc_)
-      : g(g_), S(S_), rp(rp_), w(w_), T(T_), cnt(c_), lc(lc_), valid(false) {}
+      : g(g_), S(S_), rp(rp_), w(w_), T(T_), cnt(c_), lc(lc_), valid(false), pend(false) {}
 
   __device__ __forceinline__ const DevSource &source() const { return S.s[source_of(S, id)]; }
   __device__ __forceinline__ Real rnd() {
@@ -406,7 +407,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   }
   __device__ __forceinline__ void set_v(R3<Real> d) {
     v = d;
-    if (Fast) iv = R3<Real>{(Real)1 / d.x, (Real)1 / d.y, (Real)1 / d.z};
+    if (Fast) iv = R3<Real>{(Real)__frcp_rn((float)d.x), (Real)__frcp_rn((float)d.y), (Real)__frcp_rn((float)d.z)};
   }
   __device__ __forceinline__ void flip(int a) {
     if (a == 0) { v.x = -v.x; if (Fast) iv.x = -iv.x; }
@@ -471,14 +472,18 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     ++lc.absorptions;
     if (segI >= g.safe_limit) { ++lc.safe_hits; end_history(); return; }
     if (runI >= g.recursion_limit) { ++lc.trapped; valid = false; return; }
-    const unsigned int slot = atomicAdd(w.a_count, 1u);
+    pend = true;
+    valid = false;
+  }
+  // writes the next round's entry of an absorbed packet into `slot`
+  __device__ __forceinline__ void write_absorbed(unsigned int slot) {
     w.a_id[slot] = id;
     w.a_cell[slot] = pack_cell(xP, yP, zP);
     w.a_words[slot] = st.consumed();
     w.a_run[slot] = (uint16_t)runI;
     Real *ar = (Real *)w.a_r + 3 * (size_t)slot;
     ar[0] = r.x; ar[1] = r.y; ar[2] = r.z;
-    valid = false;
+    pend = false;
   }
 
   __device__ __forceinline__ void deposit(int ci, Real val) {
@@ -630,6 +635,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
         atomicAdd(hot + s0 * kHot3 + (dx * kHot + dy) * kHot + dz, (float)val);
         return;
       }
+      hot_ok = false;  // a packet rarely comes back to its star's cube
     }
     atomicAdd(jrow + lin, (double)val);
   }
@@ -903,19 +909,34 @@ __global__ void __launch_bounds__(256) wave_march_kernel(const __grid_constant__
   const unsigned int lt_mask = (1u << lane) - 1u;
   const unsigned int qlen = w.bin_count[0];
   const int refill_min = w.refill_min;
+  // the warp's current chunk [cbeg, cend) of the sorted queue
+  constexpr unsigned int kChunk = 64;
+  unsigned long long cbeg = 0, cend = 0;
   bool qdone = qlen == 0;
   unsigned int iter = 0;
   while (true) {
     const unsigned int need = __ballot_sync(0xffffffffu, !m.valid);
     if (!qdone && (__popc(need) >= refill_min || need == 0xffffffffu)) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if ((int)lane == leader) base = atomicAdd(w.qhead, (unsigned long long)__popc(need));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (base + __popc(need) >= qlen) qdone = true;
+      const unsigned int nneed = __popc(need);
+      const unsigned long long have = cend - cbeg;
+      unsigned long long nbeg = 0;
+      if (have < nneed) {  // a new chunk (one atomic per kChunk packets)
+        if (lane == 0) nbeg = atomicAdd(w.qhead, (unsigned long long)kChunk);
+        nbeg = __shfl_sync(0xffffffffu, nbeg, 0);
+      }
+      const unsigned int rank = __popc(need & lt_mask);
+      unsigned long long q = rank < have ? cbeg + rank : nbeg + (rank - have);
+      if (have < nneed) {
+        cbeg = nbeg + (nneed - have);
+        cend = nbeg + kChunk;
+      } else {
+        cbeg += nneed;
+      }
+      if (cend > qlen) cend = qlen;
+      if (cbeg >= cend && (have < nneed ? nbeg + kChunk >= qlen : cend >= qlen)) qdone = true;
       if (Fast) {
         // the accumulator follows the bin of the first new packet
-        const unsigned long long q0 = base;
+        const unsigned long long q0 = __shfl_sync(0xffffffffu, q, __ffs(need) - 1);
         const int nu0 = q0 < qlen ? (int)(__ldg(w.q_meta + q0) & 0xFFFFu) : m.hot_nu;
         if (nu0 != m.hot_nu && nu0 != 0) {
           m.hot_flush(lane);
@@ -923,10 +944,7 @@ __global__ void __launch_bounds__(256) wave_march_kernel(const __grid_constant__
           m.refresh_hot();
         }
       }
-      if (!m.valid) {
-        const unsigned long long q = base + __popc(need & lt_mask);
-        if (q < qlen) m.start((unsigned int)q);
-      }
+      if (!m.valid && q < qlen) m.start((unsigned int)q);
     }
     if (!__any_sync(0xffffffffu, m.valid)) {
       if (qdone) break;
@@ -935,6 +953,14 @@ __global__ void __launch_bounds__(256) wave_march_kernel(const __grid_constant__
     if (m.valid) {
       if (Fast) m.advance(w.inner_steps);
       else m.step();
+    }
+    const unsigned int pm = __ballot_sync(0xffffffffu, m.pend);
+    if (pm) {  // warp-aggregated append of the absorbed packets
+      const int leader = __ffs(pm) - 1;
+      unsigned int base = 0;
+      if ((int)lane == leader) base = atomicAdd(w.a_count, (unsigned int)__popc(pm));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (m.pend) m.write_absorbed(base + __popc(pm & lt_mask));
     }
     if (((++iter) & 1023u) == 1u) {
       const unsigned long long el = global_ns() - t0;
