@@ -57,7 +57,7 @@ def measured_peak():
 
 def traffic_per_crossing():
     """DRAM bytes per crossing from the committed ncu summary, if any."""
-    p = os.path.join(HERE, "profiles", "transport_plain_fp32_dram.txt")
+    p = os.path.join(HERE, "profiles", "wave_march_dram.txt")
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_crossing:"):
