@@ -201,6 +201,31 @@ mc_status mc_ctx_device_estimators(mc_ctx_t *ctx, double **jste, double **jdif,
 
 void mc_ctx_destroy(mc_ctx_t *ctx);
 
+/* ---- opacity build ------------------------------------------------------
+ * The per-cell opacity of addOpacity (source/ionization_mod.f90:349-484)
+ * plus the dust add of iterateMC (source/iteration_mod.f90:166-227), as one
+ * dense contraction over K "species" (ions with their shell-summed
+ * cross-sections, and grain (species, size) bins):
+ *   opacity(cell, nu) = sum_k den(k, cell) * xs(k, nu) + ff(cell) [nu = 1]
+ * den: [K][Nc+1] number densities (grain rows: grainAbun * grainWeight * Ndust,
+ * zero where sublimated), cell fastest; xs: [K][nbins] cm^2; ff: [Nc+1]
+ * free-free opacity of bin 1 (the only bin addOpacity gives it), or NULL;
+ * opacity: [nbins][Nc+1] output, cell fastest.  K <= 64. */
+#define MC_OPAC_FP32 0    /* CUDA cores, FP32 fused multiply-add             */
+#define MC_OPAC_BF16X3 1  /* tensor cores: split BF16 (hi*hi + hi*lo + lo*hi),
+                             FP32 accumulate in tensor memory, ~1e-5 relative */
+
+/* Host arrays in and out. */
+mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t nbins, const float *den,
+                           const float *xs, const float *ff, int32_t method, float *opacity,
+                           double *kernel_ms);
+
+/* Builds the context's resident opacity (total, or the dust scattering
+ * opacity scaOpac when sca != 0) from host den/xs/ff: only den crosses the
+ * bus, not the (Nc+1) x nbins table. */
+mc_status mc_ctx_build_opacity(mc_ctx_t *ctx, int32_t nspecies, const float *den, const float *xs,
+                               const float *ff, int32_t method, int32_t sca, double *kernel_ms);
+
 /* ---- allocation-free transport ------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a code that only hands over device memory it already manages, or a loop

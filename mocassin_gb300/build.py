@@ -26,6 +26,7 @@ UNITS = [
     ("transport_fp32.cu", []),
     ("transport_fp64.cu", ["-fmad=false"]),
     ("transport_noalloc.cu", ["-fmad=false"]),
+    ("opacity.cu", []),
 ]
 
 

@@ -37,6 +37,10 @@ cudaError_t launch_wave_fold(const double *src, double *dst, const int32_t *lin2
 cudaError_t launch_wave_expand(const float *src, float *dst, const int32_t *lin2cell, long long ncell3, int nc1,
                                int nb, cudaStream_t stream);
 
+// Opacity contraction: method 0 = FP32 CUDA cores, 1 = tcgen05 split BF16.
+cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const float *den, const float *xs,
+                           const float *ff, float *out, int *error, int num_sms, cudaStream_t stream);
+
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);
 

@@ -624,6 +624,83 @@ void mc_ctx_destroy(mc_ctx_t *c) {
   if (s) cudaStreamDestroy(s);
 }
 
+namespace {
+
+mc_status opacity_device(int method, int nc1, int nspecies, int nb, const float *hden, const float *hxs,
+                         const float *hff, float *dout, int num_sms, cudaStream_t s, double *kernel_ms) {
+  if (nspecies < 1 || nspecies > 64) return set_error(MC_ERR_ARG, "nspecies must be 1..64 (got %d)", nspecies);
+  if (method != MC_OPAC_FP32 && method != MC_OPAC_BF16X3) return set_error(MC_ERR_ARG, "unknown opacity method");
+  if (!hden || !hxs || !dout || nc1 < 1 || nb < 1) return set_error(MC_ERR_ARG, "opacity: bad arguments");
+  DBuf den, xs, ff, err;
+  MC_CUDA(den.alloc((size_t)nspecies * nc1 * sizeof(float)));
+  MC_CUDA(xs.alloc((size_t)nspecies * nb * sizeof(float)));
+  MC_CUDA(err.alloc(sizeof(int)));
+  MC_CUDA(cudaMemcpyAsync(den.p, hden, den.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(xs.p, hxs, xs.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  if (hff) {
+    MC_CUDA(ff.alloc((size_t)nc1 * sizeof(float)));
+    MC_CUDA(cudaMemcpyAsync(ff.p, hff, ff.bytes, cudaMemcpyHostToDevice, s));
+  }
+  cudaEvent_t e0, e1;
+  MC_CUDA(cudaEventCreate(&e0));
+  MC_CUDA(cudaEventCreate(&e1));
+  MC_CUDA(cudaEventRecord(e0, s));
+  cudaError_t e = mcg::launch_opacity(method, nc1, nspecies, nb, den.as<float>(), xs.as<float>(),
+                                      hff ? ff.as<float>() : nullptr, dout, err.as<int>(), num_sms, s);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return set_error(MC_ERR_CUDA, "opacity launch failed: %s", cudaGetErrorString(e));
+  }
+  MC_CUDA(cudaEventRecord(e1, s));
+  int herr = 0;
+  MC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (kernel_ms) *kernel_ms = ms;
+  if (herr) return set_error((mc_status)herr, "opacity kernel: tensor-core wait timed out");
+  return MC_OK;
+}
+
+}  // namespace
+
+extern "C" mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t nbins, const float *den,
+                                      const float *xs, const float *ff, int32_t method, float *opacity,
+                                      double *kernel_ms) {
+  if (!opacity) return set_error(MC_ERR_ARG, "opacity is NULL");
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(MC_ERR_NO_DEVICE, "no CUDA device");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nc1 = ncells + 1;
+  DBuf out;
+  MC_CUDA(out.alloc((size_t)nc1 * nbins * sizeof(float)));
+  mc_status st = opacity_device(method, nc1, nspecies, nbins, den, xs, ff, out.as<float>(), sms, 0, kernel_ms);
+  if (st) return st;
+  MC_CUDA(cudaMemcpy(opacity, out.p, out.bytes, cudaMemcpyDeviceToHost));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_build_opacity(mc_ctx_t *c, int32_t nspecies, const float *den, const float *xs,
+                                          const float *ff, int32_t method, int32_t sca, double *kernel_ms) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  DBuf &target = sca ? c->sca : c->opacity;
+  if (!target.p) return set_error(MC_ERR_ARG, "the context has no %s table", sca ? "scaOpac" : "opacity");
+  const int nc1 = c->nc + 1, nb = c->nb;
+  mc_status st = opacity_device(method, nc1, nspecies, nb, den, xs, ff, target.as<float>(), c->num_sms, c->stream,
+                                kernel_ms);
+  if (st) return st;
+  if (!c->identity) {
+    DBuf &m = sca ? c->sca_m : c->opac_m;
+    MC_CUDA(mcg::launch_wave_expand(target.as<float>(), m.as<float>(), c->lin2cell.as<int32_t>(), c->ncell3, nc1, nb,
+                                    c->stream));
+    MC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return MC_OK;
+}
+
 mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
                            double *jste, double *jdif, double *escaped, mc_stats_t *stats) {
   if (!jste) return set_error(MC_ERR_ARG, "jste is NULL");

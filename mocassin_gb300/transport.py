@@ -57,6 +57,11 @@ def library():
         lib.mc_ctx_device_estimators.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
         lib.mc_ctx_destroy.restype = None
         lib.mc_ctx_destroy.argtypes = [C.c_void_p]
+        fp = C.POINTER(C.c_float)
+        lib.mc_opacity_build.restype = C.c_int
+        lib.mc_opacity_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, fp, fp, fp, C.c_int32, fp, dp]
+        lib.mc_ctx_build_opacity.restype = C.c_int
+        lib.mc_ctx_build_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp, fp, C.c_int32, C.c_int32, dp]
         if lib.mc_abi_version() != 1:
             raise TransportError(1, "ABI version mismatch")
         _LIB = lib
@@ -104,6 +109,33 @@ def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp
     return jste, jdif, escaped, st.as_dict()
 
 
+OPACITY_METHODS = {"fp32": 0, "bf16x3": 1}
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def opacity_build(den, xs, ff=None, method="bf16x3"):
+    """opacity(cell, nu) = sum_k den(k, cell) xs(k, nu) + ff(cell) [nu = 1] on the GPU.
+
+    den: (K, Nc+1), xs: (K, nbins), ff: (Nc+1,) or None; returns (opacity
+    (nbins, Nc+1) float32, kernel ms).  The dense form of addOpacity
+    (ionization_mod.f90:349-484) with the dust add (iteration_mod.f90:166-227).
+    """
+    lib = library()
+    den = np.ascontiguousarray(den, dtype=np.float32)
+    xs = np.ascontiguousarray(xs, dtype=np.float32)
+    ff = None if ff is None else np.ascontiguousarray(ff, dtype=np.float32)
+    k, nc1 = den.shape
+    nb = xs.shape[1]
+    out = np.empty((nb, nc1), dtype=np.float32)
+    ms = C.c_double()
+    _check(lib.mc_opacity_build(nc1 - 1, k, nb, _fptr(den), _fptr(xs), _fptr(ff), OPACITY_METHODS[method],
+                                _fptr(out), C.byref(ms)))
+    return out, ms.value
+
+
 def abi_flag_debug():
     return 1 << 4
 
@@ -144,6 +176,16 @@ class TransportContext:
         escaped = es0 if escaped is None else escaped
         _check(self.lib.mc_ctx_download(self.handle, _dptr(jste), _dptr(jdif), _dptr(escaped), int(accumulate)))
         return jste, jdif, escaped
+
+    def build_opacity(self, den, xs, ff=None, method="bf16x3", sca=False):
+        """Rebuilds the resident opacity (or scaOpac) from den / xs on the GPU."""
+        den = np.ascontiguousarray(den, dtype=np.float32)
+        xs = np.ascontiguousarray(xs, dtype=np.float32)
+        ff = None if ff is None else np.ascontiguousarray(ff, dtype=np.float32)
+        ms = C.c_double()
+        _check(self.lib.mc_ctx_build_opacity(self.handle, den.shape[0], _fptr(den), _fptr(xs), _fptr(ff),
+                                             OPACITY_METHODS[method], int(sca), C.byref(ms)))
+        return ms.value
 
     def device_estimators(self):
         j, d, e = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()

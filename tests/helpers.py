@@ -67,3 +67,10 @@ def cell_volumes(neb):
 def rel_err(a, b):
     scale = max(np.abs(b).max(), 1e-300)
     return float(np.abs(a - b).max() / scale)
+
+
+def with_opacity(neb, opacity):
+    """The same nebula with another opacity table (nbins, Nc+1)."""
+    n = dataclasses.replace(neb)
+    n.opacity = np.ascontiguousarray(opacity, dtype=np.float32)
+    return n
