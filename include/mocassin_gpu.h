@@ -161,11 +161,20 @@ const char *mc_last_error(void);
  * (photon_mod.f90:26-285, the star loop of iteration_mod.f90:474-496).
  * HOST pointers in, HOST accumulators out: uploads the grid, runs all packets
  * of all sources on the GPU and adds the estimators into jste / jdif /
- * escaped.  jdif may be NULL unless MC_FLAG_DEBUG; escaped may be NULL. */
+ * escaped (their current values are copied to the device, the kernels add
+ * to them, the sums are copied back).  jdif may be NULL unless
+ * MC_FLAG_DEBUG; escaped may be NULL.  The device buffers are kept for the
+ * next call with the same grid shape (see mc_transport_release). */
 mc_status mc_transport_run(const mc_grid_t *grid, const mc_source_t *src,
                            int32_t nsrc, const mc_run_opts_t *opts,
                            double *jste, double *jdif, double *escaped,
                            mc_stats_t *stats);
+
+/* mc_transport_run keeps the device buffers of the last grid shape for the
+ * next call (a Lambda iteration calls it with the same grid every time);
+ * this frees them.  No counterpart in the reference (it allocates nothing
+ * on a device). */
+mc_status mc_transport_release(void);
 
 /* ---- resident context: the grid stays in HBM across iterations --------- */
 typedef struct mc_ctx mc_ctx_t;

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -371,6 +372,60 @@ mc_status mc_ctx_create(const mc_grid_t *g, mc_ctx_t **out) {
   return MC_OK;
 }
 
+
+namespace {
+
+// Re-uploads the geometry of a grid of the context's shape (axes, active,
+// frequencies, cell widths, march order).  Returns MC_ERR_ARG when the
+// active map changes which cells are active in a way that changes the march
+// layout (the caller then builds a new context).
+mc_status refresh_geometry(mc_ctx *c, const mc_grid_t *g) {
+  const bool sym = g->flags & MC_FLAG_SYMMETRIC_XYZ;
+  const size_t n3 = (size_t)g->nx * g->ny * g->nz;
+  std::vector<int32_t> l2c(n3);
+  int identity = 1;
+  for (int x = 1; x <= g->nx; ++x)
+    for (int y = 1; y <= g->ny; ++y)
+      for (int z = 1; z <= g->nz; ++z) {
+        const long long lin = (z - 1) + (long long)g->nz * ((y - 1) + (long long)g->ny * (x - 1));
+        const int a = g->active[(x - 1) + (long long)g->nx * ((y - 1) + (long long)g->ny * (z - 1))];
+        l2c[lin] = a;
+        if (a != lin + 1) identity = 0;
+      }
+  if (identity != c->identity) return set_error(MC_ERR_ARG, "march layout changed");
+  cudaStream_t s = c->stream;
+  MC_CUDA(cudaMemcpyAsync(c->xa.p, g->x_axis, g->nx * sizeof(float), cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(c->ya.p, g->y_axis, g->ny * sizeof(float), cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(c->za.p, g->z_axis, g->nz * sizeof(float), cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(c->active.p, g->active, n3 * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(c->nu.p, g->nu_array, g->nbins * sizeof(float), cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(c->lin2cell.p, l2c.data(), n3 * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  std::vector<float> w32[3];
+  std::vector<double> w64[3];
+  const float *ax[3] = {g->x_axis, g->y_axis, g->z_axis};
+  const int na[3] = {g->nx, g->ny, g->nz};
+  DBuf *b32[3] = {&c->dx32, &c->dy32, &c->dz32};
+  DBuf *b64[3] = {&c->dx64, &c->dy64, &c->dz64};
+  for (int k = 0; k < 3; ++k) {
+    widths<float>(ax[k], na[k], sym, w32[k]);
+    widths<double>(ax[k], na[k], sym, w64[k]);
+    MC_CUDA(cudaMemcpyAsync(b32[k]->p, w32[k].data(), na[k] * sizeof(float), cudaMemcpyHostToDevice, s));
+    MC_CUDA(cudaMemcpyAsync(b64[k]->p, w64[k].data(), na[k] * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  MC_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  c->g.gc[0] = g->geo_corr[0]; c->g.gc[1] = g->geo_corr[1]; c->g.gc[2] = g->geo_corr[2];
+  c->g.rout = g->r_out;
+  c->g.ion_edge1 = g->ion_edge1;
+  return MC_OK;
+}
+
+// The context kept by mc_transport_run between calls (one host thread drives
+// the library, so a single cache suffices).
+std::mutex g_cache_mutex;
+mc_ctx *g_cached = nullptr;
+
+}  // namespace
+
 mc_status mc_ctx_update(mc_ctx_t *c, const mc_grid_t *g) {
   if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
   mc_status st = check_grid(g);
@@ -705,13 +760,42 @@ mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t n
                            double *jste, double *jdif, double *escaped, mc_stats_t *stats) {
   if (!jste) return set_error(MC_ERR_ARG, "jste is NULL");
   if (g && (g->flags & MC_FLAG_DEBUG) && !jdif) return set_error(MC_ERR_ARG, "debug grid needs jdif");
-  mc_ctx_t *c = nullptr;
-  mc_status st = mc_ctx_create(g, &c);
+  mc_status st = check_grid(g);
   if (st) return st;
-  st = mc_ctx_run(c, src, nsrc, o, stats);
-  if (st == MC_OK) st = mc_ctx_download(c, jste, jdif, escaped, 1);
-  mc_ctx_destroy(c);
+  std::lock_guard<std::mutex> lock(g_cache_mutex);
+  mc_ctx *c = g_cached;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  bool reuse = c && c->device == dev && c->nx == g->nx && c->ny == g->ny && c->nz == g->nz && c->nc == g->ncells &&
+               c->nb == g->nbins && c->flags == g->flags;
+  if (reuse && (refresh_geometry(c, g) != MC_OK || upload_arrays(c, g, false) != MC_OK)) reuse = false;
+  if (!reuse) {
+    if (c) mc_ctx_destroy(c);
+    g_cached = nullptr;
+    if ((st = mc_ctx_create(g, &c))) return st;
+    g_cached = c;
+  }
+  // the estimators accumulate into the caller's arrays: their current
+  // values go to the device first, the kernels add to them, and the sums
+  // come back (no host-side pass over the arrays)
+  struct Item { double *h; DBuf *d; } items[3] = {{jste, &c->jste}, {jdif, &c->jdif}, {escaped, &c->esc}};
+  for (auto &it : items) {
+    if (!it.d->p) continue;
+    if (it.h) MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, c->stream));
+    else MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, c->stream));
+  }
+  mc_run_opts_t o2 = *o;
+  o2.run_flags &= ~MC_RUN_ZERO_FIRST;
+  st = mc_ctx_run(c, src, nsrc, &o2, stats);
+  if (st == MC_OK) st = mc_ctx_download(c, jste, jdif, escaped, 0);
   return st;
+}
+
+mc_status mc_transport_release(void) {
+  std::lock_guard<std::mutex> lock(g_cache_mutex);
+  if (g_cached) mc_ctx_destroy(g_cached);
+  g_cached = nullptr;
+  return MC_OK;
 }
 
 }  // extern "C"

@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 
 #include "mc_launch.h"
 
@@ -103,7 +104,7 @@ struct OpacityTcArgs {
   int *error;              // set to MC_ERR_TIMEOUT when an mbarrier wait gives up
 };
 
-__global__ void __launch_bounds__(128, 1) opacity_tc_kernel(const __grid_constant__ OpacityTcArgs a) {
+__global__ void __launch_bounds__(128, 4) opacity_tc_kernel(const __grid_constant__ OpacityTcArgs a) {
   // shared: B hi/lo [N=128 bins][K], A hi/lo [M=128 cells][K], mbarrier, TMEM slot
   extern __shared__ __align__(1024) unsigned char sm[];
   const int K = a.K;
@@ -148,15 +149,33 @@ __global__ void __launch_bounds__(128, 1) opacity_tc_kernel(const __grid_constan
   const int ntiles = (a.nc1 + kOpM - 1) / kOpM;
   for (int t = blockIdx.y; t < ntiles && !failed; t += gridDim.y) {
     const int c0 = t * kOpM;
-    // A = den^T for cells c0..c0+127 (row = cell, column = species)
-    for (int i = tid; i < kOpM * K; i += blockDim.x) {
-      const int k = i / kOpM, r = i % kOpM;  // consecutive threads: consecutive cells
-      const int c = c0 + r;
-      const float x = (k < a.nspecies && c < a.nc1) ? __ldg(a.den + (long long)k * a.nc1 + c) : 0.f;
-      __nv_bfloat16 hi, lo;
-      split_bf16(x, hi, lo);
-      *(__nv_bfloat16 *)(sAhi + kmajor_off(r, k, K)) = hi;
-      *(__nv_bfloat16 *)(sAlo + kmajor_off(r, k, K)) = lo;
+    // A = den^T for cells c0..c0+127 (row = cell, column = species): thread
+    // r owns cell c0 + r; all its species loads are issued together
+    // (coalesced along cells across the warp), then each group of 8 species
+    // becomes one 16-byte row of a core matrix (conflict-free per quarter
+    // warp)
+    {
+      const int r = tid, c = c0 + r;
+      float x[kOpKMax];
+#pragma unroll
+      for (int k = 0; k < kOpKMax; ++k)
+        x[k] = (k < a.nspecies && c < a.nc1) ? __ldg(a.den + (long long)k * a.nc1 + c) : 0.f;
+#pragma unroll
+      for (int kc = 0; kc < kOpKMax / 8; ++kc) {
+        if (kc * 8 >= K) break;
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          __nv_bfloat16 h0, l0, h1, l1;
+          split_bf16(x[kc * 8 + j], h0, l0);
+          split_bf16(x[kc * 8 + j + 1], h1, l1);
+          hw[j / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+          lw[j / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+        }
+        const uint32_t off = kmajor_off(r, kc * 8, K);
+        *(uint4 *)(sAhi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *(uint4 *)(sAlo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -256,7 +275,15 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
   if (e != cudaSuccess) return e;
   const int nvt = (nb + kOpN - 1) / kOpN;
   const int ntiles = (nc1 + kOpM - 1) / kOpM;
-  int per = (num_sms * 2 + nvt - 1) / nvt;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, opacity_tc_kernel, 128, sh);
+  if (e != cudaSuccess) return e;
+  int want_sm = 2;  // CTAs per SM (at most 4: 4 x 128 TMEM columns = 512)
+  if (const char *e2 = getenv("MC_OPAC_CTAS_PER_SM")) want_sm = atoi(e2);
+  if (per_sm > want_sm) per_sm = want_sm;
+  if (per_sm > 4) per_sm = 4;
+  if (per_sm < 1) per_sm = 1;
+  int per = (num_sms * per_sm + nvt - 1) / nvt;
   if (per > ntiles) per = ntiles;
   if (per < 1) per = 1;
   opacity_tc_kernel<<<dim3(nvt, per), 128, sh, stream>>>(a);

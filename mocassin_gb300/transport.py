@@ -55,6 +55,7 @@ def library():
         lib.mc_ctx_download.argtypes = [C.c_void_p, dp, dp, dp, C.c_int32]
         lib.mc_ctx_device_estimators.restype = C.c_int
         lib.mc_ctx_device_estimators.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
+        lib.mc_transport_release.restype = C.c_int
         lib.mc_ctx_destroy.restype = None
         lib.mc_ctx_destroy.argtypes = [C.c_void_p]
         fp = C.POINTER(C.c_float)

@@ -74,3 +74,8 @@ def with_opacity(neb, opacity):
     n = dataclasses.replace(neb)
     n.opacity = np.ascontiguousarray(opacity, dtype=np.float32)
     return n
+
+
+def zeros_like_estimators(neb):
+    nc1 = neb.ncells + 1
+    return np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins + 1, nc1))

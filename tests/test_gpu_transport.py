@@ -166,3 +166,20 @@ def test_grey_absorber_known_answer_on_gpu(gpu_lib, form, prec, symmetric):
     mu, sd = helpers.octant_path_expectation(3.0e18, kappa=6.0e-19)
     assert abs(path - mu) < 4 * sd / np.sqrt(neb.n_packets[0]) + 2e-4 * mu
     assert st["escaped"] + st["lines"] + st["trapped"] == neb.n_packets[0]
+
+
+def test_drop_in_call_accumulates_and_reuses_its_buffers(gpu_lib):
+    """Two drop-in calls into the same arrays add up (the Fortran zeroes Jste
+    once per iteration and calls once per star); a call on another grid shape
+    in between makes the library rebuild its cached buffers."""
+    neb = nebula.build(CASES[1])
+    other = nebula.build(CASES[0])
+    js, jd, es = helpers.zeros_like_estimators(neb)
+    transport.energy_packet_driver(neb, precision="fp64", seed=41, jste=js, escaped=es)
+    transport.energy_packet_driver(other, precision="fp64", seed=1)
+    transport.energy_packet_driver(neb, precision="fp64", seed=42, jste=js, escaped=es)
+    a = runner.run(neb, precision="fp64", seed=41)
+    b = runner.run(neb, precision="fp64", seed=42)
+    assert helpers.rel_err(js, a[0] + b[0]) < RTOL
+    assert helpers.rel_err(es, a[2] + b[2]) < RTOL
+    assert gpu_lib.mc_transport_release() == 0
