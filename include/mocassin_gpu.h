@@ -235,6 +235,17 @@ mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t nbins, cons
 mc_status mc_ctx_build_opacity(mc_ctx_t *ctx, int32_t nspecies, const float *den, const float *xs,
                                const float *ff, int32_t method, int32_t sca, double *kernel_ms);
 
+/* ---- moments of the estimator for the cell update -------------------------
+ * out(o, cell) = scale * sum_nu Jste(nu, cell) * w(nu, o), o < nout <= 64, on
+ * the context's device Jste after mc_ctx_run: the photoionisation sums of
+ * updateCell (source/update_mod.f90:175-269, with w = phXSec / (hcRyd nu)
+ * and scale the normalisation of iteration_mod.f90:705-724; the reference
+ * adds 1e-20 afterwards) and the heating sums of its thermal balance have
+ * this form.  w: host [nbins][nout]; out: host [nout][Nc+1] (cell fastest).
+ * Tensor cores (tcgen05, split BF16, FP32 accumulate): ~1e-5 relative. */
+mc_status mc_ctx_jste_moments(mc_ctx_t *ctx, int32_t nout, const float *w, double scale, float *out,
+                              double *kernel_ms);
+
 /* ---- allocation-free transport ------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a code that only hands over device memory it already manages, or a loop

@@ -27,6 +27,7 @@ UNITS = [
     ("transport_fp64.cu", ["-fmad=false"]),
     ("transport_noalloc.cu", ["-fmad=false"]),
     ("opacity.cu", []),
+    ("jmoments.cu", []),
 ]
 
 

@@ -41,6 +41,10 @@ cudaError_t launch_wave_expand(const float *src, float *dst, const int32_t *lin2
 cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const float *den, const float *xs,
                            const float *ff, float *out, int *error, int num_sms, cudaStream_t stream);
 
+// Jste moments: out[o][cell] = scale * sum_nu J[nu][cell] W[nu][o] (tcgen05).
+cudaError_t launch_jmoments(int nc1, int nb, int nout, const double *J, const float *W, double scale, float *out,
+                            int *error, int num_sms, cudaStream_t stream);
+
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);
 

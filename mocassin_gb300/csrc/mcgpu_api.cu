@@ -738,6 +738,34 @@ extern "C" mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t 
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_jste_moments(mc_ctx_t *c, int32_t nout, const float *w, double scale, float *out,
+                                          double *kernel_ms) {
+  if (!c || !w || !out) return set_error(MC_ERR_ARG, "ctx, w and out are required");
+  if (nout < 1 || nout > 64) return set_error(MC_ERR_ARG, "nout must be 1..64 (got %d)", nout);
+  const int nc1 = c->nc + 1, nb = c->nb;
+  DBuf dw, dout, err;
+  MC_CUDA(dw.alloc((size_t)nb * nout * sizeof(float)));
+  MC_CUDA(dout.alloc((size_t)nout * nc1 * sizeof(float)));
+  MC_CUDA(err.alloc(sizeof(int)));
+  cudaStream_t s = c->stream;
+  MC_CUDA(cudaMemcpyAsync(dw.p, w, dw.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  MC_CUDA(cudaEventRecord(c->evm0, s));
+  cudaError_t e = mcg::launch_jmoments(nc1, nb, nout, c->jste.as<double>(), dw.as<float>(), scale, dout.as<float>(),
+                                       err.as<int>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "moment launch failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(c->evm1, s));
+  int herr = 0;
+  MC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaMemcpyAsync(out, dout.p, dout.bytes, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->evm0, c->evm1);
+  if (kernel_ms) *kernel_ms = ms;
+  if (herr) return set_error((mc_status)herr, "moment kernel: tensor-core wait timed out");
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_build_opacity(mc_ctx_t *c, int32_t nspecies, const float *den, const float *xs,
                                           const float *ff, int32_t method, int32_t sca, double *kernel_ms) {
   if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");

@@ -37,6 +37,7 @@
 #include <cstdlib>
 
 #include "mc_launch.h"
+#include "tc_util.cuh"
 
 namespace mcg {
 
@@ -67,35 +68,6 @@ __global__ void __launch_bounds__(256) opacity_fp32_kernel(int nc1, int K, int n
 }
 
 // ------------------------------------------------------------- tcgen05
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Shared-memory matrix descriptor: K-major, no swizzle.  Core matrices are
-// 8 rows x 16 bytes; `lbo` is the byte step between core matrices along K,
-// `sbo` along the rows.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
-  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of sm_100 family
-  return d;                // base offset 0, swizzle none
-}
-
-// Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major.
-__host__ __device__ constexpr uint32_t mma_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// byte offset of (row r, k) in a K-major no-swizzle tile of K columns
-__device__ __forceinline__ uint32_t kmajor_off(int r, int k, int K) {
-  return (uint32_t)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-}
-
 struct OpacityTcArgs {
   int nc1, K, nb;          // K padded to a multiple of 16 (<= 64)
   int nspecies;            // real species (rows of den / xs)

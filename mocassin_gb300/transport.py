@@ -37,6 +37,7 @@ def library():
             raise TransportError(2, "libmcgpu.so is not built (%s); run mocassin_gb300.build.build()" % LIB_PATH)
         lib = C.CDLL(LIB_PATH)
         dp = C.POINTER(C.c_double)
+        fp = C.POINTER(C.c_float)
         lib.mc_abi_version.restype = C.c_int
         lib.mc_last_error.restype = C.c_char_p
         lib.mc_transport_run.restype = C.c_int
@@ -56,9 +57,10 @@ def library():
         lib.mc_ctx_device_estimators.restype = C.c_int
         lib.mc_ctx_device_estimators.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
         lib.mc_transport_release.restype = C.c_int
+        lib.mc_ctx_jste_moments.restype = C.c_int
+        lib.mc_ctx_jste_moments.argtypes = [C.c_void_p, C.c_int32, fp, C.c_double, fp, dp]
         lib.mc_ctx_destroy.restype = None
         lib.mc_ctx_destroy.argtypes = [C.c_void_p]
-        fp = C.POINTER(C.c_float)
         lib.mc_opacity_build.restype = C.c_int
         lib.mc_opacity_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, fp, fp, fp, C.c_int32, fp, dp]
         lib.mc_ctx_build_opacity.restype = C.c_int
@@ -187,6 +189,16 @@ class TransportContext:
         _check(self.lib.mc_ctx_build_opacity(self.handle, den.shape[0], _fptr(den), _fptr(xs), _fptr(ff),
                                              OPACITY_METHODS[method], int(sca), C.byref(ms)))
         return ms.value
+
+    def jste_moments(self, w, scale=1.0):
+        """out(o, cell) = scale * sum_nu Jste(nu, cell) w(nu, o) on the resident Jste
+        (the photoionisation and heating sums of updateCell, update_mod.f90:175-269)."""
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        nout = w.shape[1]
+        out = np.empty((nout, self.neb.ncells + 1), dtype=np.float32)
+        ms = C.c_double()
+        _check(self.lib.mc_ctx_jste_moments(self.handle, nout, _fptr(w), float(scale), _fptr(out), C.byref(ms)))
+        return out, ms.value
 
     def device_estimators(self):
         j, d, e = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
