@@ -250,6 +250,21 @@ def main():
         plain = {"value": pc / (pms.sum() / 1e3), "unit": UNIT, "ms_per_step": float(pms.mean()),
                  "steps": args.plain_steps, "kernel": "transport_plain_kernel<float>",
                  "roofline_frac": pc * BYTES_PER_CROSSING / (pms.sum() / 1e3) / 1e9 / measured_peak()[0]}
+    # photoionisation sums of the cell update on the resident Jste (one moment per ion)
+    moments = None
+    if not args.no_opacity:
+        from mocassin_gb300 import rates
+        w = rates.photo_weights(neb.xs, neb.nu)
+        ctx.jste_moments(w, 1e-9)
+        ts = [ctx.jste_moments(w, 1e-9)[1] for _ in range(5)]
+        t = float(np.median(ts)) / 1e3
+        jb = neb.nbins * (neb.ncells + 1) * 8
+        ob = w.shape[1] * (neb.ncells + 1) * 4
+        moments = {"kernel": "jmoment_tc_kernel (tcgen05 kind::f16, split BF16 x3, FP32 accumulate)",
+                   "outputs": int(w.shape[1]), "ms": t * 1e3, "achieved_gbs": (jb + ob) / t / 1e9,
+                   "frac_of_hbm": (jb + ob) / t / 1e9 / measured_peak()[0],
+                   "bound": "hbm (reads 8 B of Jste per cell and bin)",
+                   "download_bytes": ob, "instead_of": jb}
     # opacity build on the resident grid (addOpacity + dust add as one contraction)
     opac = None
     if not args.no_opacity:
@@ -352,6 +367,8 @@ def main():
         line["plain_form"] = plain
     if opac:
         line["opacity_build"] = opac
+    if moments:
+        line["jste_moments"] = moments
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(neb)
     if rank == 0:

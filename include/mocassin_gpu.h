@@ -85,7 +85,7 @@ typedef struct mc_grid {
   int32_t nx, ny, nz;      /* grid%nx, grid%ny, grid%nz                       */
   int32_t ncells;          /* grid%nCells = Nc; arrays carry rows 0..Nc       */
   int32_t nbins;           /* nbins = Nnu                                     */
-  int32_t n_angle;         /* nAngleBins; only 0 is supported (bin 0 only)    */
+  int32_t n_angle;         /* nAngleBins (0..2, set_input_mod.f90:536-541)     */
   const float *x_axis;     /* [nx] cm                                         */
   const float *y_axis;     /* [ny] cm                                         */
   const float *z_axis;     /* [nz] cm                                         */
@@ -101,6 +101,13 @@ typedef struct mc_grid {
   float r_out;             /* R_out (0 = no outer radius)                     */
   float ion_edge1;         /* ionEdge(1), Ryd                                 */
   uint32_t flags;          /* MC_FLAG_*                                       */
+  /* Viewing angles of the escape SED (n_angle > 0 only; grid_mod.f90:416-468):
+   * every escape adds deltaE to angle plane 0 of escaped and, when its
+   * direction falls in the theta/phi bin of viewpoint i, to plane i too. */
+  int32_t n_theta_bins;    /* totAngleBinsTheta, 0 = 10 (common_mod.f90:399)  */
+  int32_t n_phi_bins;      /* totAngleBinsPhi, 0 = 20 (common_mod.f90:400)    */
+  const float *view_theta; /* viewPointTheta(0:nAngleBins) [rad], or NULL     */
+  const float *view_phi;   /* viewPointPhi(0:nAngleBins) [rad]; < 0 = no phi  */
 } mc_grid_t;
 
 /* One ionising source: one call of energyPacketDriver(iStar, n, ...). */

@@ -33,7 +33,8 @@ class McGrid(C.Structure):
                 ("opacity", _fp), ("sca_opac", _fp), ("rec_pdf", _fp), ("total_lines", _fp),
                 ("dust_pdf", _fp), ("nu_array", _fp), ("g_sca", _fp),
                 ("geo_corr", C.c_float * 3), ("r_out", C.c_float), ("ion_edge1", C.c_float),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("n_theta_bins", C.c_int32), ("n_phi_bins", C.c_int32),
+                ("view_theta", _fp), ("view_phi", _fp)]
 
 
 class McSource(C.Structure):
@@ -81,7 +82,8 @@ class Marshalled:
         self.keep.append(act)
         g = McGrid()
         g.nx, g.ny, g.nz = neb.nx, neb.ny, neb.nz
-        g.ncells, g.nbins, g.n_angle = neb.ncells, neb.nbins, 0
+        views = list(getattr(neb.spec, "views", ()) or ())
+        g.ncells, g.nbins, g.n_angle = neb.ncells, neb.nbins, len(views)
         g.x_axis = _ptr(f(neb.x_axis), C.c_float)
         g.y_axis = _ptr(f(neb.y_axis), C.c_float)
         g.z_axis = _ptr(f(neb.z_axis), C.c_float)
@@ -98,6 +100,15 @@ class Marshalled:
         g.r_out = float(neb.r_out)
         g.ion_edge1 = float(neb.ion_edge1)
         g.flags = int(neb.flags)
+        g.n_theta_bins = int(getattr(neb.spec, "n_theta_bins", 0))
+        g.n_phi_bins = int(getattr(neb.spec, "n_phi_bins", 0))
+        if views:
+            # viewPointTheta / viewPointPhi (0:nAngleBins), element 0 unused (0)
+            g.view_theta = _ptr(f([0.0] + [v[0] for v in views]), C.c_float)
+            g.view_phi = _ptr(f([0.0] + [v[1] for v in views]), C.c_float)
+        else:
+            g.view_theta = _ptr(None, C.c_float)
+            g.view_phi = _ptr(None, C.c_float)
         self.grid = g
         ns = len(neb.star_pos)
         self.sources = (McSource * ns)()
@@ -138,7 +149,19 @@ def make_opts(seed=1, iteration=1, precision=MC_PREC_FP64, replay=None, recursio
     return o
 
 
-def estimator_arrays(neb):
-    """Zeroed host accumulators: Jste, Jdif (nbins, Nc+1), escaped (nbins+1, Nc+1)."""
+def n_angle(neb):
+    return len(getattr(neb.spec, "views", ()) or ())
+
+
+def escaped_shape(neb):
+    """escapedPackets(0:Nc, 0:nbins, 0:nAngleBins) in C order: (nbins+1, Nc+1), or
+    (nAngleBins+1, nbins+1, Nc+1) with viewing angles."""
     nc1 = neb.ncells + 1
-    return (np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins + 1, nc1)))
+    na = n_angle(neb)
+    return (neb.nbins + 1, nc1) if na == 0 else (na + 1, neb.nbins + 1, nc1)
+
+
+def estimator_arrays(neb):
+    """Zeroed host accumulators: Jste, Jdif (nbins, Nc+1), escaped (escaped_shape)."""
+    nc1 = neb.ncells + 1
+    return (np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros(escaped_shape(neb)))

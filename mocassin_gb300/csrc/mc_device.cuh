@@ -23,7 +23,7 @@ constexpr int kMaxSources = 16;
 //  dust_cdf [nc+1][nb] float or null
 //  dx/dy/dz per-index cell widths / 1e15 (the dV factors of
 //           photon_mod.f90:1469-1512) at FP32 and FP64
-//  jste/jdif [nb][nc+1] double accumulators; esc [nb+1][nc+1] double
+//  jste/jdif [nb][nc+1] double accumulators; esc [n_angle+1][nb+1][nc+1] double
 struct DevGrid {
   int nx, ny, nz, nc, nb;
   const float *xa, *ya, *za;
@@ -44,6 +44,10 @@ struct DevGrid {
   int recursion_limit;
   int safe_limit;
   double *jste, *jdif, *esc;
+  // viewing angles of the escape SED (n_angle = 0: plane 0 only)
+  int n_angle, n_theta, n_phi;
+  float dtheta, dphi;     // Pi / totAngleBinsTheta, twoPi / totAngleBinsPhi (FP32)
+  const uint8_t *view;    // [n_theta+1][n_phi+1] viewpoint of each (theta, phi) bin, 0 = none
 };
 
 struct DevSource {
@@ -86,6 +90,40 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 __device__ __forceinline__ void raise_error(DevCounters *c, int code, long long packet) {
   if (atomicCAS(&c->error_code, 0, code) == 0) c->error_packet = (int)packet;
+}
+
+// Viewing-angle plane of an escaping packet (photon_mod.f90:372-412, and the
+// same code at the six escape sites of pathSegment): theta bin from acos of
+// the z cosine, phi bin from atan (not atan2) of y/x, both on |.| in a
+// symmetric octant, clamped to the last bin; the table holds the viewpoint
+// the reference's viewPointPtheta / viewPointPphi tests select (0 = none).
+// ok = false where the reference stops (a cosine outside [-1, 1]).
+template <typename Real>
+__device__ __forceinline__ int escape_view(const DevGrid &g, Real dx, Real dy, Real dz, bool &ok) {
+  const bool sym = g.flags & MC_FLAG_SYMMETRIC_XYZ;
+  const Real cz = sym ? fabs(dz) : dz;
+  ok = cz >= (Real)-1 && cz <= (Real)1;
+  if (!ok) return 0;
+  int it = (int)(acos(cz) / (Real)g.dtheta) + 1;
+  if (it > g.n_theta) it = g.n_theta;
+  int ip = 0;
+  if (!(fabs(dx) < (Real)1.e-35f)) {
+    const Real t = sym ? atan(fabs(dy) / fabs(dx)) : atan(dy / dx);
+    ip = (int)(t / (Real)g.dphi);
+  }
+  if (ip < 0) ip = g.n_phi + ip;
+  ip = ip + 1;
+  if (ip > g.n_phi) ip = g.n_phi;
+  ok = ip >= 1;
+  return ok ? (int)__ldg(g.view + it * (g.n_phi + 1) + ip) : 0;
+}
+
+// escapedPackets(origin, nuP, 0) += dE, and plane `view` too when view > 0.
+__device__ __forceinline__ void add_escape(const DevGrid &g, int origin, int nuP, int view, double de) {
+  if (!g.esc) return;
+  double *p = g.esc + origin + (long long)(g.nc + 1) * nuP;
+  atomicAdd(p, de);
+  if (view > 0) atomicAdd(p + (long long)(g.nc + 1) * (g.nb + 1) * view, de);
 }
 
 // Philox4x32-10, Salmon et al. (SC'11).

@@ -113,6 +113,8 @@ struct mc_ctx {
   DBuf xa, ya, za, active, opacity, sca, rec_raw, rec_cdf, dust_raw, dust_cdf, tlines, nu, gsca;
   DBuf dx32, dy32, dz32, dx64, dy64, dz64;
   DBuf jste, jdif, esc;
+  DBuf view;        // viewing-angle table (n_angle > 0)
+  int n_angle = 0;
   DBuf counters, src_cdf, replay;
   // chosen form: march-indexed views and the sorted packet queue
   int identity = 1;
@@ -136,7 +138,12 @@ mc_status check_grid(const mc_grid_t *g) {
     return set_error(MC_ERR_UNSUPPORTED, "nx, ny, nz must be >= 2 (1D grids are not supported): %d %d %d",
                      g->nx, g->ny, g->nz);
   if (g->ncells < 0 || g->nbins < 3) return set_error(MC_ERR_ARG, "bad ncells/nbins %d/%d", g->ncells, g->nbins);
-  if (g->n_angle != 0) return set_error(MC_ERR_UNSUPPORTED, "nAngleBins > 0 is not supported");
+  if (g->n_angle < 0 || g->n_angle > 2)
+    return set_error(MC_ERR_ARG, "nAngleBins must be 0..2 (set_input_mod.f90:537), got %d", g->n_angle);
+  if (g->n_angle > 0 && (!g->view_theta || !g->view_phi))
+    return set_error(MC_ERR_ARG, "nAngleBins > 0 needs view_theta and view_phi");
+  if (g->n_theta_bins < 0 || g->n_theta_bins > 254 || g->n_phi_bins < 0 || g->n_phi_bins > 254)
+    return set_error(MC_ERR_ARG, "angle bin counts must be 0..254");
   if (!g->x_axis || !g->y_axis || !g->z_axis || !g->active || !g->opacity || !g->nu_array)
     return set_error(MC_ERR_ARG, "grid axes/active/opacity/nu_array must be non-NULL");
   const bool gas = g->flags & MC_FLAG_GAS, dust = g->flags & MC_FLAG_DUST;
@@ -171,6 +178,51 @@ template <typename T> void widths(const float *ax, int n, bool sym, std::vector<
 mc_status upload(DBuf &b, const void *host, size_t bytes, cudaStream_t s) {
   MC_CUDA(b.alloc(bytes));
   if (host && bytes) MC_CUDA(cudaMemcpyAsync(b.p, host, bytes, cudaMemcpyHostToDevice, s));
+  return MC_OK;
+}
+
+// The viewpoint of every (theta, phi) escape bin, as initCartesianGrid sets
+// up viewPointPtheta / viewPointPphi (grid_mod.f90:416-468) and the escape
+// sites test them (photon_mod.f90:414-447): entry [it][ip] is the angle
+// plane that receives deltaE besides plane 0 (0 = none).
+mc_status view_table(const mc_grid_t *g, mcg::DevGrid &d, std::vector<uint8_t> &tab) {
+  const float pi = 3.141592654f, two_pi = 2.f * pi;  // constants_mod.f90:32-33
+  const int na = g->n_angle;
+  int nt = g->n_theta_bins > 0 ? g->n_theta_bins : 10;
+  int np = g->n_phi_bins > 0 ? g->n_phi_bins : 20;
+  std::vector<float> vth(g->view_theta, g->view_theta + na + 1), vph(g->view_phi, g->view_phi + na + 1);
+  const float dth = pi / (float)nt;
+  for (int i = 1; i <= na; ++i)
+    if (vph[i] < 0.f) {  // phi dependence off
+      np = 1;
+      for (float &v : vph) v = -1.f;
+      break;
+    }
+  const float dph = two_pi / (float)np;
+  std::vector<int> pt(nt + 1, 0), pp(np + 1, 0);
+  for (int i = 1; i <= na; ++i) {
+    if (vth[i] > pi / 2.f && (g->flags & MC_FLAG_SYMMETRIC_XYZ))
+      return set_error(MC_ERR_ARG, "viewing angle theta > pi/2 is not available for a symmetric grid");
+    const int it = (int)(vth[i] / dth) + 1, ip = (int)(vph[i] / dph) + 1;
+    if (it < 0 || it > nt || ip < 0 || ip > np)
+      return set_error(MC_ERR_ARG, "viewing angle %d (%g, %g) outside the angle bins", i, vth[i], vph[i]);
+    pt[it] = i;
+    pp[ip] = i;
+  }
+  tab.assign((size_t)(nt + 1) * (np + 1), 0);
+  for (int it = 1; it <= nt; ++it)
+    for (int ip = 1; ip <= np; ++ip) {
+      const int vt = pt[it], vp = pp[ip];
+      int v = 0;
+      if (vt > 0 && vph[vt] < 0.f) v = vt;
+      else if (vt == vp || vth[vp] == vth[vt] || vph[vt] == vph[vp]) v = vt;
+      tab[(size_t)it * (np + 1) + ip] = (uint8_t)v;
+    }
+  d.n_angle = na;
+  d.n_theta = nt;
+  d.n_phi = np;
+  d.dtheta = dth;
+  d.dphi = dph;
   return MC_OK;
 }
 
@@ -211,6 +263,19 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first) {
     if ((st = put(c->dust_raw, g->dust_pdf, plane))) return st;
     if (!c->dust_cdf.p) MC_CUDA(c->dust_cdf.alloc(plane));
     MC_CUDA(mcg::launch_cdf_transpose(c->dust_raw.as<float>(), c->dust_cdf.as<float>(), nc1, nb, s));
+  }
+  if (g->n_angle > 0) {
+    std::vector<uint8_t> tab;
+    if ((st = view_table(g, c->g, tab))) return st;
+    if (c->view.bytes != tab.size()) {
+      if (c->view.p) { cudaFree(c->view.p); c->view.p = nullptr; c->view.bytes = 0; }
+      MC_CUDA(c->view.alloc(tab.size()));
+    }
+    MC_CUDA(cudaMemcpyAsync(c->view.p, tab.data(), tab.size(), cudaMemcpyHostToDevice, s));
+    MC_CUDA(cudaStreamSynchronize(s));  // the host table goes out of scope
+    c->g.view = c->view.as<uint8_t>();
+  } else {
+    c->g.n_angle = 0;
   }
   return MC_OK;
 }
@@ -331,7 +396,9 @@ mc_status mc_ctx_create(const mc_grid_t *g, mc_ctx_t **out) {
       return fail(set_error(MC_ERR_NOMEM, "bins"));
   }
   if ((st = upload_arrays(c, g, true))) return fail(st);
-  const size_t nj = (size_t)(g->ncells + 1) * g->nbins, ne = (size_t)(g->ncells + 1) * (g->nbins + 1);
+  c->n_angle = g->n_angle;
+  const size_t nj = (size_t)(g->ncells + 1) * g->nbins;
+  const size_t ne = (size_t)(g->ncells + 1) * (g->nbins + 1) * (g->n_angle + 1);
   if (c->jste.alloc(nj * sizeof(double)) != cudaSuccess) return fail(set_error(MC_ERR_NOMEM, "Jste alloc"));
   if ((g->flags & MC_FLAG_DEBUG) && c->jdif.alloc(nj * sizeof(double)) != cudaSuccess)
     return fail(set_error(MC_ERR_NOMEM, "Jdif alloc"));
@@ -431,7 +498,7 @@ mc_status mc_ctx_update(mc_ctx_t *c, const mc_grid_t *g) {
   mc_status st = check_grid(g);
   if (st) return st;
   if (g->nx != c->nx || g->ny != c->ny || g->nz != c->nz || g->ncells != c->nc || g->nbins != c->nb ||
-      g->flags != c->flags)
+      g->flags != c->flags || g->n_angle != c->n_angle)
     return set_error(MC_ERR_ARG, "grid shape/flags differ from the context's");
   if ((st = upload_arrays(c, g, false))) return st;
   MC_CUDA(cudaStreamSynchronize(c->stream));
@@ -795,7 +862,7 @@ mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t n
   int dev = 0;
   cudaGetDevice(&dev);
   bool reuse = c && c->device == dev && c->nx == g->nx && c->ny == g->ny && c->nz == g->nz && c->nc == g->ncells &&
-               c->nb == g->nbins && c->flags == g->flags;
+               c->nb == g->nbins && c->flags == g->flags && c->n_angle == g->n_angle;
   if (reuse && (refresh_geometry(c, g) != MC_OK || upload_arrays(c, g, false) != MC_OK)) reuse = false;
   if (!reuse) {
     if (c) mc_ctx_destroy(c);

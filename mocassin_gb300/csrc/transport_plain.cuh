@@ -193,7 +193,13 @@ template <typename Real, int Layout = 0> struct History {
   }
 
   __device__ __forceinline__ void escape(const Pk<Real> &pk) {
-    if (g.esc) atomicAdd(g.esc + pk.origin + (long long)(g.nc + 1) * pk.nuP, (double)deltaE);
+    int view = 0;
+    if (g.n_angle > 0) {
+      bool ok;
+      view = escape_view<Real>(g, pk.dir.x, pk.dir.y, pk.dir.z, ok);
+      if (!ok) { fail(MC_ERR_NAN); return; }
+    }
+    add_escape(g, pk.origin, pk.nuP, view, (double)deltaE);
     ++lc.escaped;
   }
   __device__ __forceinline__ void addJ(const Pk<Real> &pk, int a, Real v) {

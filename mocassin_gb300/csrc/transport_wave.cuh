@@ -153,6 +153,11 @@ __device__ __forceinline__ bool sample_direction(RStream<Replay> &st, uint32_t k
   return true;
 }
 
+// origin(2) of a stellar packet: the active cell of the star
+__device__ __forceinline__ int origin_of(const DevGrid &g, const DevSource &src) {
+  return __ldg(g.active + (src.cell[0] - 1) + (long long)g.nx * ((src.cell[1] - 1) + (long long)g.ny * (src.cell[2] - 1)));
+}
+
 // ------------------------------------------------------------ round 0 sample
 template <typename Real, bool Replay>
 __global__ void __launch_bounds__(256) wave_sample_stellar_kernel(const __grid_constant__ DevGrid g,
@@ -167,6 +172,8 @@ __global__ void __launch_bounds__(256) wave_sample_stellar_kernel(const __grid_c
   for (int i = threadIdx.x; i < nh; i += blockDim.x) sh[i] = 0u;
   __syncthreads();
   const bool gas_only = !(g.flags & MC_FLAG_DUST);
+  const bool fold = (g.flags & MC_FLAG_SYMMETRIC_XYZ) && !(g.flags & MC_FLAG_MULTISTARS);
+  unsigned long long nesc_direct = 0;
   double q = 0.0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long gp = (long long)blockIdx.x * blockDim.x + threadIdx.x; gp < S.total; gp += stride) {
@@ -184,8 +191,19 @@ __global__ void __launch_bounds__(256) wave_sample_stellar_kernel(const __grid_c
     const Real nu = (Real)__ldg(g.nu + nuP - 1);
     if (nu > (Real)1) q += (double)((Real)src.delta_e / ((Real)2.1799153e-11f * nu));
     if (gas_only && nu < (Real)g.ion_edge1) {
-      atomicAdd(&hesc[s * g.nb + nuP], 1u);
       w.s_nu[gp] = 0xFFFFu;
+      if (g.n_angle > 0) {
+        // the direction initPhotonPacket drew picks the viewing-angle plane
+        R3<Real> d;
+        bool ok = sample_direction<Real, Replay>(st, src.k0, src.k1, d);
+        if (fold) { d.x = fabs(d.x); d.y = fabs(d.y); d.z = fabs(d.z); }
+        const int view = ok ? escape_view<Real>(g, d.x, d.y, d.z, ok) : 0;
+        if (!ok || st.exhausted) { raise_error(cnt, st.exhausted ? MC_ERR_REPLAY : MC_ERR_NAN, gp); continue; }
+        add_escape(g, origin_of(g, src), nuP, view, (double)(Real)src.delta_e);
+        ++nesc_direct;
+      } else {
+        atomicAdd(&hesc[s * g.nb + nuP], 1u);
+      }
     } else {
       atomicAdd(&hcount[nuP], 1u);
       w.s_nu[gp] = (uint16_t)nuP;
@@ -203,12 +221,10 @@ __global__ void __launch_bounds__(256) wave_sample_stellar_kernel(const __grid_c
     if (!c) continue;
     const int s = i / g.nb, nuP = i % g.nb;
     const DevSource &src = S.s[s];
-    const int origin = __ldg(g.active + (src.cell[0] - 1) +
-                             (long long)g.nx * ((src.cell[1] - 1) + (long long)g.ny * (src.cell[2] - 1)));
-    if (g.esc) atomicAdd(g.esc + origin + (long long)(g.nc + 1) * nuP, (double)c * (double)(Real)src.delta_e);
+    if (g.esc) atomicAdd(g.esc + origin_of(g, src) + (long long)(g.nc + 1) * nuP, (double)c * (double)(Real)src.delta_e);
     nesc += c;
   }
-  nesc = warp_sum(nesc);
+  nesc = warp_sum(nesc + nesc_direct);
   if ((threadIdx.x & 31) == 0 && nesc) atomicAdd(&cnt->escaped, nesc);
 }
 
@@ -259,9 +275,16 @@ __global__ void __launch_bounds__(256) wave_sample_reemit_kernel(const __grid_co
       continue;
     }
     if (!dust && (Real)__ldg(g.nu + nuP - 1) < (Real)g.ion_edge1) {
-      // escapes before any march; the direction draws of initPhotonPacket
-      // are not needed since the history ends here
-      if (g.esc) atomicAdd(g.esc + a + (long long)(g.nc + 1) * nuP, (double)(Real)src.delta_e);
+      // escapes before any march; the direction initPhotonPacket draws is
+      // needed only for the viewing-angle plane
+      int view = 0;
+      if (g.n_angle > 0) {
+        R3<Real> d;
+        ok = sample_direction<Real, Replay>(st, src.k0, src.k1, d);
+        if (ok) view = escape_view<Real>(g, d.x, d.y, d.z, ok);
+        if (!ok || st.exhausted) { raise_error(cnt, st.exhausted ? MC_ERR_REPLAY : MC_ERR_NAN, id); continue; }
+      }
+      add_escape(g, a, nuP, view, (double)(Real)src.delta_e);
       ++nesc;
       if (trapped_at_end) ++ntrap;
       continue;
@@ -401,7 +424,13 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     valid = false;
   }
   __device__ __forceinline__ void escape() {
-    if (g.esc) atomicAdd(g.esc + origin + (long long)(g.nc + 1) * nuP, (double)(Real)source().delta_e);
+    int view = 0;
+    if (g.n_angle > 0) {
+      bool ok;
+      view = escape_view<Real>(g, v.x, v.y, v.z, ok);
+      if (!ok) { fail(MC_ERR_NAN); return; }
+    }
+    add_escape(g, origin, nuP, view, (double)(Real)source().delta_e);
     ++lc.escaped;
     end_history();
   }

@@ -183,6 +183,9 @@ class NebulaSpec:
     dust_to_gas: float = 0.01
     line_fraction: float = 0.6
     nbins_stride: int = 1       # keep every k-th bin of the 600-bin grid
+    views: tuple = ()           # viewing angles ((theta, phi) rad, at most 2; phi < 0 = no phi)
+    n_theta_bins: int = 0       # totAngleBinsTheta (0 = 10)
+    n_phi_bins: int = 0         # totAngleBinsPhi (0 = 20)
 
 
 @dataclasses.dataclass

@@ -80,6 +80,15 @@ def _dptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _check_shapes(neb, jste, jdif, escaped):
+    nj = (neb.nbins, neb.ncells + 1)
+    for name, a, shape in (("jste", jste, nj), ("jdif", jdif, nj), ("escaped", escaped, abi.escaped_shape(neb))):
+        if a is None:
+            continue
+        if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("%s must be a C-contiguous float64 array of shape %s" % (name, shape))
+
+
 def _flags(form, zero_first=False):
     if form not in ("wave", "plain"):
         raise ValueError("form must be 'wave' or 'plain'")
@@ -104,6 +113,7 @@ def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp
     js0, jd0, es0 = abi.estimator_arrays(neb)
     jste = js0 if jste is None else jste
     escaped = es0 if escaped is None else escaped
+    _check_shapes(neb, jste, jdif, escaped)
     if jdif is None and (neb.flags & abi_flag_debug()):
         jdif = jd0
     st = abi.McStats()
@@ -177,6 +187,7 @@ class TransportContext:
         js0, jd0, es0 = abi.estimator_arrays(self.neb)
         jste = js0 if jste is None else jste
         escaped = es0 if escaped is None else escaped
+        _check_shapes(self.neb, jste, jdif, escaped)
         _check(self.lib.mc_ctx_download(self.handle, _dptr(jste), _dptr(jdif), _dptr(escaped), int(accumulate)))
         return jste, jdif, escaped
 

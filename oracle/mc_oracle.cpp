@@ -15,7 +15,7 @@
 //   hg                   source/photon_mod.f90:2875-3101
 //   randomUnitVector     source/vector_mod.f90:303-314
 // for a single mother grid (nGrids = 1, no sub-grids), no plane-parallel
-// ionisation, no 1D mode and nAngleBins = 0 (escape into angle bin 0).  The
+// ionisation and no 1D mode.  The
 // Fortran intrinsic random_number is replaced by one of two draw sources:
 // Philox4x32-10 (Salmon et al., SC'11) keyed by (seed, iteration, star) with
 // the packet index in the counter, or a replay buffer of draws.
@@ -168,12 +168,75 @@ template <typename Real, typename Acc> struct Problem {
 #pragma omp atomic
     *p += (Acc)v;
   }
-  void addEsc(int c, int nu, double de) {
+  // escapedPackets(0:Nc, 0:Nnu, 0:nAngle), cell fastest
+  void addEsc(int c, int nu, int plane, double de) {
     if (!esc) return;
-    // escapedPackets(0:Nc, 0:Nnu, 0:nAngle): bin 0 only
-    Acc *p = esc + c + (int64_t)(nc + 1) * nu;
+    Acc *p = esc + c + (int64_t)(nc + 1) * nu + (int64_t)(nc + 1) * (nb + 1) * plane;
 #pragma omp atomic
     *p += (Acc)(Real)de;
+  }
+
+  // viewing angles: initCartesianGrid, grid_mod.f90:416-468
+  int nAngle = 0, nTheta = 10, nPhi = 20;
+  float dTheta = 0.f, dPhi = 0.f;
+  std::vector<int> ptheta, pphi;          // viewPointPtheta(0:nTheta), viewPointPphi(0:nPhi)
+  std::vector<float> vTheta, vPhi;        // viewPointTheta / viewPointPhi(0:nAngle)
+  int setupViews() {
+    nAngle = g->n_angle;
+    if (nAngle == 0) return 0;
+    const float pi = 3.141592654f, twoPi = 2.f * pi;
+    nTheta = g->n_theta_bins > 0 ? g->n_theta_bins : 10;
+    nPhi = g->n_phi_bins > 0 ? g->n_phi_bins : 20;
+    vTheta.assign(g->view_theta, g->view_theta + nAngle + 1);
+    vPhi.assign(g->view_phi, g->view_phi + nAngle + 1);
+    dTheta = pi / (float)nTheta;
+    for (int i = 1; i <= nAngle; ++i) {
+      if (vPhi[i] < 0.f) {
+        nPhi = 1;
+        for (auto &v : vPhi) v = -1.f;
+        break;
+      }
+    }
+    dPhi = twoPi / (float)nPhi;
+    ptheta.assign(nTheta + 1, 0);
+    pphi.assign(nPhi + 1, 0);
+    for (int i = 1; i <= nAngle; ++i) {
+      if (vTheta[i] > pi / 2.f && sym) return MC_ERR_ARG;
+      const int a = (int)(vTheta[i] / dTheta) + 1, b = (int)(vPhi[i] / dPhi) + 1;
+      if (a < 0 || a > nTheta || b < 0 || b > nPhi) return MC_ERR_ARG;
+      ptheta[a] = i;
+      pphi[b] = i;
+    }
+    return 0;
+  }
+  // the escape record of photon_mod.f90:372-462 (same at every escape site):
+  // false where the reference stops
+  bool escapeRecord(int origin, int nuP, Real dx, Real dy, Real dz, double de) {
+    if (nAngle == 0) { addEsc(origin, nuP, 0, de); return true; }
+    const Real cz = sym ? std::fabs(dz) : dz;
+    if (!(cz >= (Real)-1 && cz <= (Real)1)) return false;  // acos -> NaN
+    int idirT = (int)(std::acos(cz) / (Real)dTheta) + 1;
+    if (idirT > nTheta) idirT = nTheta;
+    if (idirT < 1 || idirT > nTheta) return false;
+    int idirP;
+    if (std::fabs(dx) < (Real)1.e-35f) idirP = 0;
+    else if (sym) idirP = (int)(std::atan(std::fabs(dy) / std::fabs(dx)) / (Real)dPhi);
+    else idirP = (int)(std::atan(dy / dx) / (Real)dPhi);
+    if (idirP < 0) idirP = nPhi + idirP;
+    idirP = idirP + 1;
+    if (idirP > nPhi) idirP = nPhi;
+    if (idirP < 1 || idirP > nPhi) return false;
+    const int vt = ptheta[idirT], vp = pphi[idirP];
+    if (vt > 0 && vPhi[vt] < 0.f) {
+      addEsc(origin, nuP, vt, de);
+      addEsc(origin, nuP, 0, de);
+    } else if (vt == vp || vTheta[vp] == vTheta[vt] || vPhi[vt] == vPhi[vp]) {
+      addEsc(origin, nuP, vt, de);
+      if (vt != 0) addEsc(origin, nuP, 0, de);
+    } else {
+      addEsc(origin, nuP, 0, de);
+    }
+    return true;
   }
   void fail(int code, int64_t packet) {
     int z = 0;
@@ -327,7 +390,7 @@ template <typename Real, typename Acc> class Runner {
   }
 
   void escape(const Packet<Real> &pk) {
-    P.addEsc(pk.origin, pk.nuP, (double)deltaE);
+    if (!P.escapeRecord(pk.origin, pk.nuP, pk.dir.x, pk.dir.y, pk.dir.z, (double)deltaE)) { P.fail(MC_ERR_NAN, gpacket); return; }
     P.escaped.fetch_add(1, std::memory_order_relaxed);
   }
 
@@ -676,7 +739,8 @@ int run(const mc_grid_t *g, const mc_source_t *src, int nsrc, const mc_run_opts_
   P.safeLimit = o->safe_limit > 0 ? o->safe_limit : 500000;
 
   const int64_t nj = (int64_t)(P.nc + 1) * P.nb;
-  const int64_t ne = (int64_t)(P.nc + 1) * (P.nb + 1);
+  if (P.setupViews()) return MC_ERR_ARG;
+  const int64_t ne = (int64_t)(P.nc + 1) * (P.nb + 1) * (g->n_angle + 1);
   std::vector<Acc> aj, ad, ae;
   const bool direct = sizeof(Acc) == sizeof(double);
   if (direct) {
@@ -746,7 +810,7 @@ int oracle_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsr
                          const mc_run_opts_t *o, double *jste, double *jdif, double *esc,
                          mc_stats_t *st, int32_t nthreads, int32_t acc32) {
   if (!g || !src || !o || !jste || nsrc < 0) return MC_ERR_ARG;
-  if (g->n_angle != 0) return MC_ERR_UNSUPPORTED;
+  if (g->n_angle < 0 || g->n_angle > 2 || (g->n_angle > 0 && (!g->view_theta || !g->view_phi))) return MC_ERR_ARG;
   if (o->rng == MC_RNG_REPLAY && (!o->replay || o->replay_stride <= 0)) return MC_ERR_ARG;
   if (o->precision == MC_PREC_FP64)
     return run<double, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads);

@@ -78,4 +78,5 @@ def with_opacity(neb, opacity):
 
 def zeros_like_estimators(neb):
     nc1 = neb.ncells + 1
-    return np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins + 1, nc1))
+    from mocassin_gb300 import abi
+    return np.zeros((neb.nbins, nc1)), np.zeros((neb.nbins, nc1)), np.zeros(abi.escaped_shape(neb))

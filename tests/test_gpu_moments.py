@@ -6,14 +6,13 @@ Tensor-core path (split BF16, FP32 accumulate): 3e-5 relative per element
 import numpy as np
 import pytest
 
-from mocassin_gb300 import nebula, transport
+from mocassin_gb300 import nebula, rates, transport
 from oracle import rates_oracle, runner
-
-pytestmark = pytest.mark.gpu
 
 TOL = 3e-5
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("spec", [nebula.small_cases()[1], nebula.small_cases()[2], nebula.small_cases()[3]],
                          ids=lambda s: s.name)
 def test_photoionisation_sums_match_the_oracle(gpu_lib, spec):
@@ -25,7 +24,10 @@ def test_photoionisation_sums_match_the_oracle(gpu_lib, spec):
     w = rates_oracle.photo_weights(neb.xs, neb.nu).astype(np.float32)
     scale = 1e-9 / (8.0 if sym else 1.0)
     got, ms = ctx.jste_moments(w, scale)
+    nps = rates.n_photo(ctx, neb.xs, neb.nu, sym)
     ctx.close()
+    onps = rates_oracle.n_photo(js, neb.xs, neb.nu, sym)
+    assert np.all(np.abs(nps - onps) <= TOL * onps)
     ref = rates_oracle.moments(js, w, scale)
     err = np.abs(got.astype(np.float64) - ref)
     assert np.all(err <= TOL * np.abs(ref) + 1e-300), float((err / (np.abs(ref) + 1e-300)).max())
@@ -34,6 +36,7 @@ def test_photoionisation_sums_match_the_oracle(gpu_lib, spec):
     np.testing.assert_allclose(rates_oracle.moments(ojs, w, scale), ref, rtol=1e-12)
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("nout", [1, 16, 33, 64])
 def test_moments_of_random_weights(gpu_lib, nout):
     neb = nebula.build(nebula.small_cases()[0])
@@ -46,3 +49,9 @@ def test_moments_of_random_weights(gpu_lib, nout):
     ref = rates_oracle.moments(js, w, 0.5)
     err = np.abs(got.astype(np.float64) - ref)
     assert np.all(err <= TOL * np.abs(ref) + 1e-300)
+
+
+def test_host_weight_table_matches_the_oracle_formula():
+    neb = nebula.build(nebula.small_cases()[0])
+    np.testing.assert_allclose(rates.photo_weights(neb.xs, neb.nu),
+                               rates_oracle.photo_weights(neb.xs, neb.nu), rtol=1e-7)
