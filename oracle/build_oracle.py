@@ -13,12 +13,16 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmc_oracle.so")
 
 
+SOURCES = ("mc_oracle.cpp", "update_oracle.cpp")
+
+
 def build(force=False):
     os.makedirs(OUT, exist_ok=True)
-    src = os.path.join(HERE, "mc_oracle.cpp")
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
     hdr = os.path.join(os.path.dirname(HERE), "include", "mocassin_gpu.h")
-    if force or not os.path.exists(LIB) or max(os.path.getmtime(src), os.path.getmtime(hdr)) > os.path.getmtime(LIB):
-        cmd = ["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-o", LIB, src]
+    newest = max([os.path.getmtime(s) for s in srcs] + [os.path.getmtime(hdr)])
+    if force or not os.path.exists(LIB) or newest > os.path.getmtime(LIB):
+        cmd = ["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-o", LIB] + srcs
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("oracle build failed:\n" + p.stderr)
