@@ -243,8 +243,8 @@ mc_status mc_ctx_build_opacity(mc_ctx_t *ctx, int32_t nspecies, const float *den
                                const float *ff, int32_t method, int32_t sca, double *kernel_ms);
 
 /* ---- moments of the estimator for the cell update -------------------------
- * out(o, cell) = scale * sum_nu Jste(nu, cell) * w(nu, o), o < nout <= 64, on
- * the context's device Jste after mc_ctx_run: the photoionisation sums of
+ * out(o, cell) = scale * sum_nu Jste(nu, cell) * w(nu, o), o < nout, on
+ * the context's device Jste after mc_ctx_run (nout <= 128): the photoionisation sums of
  * updateCell (source/update_mod.f90:175-269, with w = phXSec / (hcRyd nu)
  * and scale the normalisation of iteration_mod.f90:705-724; the reference
  * adds 1e-20 afterwards) and the heating sums of its thermal balance have
@@ -252,6 +252,74 @@ mc_status mc_ctx_build_opacity(mc_ctx_t *ctx, int32_t nspecies, const float *den
  * Tensor cores (tcgen05, split BF16, FP32 accumulate): ~1e-5 relative. */
 mc_status mc_ctx_jste_moments(mc_ctx_t *ctx, int32_t nout, const float *w, double scale, float *out,
                               double *kernel_ms);
+
+/* ---- the cell update (ionisation and thermal balance) ----------------------
+ * updateCell (source/update_mod.f90:15-525) for every active cell of the
+ * context, in FP64 on the GPU, after a transport: one warp per cell runs the
+ * reference's bracketed secant in Te (iterateT, <= 25 steps) around its
+ * ionisation balance (ionBalance, <= 25 passes) and thermal balance
+ * (thermBalance with the multi-level forbidden-line cooling of equilibrium,
+ * emission_mod.f90:1913-2115), for H, He, C, N, O, Ne, S at nstages = 7.
+ * The photoionisation and heating sums come from the resident Jste through
+ * the moment kernel (weights w, see mocassin_gb300/balance.py).  The cell
+ * state stays on the GPU between calls. */
+typedef struct mc_update_tables {
+  const double *rrec;        /* [2][31][31] radRecFit power laws (radrec.dat)  */
+  const double *rnew;        /* [4][31][31] Verner & Ferland fits              */
+  const double *direc;       /* [ndirec][8] dielectronic.dat rows              */
+  int32_t ndirec;
+  const double *aldro;       /* [naldro][6] aldrovandi.dat rows                */
+  int32_t naldro;
+  int32_t ncel;              /* ions with forbidden-line data                  */
+  const int32_t *cel_key;    /* [ncel][2] (Z, ion stage)                       */
+  const int32_t *cel_nlev;   /* levels (<= 17)                                 */
+  const int32_t *cel_ntemp;  /* collision-strength temperatures (<= 32)        */
+  const double *cel_logt;    /* [ncel][32] log10 T                              */
+  const double *cel_qom;     /* [ncel][32][18][18] (T, lower, upper)           */
+  const double *cel_a;       /* [ncel][18][18] a[upper][lower] A values [1/s]  */
+  const double *cel_g;       /* [ncel][18] statistical weights                 */
+  const double *cel_e;       /* [ncel][18] level energies [1/cm]               */
+  const double *cel_br, *cel_z;
+  const double *cel_ar;      /* [ncel][4]                                      */
+  const double *cel_ad;      /* [ncel][5]                                      */
+} mc_update_tables_t;
+
+typedef struct mc_update_stats {
+  int64_t hit;               /* cells reached by a packet (updated)            */
+  int64_t converged;         /* |dX(H0)/X(H0)| <= xhi_limit                    */
+  int64_t no_te_balance;     /* noTeBal: 25 T steps without balance            */
+  int64_t no_ion_balance;    /* noIonBal                                       */
+  int64_t t_iterations;      /* sum of T steps over the hit cells              */
+  double dte_max;            /* max |Te_new - Te_old| / Te_old over hit cells  */
+  double frac_dte_1pc;       /* fraction of hit cells with |dTe| / Te < 1 %    */
+  double moments_ms, update_ms;
+} mc_update_stats_t;
+
+/* Uploads the atomic tables, the per-cell Hden and the abundances of
+ * H, He, C, N, O, Ne, S (number, relative to H). */
+mc_status mc_ctx_set_update_tables(mc_ctx_t *ctx, const mc_update_tables_t *tables, const double *hden,
+                                   const double *abund);
+/* Cell state: te, ne [Nc+1]; ionden [Nc+1][7][8] (element, stage 1..7). */
+mc_status mc_ctx_set_cell_state(mc_ctx_t *ctx, const double *te, const double *ne, const double *ionden);
+mc_status mc_ctx_get_cell_state(mc_ctx_t *ctx, double *te, double *ne, double *ionden, int32_t *conv,
+                                int32_t *niter, int32_t *flags);
+/* One update of every cell from the resident Jste: w [nbins][67] (column 0
+ * = 1, then the photoionisation and the heating weights of the 33 balance
+ * ions), scale = the Jste normalisation (1e-9, / 8 for a symmetric octant).
+ * precision MC_PREC_FP64: the FP64 method (follows the FP64 oracle to
+ * ~1e-9); MC_PREC_FP32: the same steps in 4-byte floats, the precision of
+ * the reference's own updateCell (`real`), ~64x the FP64 rate on GB300. */
+mc_status mc_ctx_update_cells(mc_ctx_t *ctx, const float *w, double scale, double xhi_limit, int32_t precision,
+                              mc_update_stats_t *stats);
+/* Rebuilds the resident opacity from the cell state: den[k][cell] =
+ * ionden(elem_k, stage_k) * abund(elem_k) * Hden(cell) for the nspecies rows
+ * (elem, stage) = species[k], then the contraction with xs [nspecies][nbins]
+ * as mc_ctx_build_opacity. */
+mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32_t *species, const float *xs,
+                                    int32_t method, double *kernel_ms);
+
+/* Copies the resident opacity [nbins][Nc+1] (cell fastest) to the host. */
+mc_status mc_ctx_get_opacity(mc_ctx_t *ctx, float *opacity);
 
 /* ---- allocation-free transport ------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

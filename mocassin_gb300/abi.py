@@ -59,6 +59,45 @@ class McStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class McUpdateTables(C.Structure):
+    _fields_ = [("rrec", _dp), ("rnew", _dp), ("direc", _dp), ("ndirec", C.c_int32), ("aldro", _dp),
+                ("naldro", C.c_int32), ("ncel", C.c_int32), ("cel_key", _ip), ("cel_nlev", _ip),
+                ("cel_ntemp", _ip), ("cel_logt", _dp), ("cel_qom", _dp), ("cel_a", _dp), ("cel_g", _dp),
+                ("cel_e", _dp), ("cel_br", _dp), ("cel_z", _dp), ("cel_ar", _dp), ("cel_ad", _dp)]
+
+
+class McUpdateStats(C.Structure):
+    _fields_ = [("hit", C.c_int64), ("converged", C.c_int64), ("no_te_balance", C.c_int64),
+                ("no_ion_balance", C.c_int64), ("t_iterations", C.c_int64), ("dte_max", C.c_double),
+                ("frac_dte_1pc", C.c_double), ("moments_ms", C.c_double), ("update_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def update_tables_struct(t):
+    """McUpdateTables over the arrays of mocassin_gb300.balance.tables()."""
+    keep = {}
+
+    def d(name):
+        a = np.ascontiguousarray(t[name], dtype=np.float64)
+        keep[name] = a
+        return a.ctypes.data_as(_dp)
+
+    def i(name):
+        a = np.ascontiguousarray(t[name], dtype=np.int32)
+        keep[name] = a
+        return a.ctypes.data_as(_ip)
+
+    s = McUpdateTables(rrec=d("rrec"), rnew=d("rnew"), direc=d("direc"), ndirec=len(t["direc"]),
+                       aldro=d("aldro"), naldro=len(t["aldro"]), ncel=len(t["cel_key"]), cel_key=i("cel_key"),
+                       cel_nlev=i("cel_nlev"), cel_ntemp=i("cel_ntemp"), cel_logt=d("cel_logt"),
+                       cel_qom=d("cel_qom"), cel_a=d("cel_a"), cel_g=d("cel_g"), cel_e=d("cel_e"),
+                       cel_br=d("cel_br"), cel_z=d("cel_z"), cel_ar=d("cel_ar"), cel_ad=d("cel_ad"))
+    s._keep = keep
+    return s
+
+
 def _ptr(a, ctype):
     if a is None:
         return C.cast(None, C.POINTER(ctype))

@@ -28,6 +28,8 @@ UNITS = [
     ("transport_noalloc.cu", ["-fmad=false"]),
     ("opacity.cu", []),
     ("jmoments.cu", []),
+    ("cellupdate.cu", ["-fmad=false", "-Xcompiler=-ffp-contract=off"]),
+    ("cellupdate_fp32.cu", []),
 ]
 
 

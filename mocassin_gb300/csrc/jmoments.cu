@@ -33,7 +33,7 @@ constexpr int kJM = 128;  // cells per tile
 constexpr int kJK = 64;   // bins per chunk
 
 struct JMomentArgs {
-  int nc1, nb, nout, N;  // N = nout rounded up to 16
+  int nc1, nb, nout, N;  // N = nout rounded up to 16 (<= 128)
   const double *J;       // [nb][nc1]
   const float *W;        // [nb][nout]
   double scale;
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(128, 4) jmoment_tc_kernel(const __grid_constan
   uint64_t *bar = (uint64_t *)(sm + 2 * abytes + 2 * bbytes);
   uint32_t *tslot = (uint32_t *)(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t ncols = a.N <= 32 ? 32u : 64u;
+  const uint32_t ncols = a.N <= 32 ? 32u : (a.N <= 64 ? 64u : 128u);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");

@@ -115,6 +115,13 @@ struct mc_ctx {
   DBuf jste, jdif, esc;
   DBuf view;        // viewing-angle table (n_angle > 0)
   int n_angle = 0;
+  // cell update: atomic tables, per-cell state and scratch
+  DBuf u_bal, u_cel, u_rrec, u_rnew, u_direc, u_aldro, u_logt, u_g, u_e, u_A, u_qq, u_q2, u_ab, u_hden;
+  DBuf f_bal, f_cel, f_rrec, f_rnew, f_direc, f_aldro, f_logt, f_g, f_e, f_A, f_qq, f_q2, f_ab;  // float copies
+  DBuf s_te, s_ne, s_X, s_conv, s_niter, s_flags, s_dte, s_mom, s_w, s_ustats, s_err, s_den, s_xs, s_spe, s_sps;
+  int u_ncel = 0, u_ndirec = 0, u_naldro = 0, u_maxlev = 1;
+  int u_bal_z[7] = {}, u_bal_first[7] = {};
+  bool u_ready = false, s_ready = false;
   DBuf counters, src_cdf, replay;
   // chosen form: march-indexed views and the sorted packet queue
   int identity = 1;
@@ -808,7 +815,7 @@ extern "C" mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t 
 extern "C" mc_status mc_ctx_jste_moments(mc_ctx_t *c, int32_t nout, const float *w, double scale, float *out,
                                           double *kernel_ms) {
   if (!c || !w || !out) return set_error(MC_ERR_ARG, "ctx, w and out are required");
-  if (nout < 1 || nout > 64) return set_error(MC_ERR_ARG, "nout must be 1..64 (got %d)", nout);
+  if (nout < 1 || nout > 128) return set_error(MC_ERR_ARG, "nout must be 1..128 (got %d)", nout);
   const int nc1 = c->nc + 1, nb = c->nb;
   DBuf dw, dout, err;
   MC_CUDA(dw.alloc((size_t)nb * nout * sizeof(float)));
@@ -848,6 +855,380 @@ extern "C" mc_status mc_ctx_build_opacity(mc_ctx_t *c, int32_t nspecies, const f
                                     c->stream));
     MC_CUDA(cudaStreamSynchronize(c->stream));
   }
+  return MC_OK;
+}
+
+// ---------------------------------------------------------------- cell update
+namespace {
+
+constexpr int kUZ[7] = {1, 2, 6, 7, 8, 10, 16};
+constexpr int kUNL = 18, kUNT = 32;
+
+mc_status put_buf(DBuf &b, const void *h, size_t bytes, cudaStream_t s) {
+  if (b.p && b.bytes != bytes) { cudaFree(b.p); b.p = nullptr; b.bytes = 0; }
+  if (!b.p) MC_CUDA(b.alloc(bytes));
+  if (h && bytes) MC_CUDA(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, s));
+  return MC_OK;
+}
+
+// chex(elem, ion, 1:4) of ionBalance (update_mod.f90:1400-1460) for the
+// benchmark elements
+void chex_coeff(int z, int ion, double c[4]) {
+  c[0] = c[1] = c[2] = c[3] = 0.;
+  auto set = [&](double a, double b, double d, double e) { c[0] = a; c[1] = b; c[2] = d; c[3] = e; };
+  switch (z * 100 + ion) {
+    case 201: set(7.47e-6, 2.06, 9.93, -3.89); break;
+    case 202: set(1.e-5, 0., 0., 0.); break;
+    case 601: set(1.76e-9, 8.33, 4278.78, -6.41); break;
+    case 602: set(1.67e-4, 2.79, 304.72, -4.07); break;
+    case 603: set(3.25, 0.21, 0.19, -3.29); break;
+    case 604: set(332.46, -0.11, -0.995, -1.58e-3); break;
+    case 701: set(1.01e-3, -0.29, -0.92, -8.38); break;
+    case 702: set(3.05e-1, 0.60, 2.65, -0.93); break;
+    case 703: set(4.54, 0.57, -0.65, -0.89); break;
+    case 704: set(3.28, 0.52, -0.52, -0.19); break;
+    case 801: set(1.04, 3.15e-2, -0.61, -9.73); break;
+    case 802: set(1.04, 0.27, 2.02, -5.92); break;
+    case 803: set(3.98, 0.26, 0.56, -2.62); break;
+    case 804: set(2.52e-1, 0.63, 2.08, -4.16); break;
+    case 1002: set(1.e-5, 0., 0., 0.); break;
+    case 1003: set(14.73, 4.52e-2, -0.84, -0.31); break;
+    case 1004: set(6.47, 0.54, 3.59, -5.22); break;
+    case 1601: set(3.82e-7, 11.10, 2.57e4, -8.22); break;
+    case 1602: set(1.e-5, 0., 0., 0.); break;
+    case 1603: set(2.29, 4.02e-2, 1.59, -6.06); break;
+    case 1604: set(6.44, 0.13, 2.69, -5.69); break;
+    default: break;
+  }
+  c[0] *= 1.e-9;
+}
+
+// g0 / g1 of getOuterShell (hydro_mod.f90:89-182) for z <= 20
+double g0g1_of(int nElec) {
+  static const int gl[30] = {2, 1, 2, 1, 6, 9, 4, 9, 6, 1, 2, 1, 6, 9, 4, 9, 6, 1, 2, 1,
+                             10, 21, 28, 7, 6, 25, 28, 21, 2, 1};
+  const int g0 = gl[nElec - 1], g1 = nElec == 1 ? 1 : gl[nElec - 2];
+  return (double)g0 / (double)g1;
+}
+
+int elem_index(int z) {
+  for (int e = 0; e < 7; ++e)
+    if (kUZ[e] == z) return e;
+  return -1;
+}
+
+}  // namespace
+
+extern "C" mc_status mc_ctx_set_update_tables(mc_ctx_t *c, const mc_update_tables_t *t, const double *hden,
+                                              const double *abund) {
+  if (!c || !t || !hden || !abund) return set_error(MC_ERR_ARG, "ctx, tables, hden and abund are required");
+  if (!t->rrec || !t->rnew || !t->direc || !t->aldro || t->ndirec < 0 || t->naldro < 0)
+    return set_error(MC_ERR_ARG, "update tables: recombination data missing");
+  if (t->ncel < 0 || t->ncel > 32) return set_error(MC_ERR_ARG, "update tables: ncel must be 0..32 (got %d)", t->ncel);
+  cudaStream_t s = c->stream;
+  std::vector<mcg::UpdIonDev> bal;
+  int b = 0;
+  for (int e = 0; e < 7; ++e) {
+    const int z = kUZ[e], ni = std::min(z, 6);
+    c->u_bal_z[e] = z;
+    c->u_bal_first[e] = b;
+    for (int ion = 1; ion <= ni; ++ion, ++b) {
+      mcg::UpdIonDev d{};
+      d.z = z; d.ion = ion; d.e = e; d.nelec = z - ion + 1;
+      chex_coeff(z, ion, d.chex);
+      d.dek = (z == 7 && ion == 1) ? 10863. : (z == 8 && ion == 1) ? 2205. : 0.;
+      d.g0g1 = g0g1_of(d.nelec);
+      // the dielectronic rows of (z, ion) and of (O, ion), in file order
+      auto rows_for = [&](int zz, int *dr, int &ndr, int &ar) -> bool {
+        ndr = 0;
+        ar = -1;
+        for (int i = 0; i < t->ndirec; ++i) {
+          const int el = (int)t->direc[8 * i], n = (int)t->direc[8 * i + 1];
+          if (el != zz || el + 1 - n != ion) continue;
+          if (ndr == 4) return false;
+          dr[ndr++] = i;
+        }
+        for (int i = 0; i < t->naldro; ++i) {
+          const int el = (int)t->aldro[6 * i], n = (int)t->aldro[6 * i + 1];
+          if (el == zz && el + 1 - n == ion) ar = i;
+        }
+        return true;
+      };
+      if (!rows_for(z, d.dr, d.ndr, d.ar) || !rows_for(8, d.dr8, d.ndr8, d.ar8))
+        return set_error(MC_ERR_ARG, "update tables: more than 4 dielectronic rows for one ion");
+      bal.push_back(d);
+    }
+  }
+  const int ncel = t->ncel;
+  std::vector<mcg::UpdCelDev> cel(ncel);
+  std::vector<double> q2((size_t)std::max(ncel, 1) * kUNL * kUNL * kUNT, 0.);
+  for (int k = 0; k < ncel; ++k) {
+    mcg::UpdCelDev &d = cel[k];
+    d.z = t->cel_key[2 * k];
+    d.ion = t->cel_key[2 * k + 1];
+    d.e = elem_index(d.z);
+    d.nlev = t->cel_nlev[k];
+    d.nt = t->cel_ntemp[k];
+    if (d.e < 0 || d.ion < 1 || d.ion > std::min(d.z + 1, 7) || d.nlev < 1 || d.nlev > 17 || d.nt < 1 || d.nt > kUNT)
+      return set_error(MC_ERR_ARG, "update tables: line ion %d (Z %d, ion %d, %d levels, %d temperatures) unusable", k,
+                       d.z, d.ion, d.nlev, d.nt);
+    d.br = t->cel_br[k];
+    d.zz = t->cel_z[k];
+    for (int i = 0; i < 4; ++i) d.ar[i] = t->cel_ar[4 * k + i];
+    for (int i = 0; i < 5; ++i) d.ad[i] = t->cel_ad[5 * k + i];
+    if (d.nt > 2) {
+      const double *lt = t->cel_logt + (size_t)k * kUNT;
+      for (int lo = 1; lo < d.nlev; ++lo)
+        for (int hi = lo + 1; hi <= d.nlev; ++hi) {
+          double y[kUNT];
+          for (int it = 0; it < d.nt; ++it) y[it] = t->cel_qom[(((size_t)k * kUNT + it) * kUNL + lo) * kUNL + hi];
+          mcg::spline_natural(lt, y, d.nt, &q2[(((size_t)k * kUNL + lo) * kUNL + hi) * kUNT]);
+        }
+    }
+  }
+  // collision strengths re-laid out [ion][lower][upper][T]
+  std::vector<double> qq((size_t)std::max(ncel, 1) * kUNL * kUNL * kUNT, 0.);
+  for (int k = 0; k < ncel; ++k)
+    for (int it = 0; it < kUNT; ++it)
+      for (int lo = 0; lo < kUNL; ++lo)
+        for (int hi = 0; hi < kUNL; ++hi)
+          qq[(((size_t)k * kUNL + lo) * kUNL + hi) * kUNT + it] = t->cel_qom[(((size_t)k * kUNT + it) * kUNL + lo) * kUNL + hi];
+  const size_t nk = (size_t)std::max(ncel, 1);
+  // float copies for the FP32 form
+  auto tof = [](const double *p, size_t n) {
+    std::vector<float> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = p ? (float)p[i] : 0.f;
+    return v;
+  };
+  std::vector<mcg::UpdIonT<float>> balf(bal.size());
+  for (size_t i = 0; i < bal.size(); ++i) {
+    const mcg::UpdIonDev &d = bal[i];
+    mcg::UpdIonT<float> &f = balf[i];
+    f.z = d.z; f.ion = d.ion; f.e = d.e; f.nelec = d.nelec;
+    for (int j = 0; j < 4; ++j) { f.dr[j] = d.dr[j]; f.dr8[j] = d.dr8[j]; f.chex[j] = (float)d.chex[j]; }
+    f.ndr = d.ndr; f.ar = d.ar; f.ndr8 = d.ndr8; f.ar8 = d.ar8;
+    f.dek = (float)d.dek; f.g0g1 = (float)d.g0g1;
+  }
+  std::vector<mcg::UpdCelT<float>> celf(nk);
+  for (int k = 0; k < ncel; ++k) {
+    const mcg::UpdCelDev &d = cel[k];
+    mcg::UpdCelT<float> &f = celf[k];
+    f.z = d.z; f.ion = d.ion; f.e = d.e; f.nlev = d.nlev; f.nt = d.nt;
+    f.br = (float)d.br; f.zz = (float)d.zz;
+    for (int j = 0; j < 4; ++j) f.ar[j] = (float)d.ar[j];
+    for (int j = 0; j < 5; ++j) f.ad[j] = (float)d.ad[j];
+  }
+  const std::vector<float> rrecf = tof(t->rrec, 2 * 31 * 31), rnewf = tof(t->rnew, 4 * 31 * 31),
+                           direcf = tof(t->direc, (size_t)t->ndirec * 8), aldrof = tof(t->aldro, (size_t)t->naldro * 6),
+                           logtf = tof(ncel ? t->cel_logt : nullptr, nk * kUNT),
+                           gf = tof(ncel ? t->cel_g : nullptr, nk * kUNL), ef = tof(ncel ? t->cel_e : nullptr, nk * kUNL),
+                           Af = tof(ncel ? t->cel_a : nullptr, nk * kUNL * kUNL), qqf = tof(qq.data(), qq.size()),
+                           q2f = tof(q2.data(), q2.size()), abf = tof(abund, 7);
+  mc_status st;
+  if ((st = put_buf(c->f_bal, balf.data(), balf.size() * sizeof(balf[0]), s)) ||
+      (st = put_buf(c->f_cel, celf.data(), nk * sizeof(celf[0]), s)) ||
+      (st = put_buf(c->f_rrec, rrecf.data(), rrecf.size() * 4, s)) ||
+      (st = put_buf(c->f_rnew, rnewf.data(), rnewf.size() * 4, s)) ||
+      (st = put_buf(c->f_direc, direcf.data(), std::max<size_t>(direcf.size(), 1) * 4, s)) ||
+      (st = put_buf(c->f_aldro, aldrof.data(), std::max<size_t>(aldrof.size(), 1) * 4, s)) ||
+      (st = put_buf(c->f_logt, logtf.data(), logtf.size() * 4, s)) || (st = put_buf(c->f_g, gf.data(), gf.size() * 4, s)) ||
+      (st = put_buf(c->f_e, ef.data(), ef.size() * 4, s)) || (st = put_buf(c->f_A, Af.data(), Af.size() * 4, s)) ||
+      (st = put_buf(c->f_qq, qqf.data(), qqf.size() * 4, s)) || (st = put_buf(c->f_q2, q2f.data(), q2f.size() * 4, s)) ||
+      (st = put_buf(c->f_ab, abf.data(), abf.size() * 4, s)))
+    return st;
+  if ((st = put_buf(c->u_bal, bal.data(), bal.size() * sizeof(mcg::UpdIonDev), s)) ||
+      (st = put_buf(c->u_cel, cel.data(), nk * sizeof(mcg::UpdCelDev), s)) ||
+      (st = put_buf(c->u_rrec, t->rrec, 2 * 31 * 31 * sizeof(double), s)) ||
+      (st = put_buf(c->u_rnew, t->rnew, 4 * 31 * 31 * sizeof(double), s)) ||
+      (st = put_buf(c->u_direc, t->direc, (size_t)std::max(t->ndirec, 1) * 8 * sizeof(double), s)) ||
+      (st = put_buf(c->u_aldro, t->aldro, (size_t)std::max(t->naldro, 1) * 6 * sizeof(double), s)) ||
+      (st = put_buf(c->u_logt, ncel ? t->cel_logt : nullptr, nk * kUNT * sizeof(double), s)) ||
+      (st = put_buf(c->u_g, ncel ? t->cel_g : nullptr, nk * kUNL * sizeof(double), s)) ||
+      (st = put_buf(c->u_e, ncel ? t->cel_e : nullptr, nk * kUNL * sizeof(double), s)) ||
+      (st = put_buf(c->u_A, ncel ? t->cel_a : nullptr, nk * kUNL * kUNL * sizeof(double), s)) ||
+      (st = put_buf(c->u_qq, qq.data(), qq.size() * sizeof(double), s)) ||
+      (st = put_buf(c->u_q2, q2.data(), q2.size() * sizeof(double), s)) ||
+      (st = put_buf(c->u_ab, abund, 7 * sizeof(double), s)) ||
+      (st = put_buf(c->u_hden, hden, (size_t)(c->nc + 1) * sizeof(double), s)))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  c->u_ncel = ncel;
+  c->u_maxlev = 1;
+  for (int k = 0; k < ncel; ++k) c->u_maxlev = std::max(c->u_maxlev, (int)t->cel_nlev[k]);
+  c->u_ndirec = t->ndirec;
+  c->u_naldro = t->naldro;
+  c->u_ready = true;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_set_cell_state(mc_ctx_t *c, const double *te, const double *ne, const double *X) {
+  if (!c || !te || !ne || !X) return set_error(MC_ERR_ARG, "ctx, te, ne and ionden are required");
+  const size_t nc1 = (size_t)c->nc + 1;
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = put_buf(c->s_te, te, nc1 * sizeof(double), s)) || (st = put_buf(c->s_ne, ne, nc1 * sizeof(double), s)) ||
+      (st = put_buf(c->s_X, X, nc1 * 56 * sizeof(double), s)) || (st = put_buf(c->s_conv, nullptr, nc1 * 4, s)) ||
+      (st = put_buf(c->s_niter, nullptr, nc1 * 4, s)) || (st = put_buf(c->s_flags, nullptr, nc1 * 4, s)) ||
+      (st = put_buf(c->s_dte, nullptr, nc1 * sizeof(double), s)))
+    return st;
+  MC_CUDA(cudaMemsetAsync(c->s_conv.p, 0, c->s_conv.bytes, s));
+  MC_CUDA(cudaMemsetAsync(c->s_niter.p, 0, c->s_niter.bytes, s));
+  MC_CUDA(cudaMemsetAsync(c->s_flags.p, 0, c->s_flags.bytes, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  c->s_ready = true;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_get_cell_state(mc_ctx_t *c, double *te, double *ne, double *X, int32_t *conv,
+                                          int32_t *niter, int32_t *flags) {
+  if (!c || !c->s_ready) return set_error(MC_ERR_ARG, "no cell state on the context");
+  cudaStream_t s = c->stream;
+  struct Item { void *h; DBuf *d; } items[6] = {{te, &c->s_te}, {ne, &c->s_ne}, {X, &c->s_X},
+                                                {conv, &c->s_conv}, {niter, &c->s_niter}, {flags, &c->s_flags}};
+  for (auto &it : items)
+    if (it.h) MC_CUDA(cudaMemcpyAsync(it.h, it.d->p, it.d->bytes, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double scale, double xhi_limit,
+                                        int32_t precision, mc_update_stats_t *stats) {
+  if (!c || !w) return set_error(MC_ERR_ARG, "ctx and w are required");
+  if (precision != MC_PREC_FP32 && precision != MC_PREC_FP64) return set_error(MC_ERR_ARG, "unknown precision");
+  if (!c->u_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_update_tables has not been called");
+  if (!c->s_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_cell_state has not been called");
+  const int nout = 67, nc1 = c->nc + 1, nb = c->nb;
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = put_buf(c->s_w, w, (size_t)nb * nout * sizeof(float), s)) ||
+      (st = put_buf(c->s_mom, nullptr, (size_t)nout * nc1 * sizeof(float), s)) ||
+      (st = put_buf(c->s_err, nullptr, sizeof(int), s)) ||
+      (st = put_buf(c->s_ustats, nullptr, sizeof(mcg::UpdStatsDev), s)))
+    return st;
+  MC_CUDA(cudaMemsetAsync(c->s_err.p, 0, sizeof(int), s));
+  MC_CUDA(cudaMemsetAsync(c->s_ustats.p, 0, sizeof(mcg::UpdStatsDev), s));
+  cudaEvent_t e0, e1, e2;
+  MC_CUDA(cudaEventCreate(&e0));
+  MC_CUDA(cudaEventCreate(&e1));
+  MC_CUDA(cudaEventCreate(&e2));
+  MC_CUDA(cudaEventRecord(e0, s));
+  cudaError_t e = mcg::launch_jmoments(nc1, nb, nout, c->jste.as<double>(), c->s_w.as<float>(), scale,
+                                       c->s_mom.as<float>(), c->s_err.as<int>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "moment launch failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(e1, s));
+  mcg::UpdArgs a{};
+  a.nc = c->nc;
+  a.ncel = c->u_ncel;
+  a.ndirec = c->u_ndirec;
+  a.naldro = c->u_naldro;
+  for (int i = 0; i < 7; ++i) { a.bal_z[i] = c->u_bal_z[i]; a.bal_first[i] = c->u_bal_first[i]; }
+  a.d.bal = c->u_bal.as<mcg::UpdIonDev>();
+  a.d.cel = c->u_cel.as<mcg::UpdCelDev>();
+  a.d.rrec = c->u_rrec.as<double>(); a.d.rnew = c->u_rnew.as<double>();
+  a.d.direc = c->u_direc.as<double>(); a.d.aldro = c->u_aldro.as<double>();
+  a.d.logt = c->u_logt.as<double>(); a.d.g = c->u_g.as<double>(); a.d.e = c->u_e.as<double>();
+  a.d.A = c->u_A.as<double>(); a.d.qq = c->u_qq.as<double>(); a.d.q2 = c->u_q2.as<double>();
+  a.d.ab = c->u_ab.as<double>();
+  a.f.bal = c->f_bal.as<mcg::UpdIonT<float>>();
+  a.f.cel = c->f_cel.as<mcg::UpdCelT<float>>();
+  a.f.rrec = c->f_rrec.as<float>(); a.f.rnew = c->f_rnew.as<float>();
+  a.f.direc = c->f_direc.as<float>(); a.f.aldro = c->f_aldro.as<float>();
+  a.f.logt = c->f_logt.as<float>(); a.f.g = c->f_g.as<float>(); a.f.e = c->f_e.as<float>();
+  a.f.A = c->f_A.as<float>(); a.f.qq = c->f_qq.as<float>(); a.f.q2 = c->f_q2.as<float>();
+  a.f.ab = c->f_ab.as<float>();
+  a.hden = c->u_hden.as<double>();
+  a.mom = c->s_mom.as<float>();
+  a.mstride = nc1;
+  a.te = c->s_te.as<double>(); a.ne = c->s_ne.as<double>(); a.X = c->s_X.as<double>();
+  a.conv = c->s_conv.as<int>(); a.niter = c->s_niter.as<int>(); a.flags = c->s_flags.as<int>();
+  a.dte = c->s_dte.as<double>();
+  a.xhi = xhi_limit;
+  a.mat_rows = c->u_maxlev;
+  a.mat_stride = (c->u_maxlev * c->u_maxlev) | 1;
+  e = mcg::launch_cell_update(a, precision == MC_PREC_FP32, c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "cell update launch failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(e2, s));
+  e = mcg::launch_update_stats(c->nc, a.conv, a.niter, a.flags, a.dte, c->s_ustats.as<mcg::UpdStatsDev>(),
+                               c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "update stats launch failed: %s", cudaGetErrorString(e));
+  mcg::UpdStatsDev hs{};
+  int herr = 0;
+  MC_CUDA(cudaMemcpyAsync(&hs, c->s_ustats.p, sizeof hs, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaMemcpyAsync(&herr, c->s_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float m1 = 0.f, m2 = 0.f;
+  cudaEventElapsedTime(&m1, e0, e1);
+  cudaEventElapsedTime(&m2, e1, e2);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  if (herr) return set_error((mc_status)herr, "moment kernel: tensor-core wait timed out");
+  if (stats) {
+    stats->hit = (int64_t)hs.hit;
+    stats->converged = (int64_t)hs.converged;
+    stats->no_te_balance = (int64_t)hs.no_te;
+    stats->no_ion_balance = (int64_t)hs.no_ion;
+    stats->t_iterations = (int64_t)hs.iters;
+    double dmax;
+    std::memcpy(&dmax, &hs.dmax_bits, sizeof dmax);
+    stats->dte_max = dmax;
+    stats->frac_dte_1pc = hs.hit ? (double)hs.small / (double)hs.hit : 0.;
+    stats->moments_ms = m1;
+    stats->update_ms = m2;
+  }
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_get_opacity(mc_ctx_t *c, float *out) {
+  if (!c || !out) return set_error(MC_ERR_ARG, "ctx and opacity are required");
+  MC_CUDA(cudaMemcpyAsync(out, c->opacity.p, (size_t)(c->nc + 1) * c->nb * sizeof(float), cudaMemcpyDeviceToHost,
+                          c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, const int32_t *species,
+                                              const float *xs, int32_t method, double *kernel_ms) {
+  if (!c || !species || !xs) return set_error(MC_ERR_ARG, "ctx, species and xs are required");
+  if (!c->u_ready || !c->s_ready) return set_error(MC_ERR_ARG, "cell state or tables missing");
+  if (nspecies < 1 || nspecies > 64) return set_error(MC_ERR_ARG, "nspecies must be 1..64 (got %d)", nspecies);
+  if (method != MC_OPAC_FP32 && method != MC_OPAC_BF16X3) return set_error(MC_ERR_ARG, "unknown opacity method");
+  std::vector<int32_t> se(nspecies), ss(nspecies);
+  for (int k = 0; k < nspecies; ++k) {
+    se[k] = elem_index(species[2 * k]);
+    ss[k] = species[2 * k + 1];
+    if (se[k] < 0 || ss[k] < 1 || ss[k] > 7) return set_error(MC_ERR_ARG, "species %d: bad (Z, stage)", k);
+  }
+  const int nc1 = c->nc + 1, nb = c->nb;
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = put_buf(c->s_spe, se.data(), nspecies * sizeof(int32_t), s)) ||
+      (st = put_buf(c->s_sps, ss.data(), nspecies * sizeof(int32_t), s)) ||
+      (st = put_buf(c->s_xs, xs, (size_t)nspecies * nb * sizeof(float), s)) ||
+      (st = put_buf(c->s_den, nullptr, (size_t)nspecies * nc1 * sizeof(float), s)) ||
+      (st = put_buf(c->s_err, nullptr, sizeof(int), s)))
+    return st;
+  MC_CUDA(cudaMemsetAsync(c->s_err.p, 0, sizeof(int), s));
+  cudaEvent_t e0, e1;
+  MC_CUDA(cudaEventCreate(&e0));
+  MC_CUDA(cudaEventCreate(&e1));
+  MC_CUDA(cudaEventRecord(e0, s));
+  cudaError_t e = mcg::launch_species(c->nc, nspecies, c->s_spe.as<int>(), c->s_sps.as<int>(), c->s_X.as<double>(),
+                                      c->u_ab.as<double>(), c->u_hden.as<double>(), c->s_den.as<float>(), c->num_sms, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_opacity(method, nc1, nspecies, nb, c->s_den.as<float>(), c->s_xs.as<float>(), nullptr,
+                            c->opacity.as<float>(), c->s_err.as<int>(), c->num_sms, s);
+  if (e == cudaSuccess && !c->identity)
+    e = mcg::launch_wave_expand(c->opacity.as<float>(), c->opac_m.as<float>(), c->lin2cell.as<int32_t>(), c->ncell3,
+                                nc1, nb, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "opacity rebuild failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(e1, s));
+  int herr = 0;
+  MC_CUDA(cudaMemcpyAsync(&herr, c->s_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  if (kernel_ms) *kernel_ms = ms;
+  if (herr) return set_error((mc_status)herr, "opacity kernel: tensor-core wait timed out");
   return MC_OK;
 }
 

@@ -59,6 +59,20 @@ def library():
         lib.mc_transport_release.restype = C.c_int
         lib.mc_ctx_jste_moments.restype = C.c_int
         lib.mc_ctx_jste_moments.argtypes = [C.c_void_p, C.c_int32, fp, C.c_double, fp, dp]
+        ip = C.POINTER(C.c_int32)
+        lib.mc_ctx_set_update_tables.restype = C.c_int
+        lib.mc_ctx_set_update_tables.argtypes = [C.c_void_p, C.POINTER(abi.McUpdateTables), dp, dp]
+        lib.mc_ctx_set_cell_state.restype = C.c_int
+        lib.mc_ctx_set_cell_state.argtypes = [C.c_void_p, dp, dp, dp]
+        lib.mc_ctx_get_cell_state.restype = C.c_int
+        lib.mc_ctx_get_cell_state.argtypes = [C.c_void_p, dp, dp, dp, ip, ip, ip]
+        lib.mc_ctx_update_cells.restype = C.c_int
+        lib.mc_ctx_update_cells.argtypes = [C.c_void_p, fp, C.c_double, C.c_double, C.c_int32,
+                                            C.POINTER(abi.McUpdateStats)]
+        lib.mc_ctx_opacity_from_state.restype = C.c_int
+        lib.mc_ctx_opacity_from_state.argtypes = [C.c_void_p, C.c_int32, ip, fp, C.c_int32, dp]
+        lib.mc_ctx_get_opacity.restype = C.c_int
+        lib.mc_ctx_get_opacity.argtypes = [C.c_void_p, fp]
         lib.mc_ctx_destroy.restype = None
         lib.mc_ctx_destroy.argtypes = [C.c_void_p]
         lib.mc_opacity_build.restype = C.c_int
@@ -210,6 +224,53 @@ class TransportContext:
         ms = C.c_double()
         _check(self.lib.mc_ctx_jste_moments(self.handle, nout, _fptr(w), float(scale), _fptr(out), C.byref(ms)))
         return out, ms.value
+
+    # ---- the cell update (ionisation and thermal balance) ----
+    def set_update_tables(self, tables, hden, abund):
+        self._ut = abi.update_tables_struct(tables)
+        h = np.ascontiguousarray(hden, dtype=np.float64)
+        a = np.ascontiguousarray(abund, dtype=np.float64)
+        _check(self.lib.mc_ctx_set_update_tables(self.handle, C.byref(self._ut), _dptr(h), _dptr(a)))
+
+    def set_cell_state(self, te, ne, X):
+        te = np.ascontiguousarray(te, dtype=np.float64)
+        ne = np.ascontiguousarray(ne, dtype=np.float64)
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        if te.shape != (self.neb.ncells + 1,) or X.shape != (self.neb.ncells + 1, 7, 8):
+            raise ValueError("te (Nc+1,), ne (Nc+1,), X (Nc+1, 7, 8)")
+        _check(self.lib.mc_ctx_set_cell_state(self.handle, _dptr(te), _dptr(ne), _dptr(X)))
+
+    def get_cell_state(self):
+        nc1 = self.neb.ncells + 1
+        te, ne, X = np.empty(nc1), np.empty(nc1), np.empty((nc1, 7, 8))
+        conv, niter, flags = (np.empty(nc1, dtype=np.int32) for _ in range(3))
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        _check(self.lib.mc_ctx_get_cell_state(self.handle, _dptr(te), _dptr(ne), _dptr(X), ip(conv), ip(niter),
+                                              ip(flags)))
+        return te, ne, X, conv, niter, flags
+
+    def update_cells(self, w, scale, xhi_limit=0.05, precision="fp64"):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.shape != (self.neb.nbins, 67):
+            raise ValueError("w must be (nbins, 67)")
+        prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
+        st = abi.McUpdateStats()
+        _check(self.lib.mc_ctx_update_cells(self.handle, _fptr(w), float(scale), float(xhi_limit), prec,
+                                            C.byref(st)))
+        return st.as_dict()
+
+    def get_opacity(self):
+        out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
+        _check(self.lib.mc_ctx_get_opacity(self.handle, _fptr(out)))
+        return out
+
+    def opacity_from_state(self, species, xs, method="bf16x3"):
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        x = np.ascontiguousarray(xs, dtype=np.float32)
+        ms = C.c_double()
+        _check(self.lib.mc_ctx_opacity_from_state(self.handle, len(sp), sp.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  _fptr(x), OPACITY_METHODS[method], C.byref(ms)))
+        return ms.value
 
     def device_estimators(self):
         j, d, e = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()

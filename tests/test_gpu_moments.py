@@ -37,7 +37,7 @@ def test_photoionisation_sums_match_the_oracle(gpu_lib, spec):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nout", [1, 16, 33, 64])
+@pytest.mark.parametrize("nout", [1, 16, 33, 64, 67, 128])
 def test_moments_of_random_weights(gpu_lib, nout):
     neb = nebula.build(nebula.small_cases()[0])
     ctx = transport.TransportContext(neb)
