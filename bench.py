@@ -171,6 +171,30 @@ def run_reference(args):
     return 0
 
 
+def converged_model(neb, args):
+    """Wall time to a converged model: Lambda iterations (transport, cell
+    update, opacity rebuild) until 95 % of the cells have |dX(H0)/X(H0)| <=
+    5 % (the reference's minConvergence / XHILimit), for the chosen form
+    (persistent wave march, FP32 cell update) and the plain form (one thread
+    per history, FP64 cell update), from the same initial state."""
+    from mocassin_gb300 import iterate
+    out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
+           "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
+    for name, form, upd in (("chosen", "wave", "fp32"), ("plain", "plain", "fp64")):
+        li = iterate.LambdaIteration(neb, form=form, update=upd)
+        wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
+        li.close()
+        last = hist[-1]
+        out[name] = {"transport": form, "update": upd, "wall_s": wall, "iterations": len(hist),
+                     "converged": last["converged_pct"] >= 95.0, "converged_pct": last["converged_pct"],
+                     "dte_lt_1pc_pct": last["dte_lt_1pc_pct"],
+                     "transport_s": sum(h["transport_s"] for h in hist), "update_s": sum(h["update_s"] for h in hist),
+                     "opacity_s": sum(h["opacity_s"] for h in hist),
+                     "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist]))}
+    out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,6 +211,7 @@ def main():
     ap.add_argument("--form", default="wave", choices=["wave", "plain"])
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-opacity", action="store_true")
+    ap.add_argument("--lambda-max", type=int, default=12, help="Lambda iterations at most per form (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -369,6 +394,8 @@ def main():
         line["opacity_build"] = opac
     if moments:
         line["jste_moments"] = moments
+    if args.lambda_max > 0 and rank == 0:
+        line["converged_model"] = converged_model(neb, args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(neb)
     if rank == 0:

@@ -1,0 +1,86 @@
+"""The Lambda iteration on one GPU: transport, cell update, opacity rebuild,
+until the model converges (iterateMC, source/iteration_mod.f90:33-1140).
+
+Each iteration runs, on the grid resident in HBM,
+  1. the energy-packet transport of every star (energyPacketDriver, :474-496),
+  2. the cell update of every active cell from the normalised Jste
+     (updateCell over the grid, :800-840; Jste x 1e-9, / 8 in a symmetric
+     octant, :705-724),
+  3. the convergence test: the percentage of cells with
+     |dX(H0)/X(H0)| <= XHILimit (0.05, set_input_mod.f90:117) against
+     minConvergence (95 %, set_input_mod.f90:105; test :1135), at most
+     maxIterateMC (30) iterations,
+  4. the opacity of the next transport from the new ion densities
+     (ionizationDriver, ionization_mod.f90:26-129, on the tensor cores).
+The re-emission CDFs (recPDF) stay those of the input grid: the emission
+step (emission_mod.f90:905-1311) is not part of this path.
+
+``form`` picks the transport ("wave": the frequency-sorted persistent march;
+"plain": one thread per history) and ``update`` the arithmetic of the cell
+update ("fp64": the FP64 method; "fp32": the reference's own 4-byte
+precision).  ``warm_start`` is an optional callable that sets the cell state
+(Te, ionic fractions) before each update from the Jste sums.
+"""
+import time
+
+import numpy as np
+
+from . import balance, nebula, transport
+
+
+def _ions():
+    return np.array([tuple(int(v) for v in r) for r in nebula.atomic_table()["ions"]], dtype=np.int32)
+
+
+class LambdaIteration:
+    """A nebula resident on the GPU with its cell state."""
+
+    def __init__(self, neb, form="wave", update="fp32", xhi_limit=0.05, opacity_method="bf16x3"):
+        self.neb = neb
+        self.form = form
+        self.update = update
+        self.xhi = xhi_limit
+        self.opacity_method = opacity_method
+        self.ctx = transport.TransportContext(neb)
+        self.ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+        te, ne, X = balance.initial_state(neb)
+        self.ctx.set_cell_state(te, ne, X)
+        self.species = _ions()
+        self.w = balance.moment_weights(neb.xs, neb.nu, self.species)
+        self.scale = 1e-9 / (8.0 if neb.flags & nebula.FLAG_SYMMETRIC_XYZ else 1.0)
+        self.history = []
+
+    def step(self, seed, n_packets=None, warm_start=None):
+        t0 = time.perf_counter()
+        tr = self.ctx.run(n_packets=n_packets, seed=seed, iteration=len(self.history) + 1, precision="fp32",
+                          zero_first=True, form=self.form)
+        t1 = time.perf_counter()
+        if warm_start is not None:
+            warm_start(self)
+        up = self.ctx.update_cells(self.w, self.scale, xhi_limit=self.xhi, precision=self.update)
+        t2 = time.perf_counter()
+        op_ms = self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
+        t3 = time.perf_counter()
+        rec = {"iteration": len(self.history) + 1, "transport_s": t1 - t0, "update_s": t2 - t1, "opacity_s": t3 - t2,
+               "wall_s": t3 - t0, "crossings": tr["crossings"], "transport_kernel_ms": tr["kernel_ms"],
+               "update_ms": up["update_ms"], "moments_ms": up["moments_ms"], "opacity_ms": op_ms,
+               "hit": up["hit"], "converged_pct": 100.0 * up["converged"] / max(up["hit"], 1),
+               "dte_lt_1pc_pct": 100.0 * up["frac_dte_1pc"], "t_steps_per_cell": up["t_iterations"] / max(up["hit"], 1),
+               "no_te_balance": up["no_te_balance"], "no_ion_balance": up["no_ion_balance"]}
+        self.history.append(rec)
+        return rec
+
+    def run(self, seed=1, max_iterations=30, min_convergence=95.0, n_packets=None, warm_start=None):
+        """Iterates until converged_pct >= min_convergence; returns the wall time and the history."""
+        t0 = time.perf_counter()
+        for it in range(max_iterations):
+            rec = self.step(seed + it, n_packets=n_packets, warm_start=warm_start)
+            if rec["converged_pct"] >= min_convergence:
+                break
+        return time.perf_counter() - t0, self.history
+
+    def state(self):
+        return self.ctx.get_cell_state()
+
+    def close(self):
+        self.ctx.close()
