@@ -318,6 +318,32 @@ mc_status mc_ctx_update_cells(mc_ctx_t *ctx, const float *w, double scale, doubl
 mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32_t *species, const float *xs,
                                     int32_t method, double *kernel_ms);
 
+/* ---- the learned warm start of the cell update ----------------------------
+ * A small MLP (80 -> 128 -> 128 -> 48, ReLU; BF16 operands, FP32
+ * accumulation and Adam, all on the GPU) from the Jste sums of a cell (log10
+ * of sum Jste, of the 33 photoionisation and 33 heating sums, of Hden) to
+ * log10 Te and log10 of the 40 ionic fractions.  Trained on cell states the
+ * update produced (collect after mc_ctx_update_cells), it warm-starts the
+ * update: mc_ctx_update_cells_warm writes the prediction into the state and
+ * runs the same solve from there; the solve accepts the prediction when the
+ * thermal residual is below 1 % of the heating at its first step, and
+ * otherwise brackets the balance with steps of 3 %, 6 %, 12 %, then the
+ * reference's 20 %, before its secant; every result meets the reference's
+ * 1 % residual test.  No counterpart in the reference (updateCell starts
+ * from the previous iteration's state with 20 % steps). */
+mc_status mc_ctx_surrogate_init(mc_ctx_t *ctx, uint64_t seed, int64_t capacity);
+mc_status mc_ctx_surrogate_collect(mc_ctx_t *ctx, int64_t *rows);
+mc_status mc_ctx_surrogate_train(mc_ctx_t *ctx, int32_t steps, int32_t batch, float lr, uint64_t seed, double *loss,
+                                 double *train_ms);
+mc_status mc_ctx_update_cells_warm(mc_ctx_t *ctx, const float *w, double scale, double xhi_limit, int32_t precision,
+                                   mc_update_stats_t *stats);
+/* Parameters (33072 floats: W1[128][80] b1 W2[128][128] b2 W3[48][128] b3). */
+mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
+/* Loss and gradients of one batch (x [m][80], normalised targets t [m][48];
+ * the first 41 columns count), and the outputs y [m][48]. */
+mc_status mc_ctx_surrogate_grads(mc_ctx_t *ctx, int32_t m, const float *x, const float *t, double *loss, float *grads,
+                                 float *y);
+
 /* Copies the resident opacity [nbins][Nc+1] (cell fastest) to the host. */
 mc_status mc_ctx_get_opacity(mc_ctx_t *ctx, float *opacity);
 

@@ -30,6 +30,7 @@ UNITS = [
     ("jmoments.cu", []),
     ("cellupdate.cu", ["-fmad=false", "-Xcompiler=-ffp-contract=off"]),
     ("cellupdate_fp32.cu", []),
+    ("mlp.cu", []),
 ]
 
 

@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
     for (int i = lane; i < kNE * kNX; i += 32) sX[w][i / kNX][i % kNX] = (Real)Xc[i];
     const Real hden = (Real)a.hden[c];
     Real Te = (Real)a.te[c], Ne = (Real)a.ne[c];
-    const Real Te0 = Te;
+    const Real Te0 = a.te_prev ? (Real)a.te_prev[c] : Te;
     Real P[2] = {(Real)0., (Real)0.}, Hh[2] = {(Real)0., (Real)0.};
     for (int r = 0; r < 2; ++r) {
       const int b = lane + 32 * r;
@@ -318,10 +318,11 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       }
     }
     __syncwarp();
-    const Real XOldHI = sX[w][0][1];
+    const Real XOldHI = a.xh0_prev ? (Real)a.xh0_prev[c] : sX[w][0][1];
     int nIterT = 0, noTe = 0;
     bool ionConv = true;
     Real thResHigh = 0., thResLow = 0., Thigh = 0., Tlow = 0.;
+    Real fstep = (Real)a.step0;
     for (;;) {
       ++nIterT;
       for (int r = 0; r < 2; ++r) {
@@ -457,17 +458,19 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       bool again = false;
       if (fabs(thResidual) >= (Real)0.01 * heatInt) {
         if (nIterT < 25) {
+          bool open = false;
           if (thResidual < (Real)0) {
             thResLow = thResidual;
             Tlow = Te;
             if (Thigh != (Real)0.) Te = Tlow - (Thigh - Tlow) * thResLow / (thResHigh - thResLow);
-            else Te = Te / (Real)1.2;
+            else { Te = Te / fstep; open = true; }
           } else {
             thResHigh = thResidual;
             Thigh = Te;
             if (Tlow != (Real)0.) Te = Tlow - (Thigh - Tlow) * thResLow / (thResHigh - thResLow);
-            else Te = Te * (Real)1.2;
+            else { Te = Te * fstep; open = true; }
           }
+          if (open && a.step_grow) fstep = fstep - (Real)1. < (Real)0.1 ? (Real)1. + (Real)2. * (fstep - (Real)1.) : (Real)1.2;
           if (nIterT >= 6 && fabs(Thigh - Tlow) <= (Real)0.002 * (Thigh + Tlow)) {
             if (thResidual < (Real)0) { Te = Thigh - (Real)100.; Thigh = (Real)0.; }
             else { Te = Tlow + (Real)100.; Tlow = (Real)0.; }

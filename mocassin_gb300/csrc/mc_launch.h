@@ -84,6 +84,9 @@ struct UpdArgs {
   double *dte;
   double xhi;
   int mat_rows, mat_stride;  // FP32 form: matrix row length (max levels) and odd per-lane stride
+  const double *te_prev, *xh0_prev;  // warm start: the state before the prediction (null: cold)
+  double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
+  int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
 };
 cudaError_t launch_cell_update(const UpdArgs &a, int fp32, int num_sms, cudaStream_t stream);
 cudaError_t launch_cell_update_fp32(const UpdArgs &a, int blocks, cudaStream_t stream);
@@ -92,6 +95,33 @@ cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const
 cudaError_t launch_species(int nc, int nsp, const int *sp_e, const int *sp_s, const double *X, const double *ab,
                            const double *hden, float *den, int num_sms, cudaStream_t stream);
 void spline_natural(const double *x, const double *y, int n, double *y2);
+
+// ---- the learned warm start (mlp.cu) ----
+constexpr int kMlpIn = 80, kMlpHid = 128, kMlpOut = 48, kMlpTargets = 41;
+constexpr int kMlpW1 = 0, kMlpB1 = kMlpW1 + kMlpHid * kMlpIn, kMlpW2 = kMlpB1 + kMlpHid,
+              kMlpB2 = kMlpW2 + kMlpHid * kMlpHid, kMlpW3 = kMlpB2 + kMlpHid, kMlpB3 = kMlpW3 + kMlpOut * kMlpHid,
+              kMlpParams = kMlpB3 + kMlpOut;
+size_t mlp_dense_smem(int nin, int nout);
+cudaError_t launch_mlp_dense(int M, int nin, int nout, const float *in, int ldin, const float *mask, const float *W,
+                             bool transposed, const float *bias, int act, bool round_in, float *out, int ldout,
+                             cudaStream_t s);
+cudaError_t launch_mlp_wgrad(int M, int nin, int nout, const float *dz, const float *mask, const float *in, float *dW,
+                             float *db, int num_sms, cudaStream_t s);
+cudaError_t launch_mlp_loss(int M, int nt, int ld, const float *y, const float *tn, float *dy, double *loss,
+                            cudaStream_t s);
+cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, float lr, float b1t, float b2t,
+                            cudaStream_t s);
+cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, int step, const float *xs, const float *ts,
+                              const float *fmean, const float *fstd, const float *tmean, const float *tstd, float *xb,
+                              float *tb, cudaStream_t s);
+cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s);
+cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
+                               const double *X, long long cap, unsigned long long *count, float *xs, float *ts,
+                               int num_sms, cudaStream_t s);
+cudaError_t launch_mlp_infer_features(int nc, const float *mom, long long ms, const double *hden, const float *fmean,
+                                      const float *fstd, float *x, int num_sms, cudaStream_t s);
+cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const float *tmean, const float *tstd, double *te,
+                             double *X, double *te_prev, double *xh0_prev, int num_sms, cudaStream_t s);
 
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);

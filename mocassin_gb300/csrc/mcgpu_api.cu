@@ -121,6 +121,12 @@ struct mc_ctx {
   DBuf s_te, s_ne, s_X, s_conv, s_niter, s_flags, s_dte, s_mom, s_w, s_ustats, s_err, s_den, s_xs, s_spe, s_sps;
   int u_ncel = 0, u_ndirec = 0, u_naldro = 0, u_maxlev = 1;
   int u_bal_z[7] = {}, u_bal_first[7] = {};
+  // learned warm start: parameters, Adam state, training buffer, work arrays
+  DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss;
+  DBuf m_xb, m_tb, m_a1, m_a2, m_y, m_dy, m_d2, m_d1, m_xi, m_h1, m_h2, m_yi, m_te_prev, m_xh0_prev;
+  long long m_cap = 0, m_n = 0;
+  int m_step = 0, m_B = 0;
+  bool m_ready = false, m_norm = false;
   bool u_ready = false, s_ready = false;
   DBuf counters, src_cdf, replay;
   // chosen form: march-indexed views and the sorted packet queue
@@ -1091,9 +1097,14 @@ extern "C" mc_status mc_ctx_get_cell_state(mc_ctx_t *c, double *te, double *ne, 
   return MC_OK;
 }
 
-extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double scale, double xhi_limit,
-                                        int32_t precision, mc_update_stats_t *stats) {
+namespace {
+mc_status surrogate_predict_state(mc_ctx_t *c);
+}
+
+static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, double xhi_limit, int32_t precision,
+                                   bool warm, mc_update_stats_t *stats) {
   if (!c || !w) return set_error(MC_ERR_ARG, "ctx and w are required");
+  if (warm && !(c->m_ready && c->m_norm)) return set_error(MC_ERR_ARG, "the surrogate is not trained");
   if (precision != MC_PREC_FP32 && precision != MC_PREC_FP64) return set_error(MC_ERR_ARG, "unknown precision");
   if (!c->u_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_update_tables has not been called");
   if (!c->s_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_cell_state has not been called");
@@ -1116,8 +1127,17 @@ extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double sca
                                        c->s_mom.as<float>(), c->s_err.as<int>(), c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "moment launch failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(e1, s));
+  if (warm) {
+    mc_status ws = surrogate_predict_state(c);
+    if (ws) return ws;
+  }
   mcg::UpdArgs a{};
   a.nc = c->nc;
+  a.te_prev = warm ? c->m_te_prev.as<double>() : nullptr;
+  a.xh0_prev = warm ? c->m_xh0_prev.as<double>() : nullptr;
+  // a predicted Te is near the balance: bracket it with small steps first
+  a.step0 = warm ? 1.03 : 1.2;
+  a.step_grow = warm ? 1 : 0;
   a.ncel = c->u_ncel;
   a.ndirec = c->u_ndirec;
   a.naldro = c->u_naldro;
@@ -1174,6 +1194,263 @@ extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double sca
     stats->moments_ms = m1;
     stats->update_ms = m2;
   }
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double scale, double xhi_limit,
+                                        int32_t precision, mc_update_stats_t *stats) {
+  return update_cells_impl(c, w, scale, xhi_limit, precision, false, stats);
+}
+
+extern "C" mc_status mc_ctx_update_cells_warm(mc_ctx_t *c, const float *w, double scale, double xhi_limit,
+                                             int32_t precision, mc_update_stats_t *stats) {
+  return update_cells_impl(c, w, scale, xhi_limit, precision, true, stats);
+}
+
+// ------------------------------------------------------------ surrogate
+namespace {
+
+using mcg::kMlpIn;
+using mcg::kMlpHid;
+using mcg::kMlpOut;
+using mcg::kMlpParams;
+
+mc_status ensure(DBuf &b, size_t bytes) {
+  if (b.p && b.bytes >= bytes) return MC_OK;
+  if (b.p) { cudaFree(b.p); b.p = nullptr; b.bytes = 0; }
+  MC_CUDA(b.alloc(bytes));
+  return MC_OK;
+}
+
+// forward pass of M rows: x [M][80] -> a1, a2 [M][128] -> y [M][48]
+mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, float *y) {
+  const float *W = c->m_w.as<float>();
+  cudaStream_t s = c->stream;
+  cudaError_t e = mcg::launch_mlp_dense(M, kMlpIn, kMlpHid, x, kMlpIn, nullptr, W + mcg::kMlpW1, false,
+                                        W + mcg::kMlpB1, 1, true, a1, kMlpHid, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpHid, a1, kMlpHid, nullptr, W + mcg::kMlpW2, false, W + mcg::kMlpB2, 1,
+                              true, a2, kMlpHid, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpOut, a2, kMlpHid, nullptr, W + mcg::kMlpW3, false, W + mcg::kMlpB3, 0,
+                              true, y, kMlpOut, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp forward failed: %s", cudaGetErrorString(e));
+  return MC_OK;
+}
+
+// loss and gradients of M rows (x, normalised targets t) into m_g
+mc_status mlp_backward(mc_ctx_t *c, int M, const float *x, const float *t) {
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = ensure(c->m_a1, (size_t)M * kMlpHid * 4)) || (st = ensure(c->m_a2, (size_t)M * kMlpHid * 4)) ||
+      (st = ensure(c->m_y, (size_t)M * kMlpOut * 4)) || (st = ensure(c->m_dy, (size_t)M * kMlpOut * 4)) ||
+      (st = ensure(c->m_d2, (size_t)M * kMlpHid * 4)) || (st = ensure(c->m_d1, (size_t)M * kMlpHid * 4)))
+    return st;
+  float *a1 = c->m_a1.as<float>(), *a2 = c->m_a2.as<float>(), *y = c->m_y.as<float>(), *dy = c->m_dy.as<float>();
+  float *d2 = c->m_d2.as<float>(), *d1 = c->m_d1.as<float>();
+  if ((st = mlp_forward(c, M, x, a1, a2, y))) return st;
+  const float *W = c->m_w.as<float>();
+  float *G = c->m_g.as<float>();
+  MC_CUDA(cudaMemsetAsync(G, 0, kMlpParams * sizeof(float), s));
+  cudaError_t e = mcg::launch_mlp_loss(M, mcg::kMlpTargets, kMlpOut, y, t, dy, c->m_loss.as<double>(), s);
+  // layer 3 (linear): dW3 = dY^T a2, dA2 = dY W3
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpOut, dy, nullptr, a2, G + mcg::kMlpW3, G + mcg::kMlpB3, c->num_sms, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_dense(M, kMlpOut, kMlpHid, dy, kMlpOut, nullptr, W + mcg::kMlpW3, true, nullptr, 0, false, d2,
+                              kMlpHid, s);
+  // layer 2 (ReLU): dZ2 = dA2 (a2 > 0)
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d2, a2, a1, G + mcg::kMlpW2, G + mcg::kMlpB2, c->num_sms, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpHid, d2, kMlpHid, a2, W + mcg::kMlpW2, true, nullptr, 0, false, d1,
+                              kMlpHid, s);
+  // layer 1 (ReLU): dZ1 = dA1 (a1 > 0)
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_wgrad(M, kMlpIn, kMlpHid, d1, a1, x, G + mcg::kMlpW1, G + mcg::kMlpB1, c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp backward failed: %s", cudaGetErrorString(e));
+  return MC_OK;
+}
+
+mc_status surrogate_predict_state(mc_ctx_t *c) {
+  const int nc1 = c->nc + 1;
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = ensure(c->m_xi, (size_t)nc1 * kMlpIn * 4)) || (st = ensure(c->m_h1, (size_t)nc1 * kMlpHid * 4)) ||
+      (st = ensure(c->m_h2, (size_t)nc1 * kMlpHid * 4)) || (st = ensure(c->m_yi, (size_t)nc1 * kMlpOut * 4)) ||
+      (st = ensure(c->m_te_prev, (size_t)nc1 * 8)) || (st = ensure(c->m_xh0_prev, (size_t)nc1 * 8)))
+    return st;
+  cudaError_t e = mcg::launch_mlp_infer_features(c->nc, c->s_mom.as<float>(), nc1, c->u_hden.as<double>(),
+                                                 c->m_fmean.as<float>(), c->m_fstd.as<float>(), c->m_xi.as<float>(),
+                                                 c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "features failed: %s", cudaGetErrorString(e));
+  if ((st = mlp_forward(c, nc1, c->m_xi.as<float>(), c->m_h1.as<float>(), c->m_h2.as<float>(), c->m_yi.as<float>())))
+    return st;
+  e = mcg::launch_mlp_apply(c->nc, c->s_mom.as<float>(), c->m_yi.as<float>(), c->m_tmean.as<float>(),
+                            c->m_tstd.as<float>(), c->s_te.as<double>(), c->s_X.as<double>(), c->m_te_prev.as<double>(),
+                            c->m_xh0_prev.as<double>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "apply failed: %s", cudaGetErrorString(e));
+  return MC_OK;
+}
+
+mc_status surrogate_normalise(mc_ctx_t *c) {
+  const long long n = std::min(c->m_n, c->m_cap);
+  if (n < 2) return set_error(MC_ERR_ARG, "the surrogate has fewer than 2 training rows");
+  cudaStream_t s = c->stream;
+  DBuf sums;
+  MC_CUDA(sums.alloc((size_t)4 * 128 * sizeof(double)));
+  MC_CUDA(cudaMemsetAsync(sums.p, 0, sums.bytes, s));
+  double *d = sums.as<double>();
+  cudaError_t e = mcg::launch_mlp_stats(n, kMlpIn, c->m_xs.as<float>(), d, d + 128, s);
+  if (e == cudaSuccess) e = mcg::launch_mlp_stats(n, kMlpOut, c->m_ts.as<float>(), d + 256, d + 384, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "stats failed: %s", cudaGetErrorString(e));
+  std::vector<double> h(4 * 128);
+  MC_CUDA(cudaMemcpyAsync(h.data(), d, sums.bytes, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  std::vector<float> fm(kMlpIn), fs(kMlpIn), tm(kMlpOut), ts(kMlpOut);
+  auto ms = [&](double sum, double sq, float &mean, float &sd) {
+    const double m = sum / (double)n, v = std::max(sq / (double)n - m * m, 0.);
+    mean = (float)m;
+    sd = (float)std::max(std::sqrt(v), 1e-3);
+  };
+  for (int i = 0; i < kMlpIn; ++i) ms(h[i], h[128 + i], fm[i], fs[i]);
+  for (int o = 0; o < kMlpOut; ++o) ms(h[256 + o], h[384 + o], tm[o], ts[o]);
+  mc_status st;
+  if ((st = put_buf(c->m_fmean, fm.data(), kMlpIn * 4, s)) || (st = put_buf(c->m_fstd, fs.data(), kMlpIn * 4, s)) ||
+      (st = put_buf(c->m_tmean, tm.data(), kMlpOut * 4, s)) || (st = put_buf(c->m_tstd, ts.data(), kMlpOut * 4, s)))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(s));
+  c->m_norm = true;
+  return MC_OK;
+}
+
+}  // namespace
+
+extern "C" mc_status mc_ctx_surrogate_init(mc_ctx_t *c, uint64_t seed, int64_t capacity) {
+  if (!c || capacity < 1) return set_error(MC_ERR_ARG, "ctx and a positive capacity are required");
+  cudaStream_t s = c->stream;
+  // He-uniform initial weights, zero biases
+  std::vector<float> w(kMlpParams, 0.f);
+  uint64_t x = seed ? seed : 0x9E3779B97F4A7C15ull;
+  auto uni = [&]() {
+    x ^= x << 13; x ^= x >> 7; x ^= x << 17;  // xorshift64
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+  };
+  auto fill = [&](int off, int nout, int nin) {
+    const double lim = std::sqrt(6.0 / nin);
+    for (int i = 0; i < nout * nin; ++i) w[off + i] = (float)((2. * uni() - 1.) * lim);
+  };
+  fill(mcg::kMlpW1, kMlpHid, 68);
+  fill(mcg::kMlpW2, kMlpHid, kMlpHid);
+  fill(mcg::kMlpW3, kMlpOut, kMlpHid);
+  for (int o = 0; o < kMlpHid; ++o)
+    for (int i = 68; i < kMlpIn; ++i) w[mcg::kMlpW1 + o * kMlpIn + i] = 0.f;
+  mc_status st;
+  if ((st = put_buf(c->m_w, w.data(), kMlpParams * 4, s)) || (st = put_buf(c->m_g, nullptr, kMlpParams * 4, s)) ||
+      (st = put_buf(c->m_m1, nullptr, kMlpParams * 4, s)) || (st = put_buf(c->m_m2, nullptr, kMlpParams * 4, s)) ||
+      (st = put_buf(c->m_xs, nullptr, (size_t)capacity * kMlpIn * 4, s)) ||
+      (st = put_buf(c->m_ts, nullptr, (size_t)capacity * kMlpOut * 4, s)) ||
+      (st = put_buf(c->m_count, nullptr, 8, s)) || (st = put_buf(c->m_loss, nullptr, 8, s)))
+    return st;
+  MC_CUDA(cudaMemsetAsync(c->m_m1.p, 0, c->m_m1.bytes, s));
+  MC_CUDA(cudaMemsetAsync(c->m_m2.p, 0, c->m_m2.bytes, s));
+  MC_CUDA(cudaMemsetAsync(c->m_count.p, 0, 8, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  c->m_cap = capacity;
+  c->m_n = 0;
+  c->m_step = 0;
+  c->m_ready = true;
+  c->m_norm = false;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_collect(mc_ctx_t *c, int64_t *rows) {
+  if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
+  if (!c->s_mom.p || !c->s_ready) return set_error(MC_ERR_ARG, "no cell update to learn from");
+  cudaStream_t s = c->stream;
+  cudaError_t e = mcg::launch_mlp_collect(c->nc, c->s_mom.as<float>(), c->nc + 1, c->u_hden.as<double>(),
+                                          c->s_te.as<double>(), c->s_X.as<double>(), c->m_cap,
+                                          c->m_count.as<unsigned long long>(), c->m_xs.as<float>(),
+                                          c->m_ts.as<float>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "collect failed: %s", cudaGetErrorString(e));
+  unsigned long long n = 0;
+  MC_CUDA(cudaMemcpyAsync(&n, c->m_count.p, 8, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  c->m_n = (long long)n;
+  c->m_norm = false;
+  if (rows) *rows = std::min((long long)n, c->m_cap);
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_train(mc_ctx_t *c, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                                           double *loss, double *train_ms) {
+  if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
+  if (steps < 0 || batch < 1) return set_error(MC_ERR_ARG, "steps >= 0 and batch >= 1 required");
+  mc_status st;
+  if (!c->m_norm && (st = surrogate_normalise(c))) return st;
+  cudaStream_t s = c->stream;
+  if ((st = ensure(c->m_xb, (size_t)batch * kMlpIn * 4)) || (st = ensure(c->m_tb, (size_t)batch * kMlpOut * 4)))
+    return st;
+  cudaEvent_t e0, e1;
+  MC_CUDA(cudaEventCreate(&e0));
+  MC_CUDA(cudaEventCreate(&e1));
+  MC_CUDA(cudaEventRecord(e0, s));
+  const long long n = std::min(c->m_n, c->m_cap);
+  double last = 0.;
+  for (int k = 0; k < steps; ++k) {
+    const bool tail = k == steps - 1;
+    if (tail) MC_CUDA(cudaMemsetAsync(c->m_loss.p, 0, 8, s));
+    cudaError_t e = mcg::launch_mlp_gather(batch, n, (uint32_t)seed, c->m_step, c->m_xs.as<float>(), c->m_ts.as<float>(),
+                                           c->m_fmean.as<float>(), c->m_fstd.as<float>(), c->m_tmean.as<float>(),
+                                           c->m_tstd.as<float>(), c->m_xb.as<float>(), c->m_tb.as<float>(), s);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "gather failed: %s", cudaGetErrorString(e));
+    if ((st = mlp_backward(c, batch, c->m_xb.as<float>(), c->m_tb.as<float>()))) return st;
+    ++c->m_step;
+    const float b1t = std::pow(0.9f, (float)c->m_step), b2t = std::pow(0.999f, (float)c->m_step);
+    // cosine decay over the call's steps, to 5 % of lr
+    const float lrk = lr * (0.05f + 0.95f * 0.5f * (1.f + std::cos(3.14159265f * (float)k / (float)steps)));
+    e = mcg::launch_mlp_adam(kMlpParams, c->m_w.as<float>(), c->m_g.as<float>(), c->m_m1.as<float>(),
+                             c->m_m2.as<float>(), lrk, b1t, b2t, s);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "adam failed: %s", cudaGetErrorString(e));
+  }
+  MC_CUDA(cudaEventRecord(e1, s));
+  if (steps > 0) MC_CUDA(cudaMemcpyAsync(&last, c->m_loss.p, 8, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (loss) *loss = steps > 0 ? last / ((double)batch * mcg::kMlpTargets) : 0.;
+  if (train_ms) *train_ms = ms;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_params(mc_ctx_t *c, float *get, const float *set) {
+  if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
+  if (set) MC_CUDA(cudaMemcpyAsync(c->m_w.p, set, kMlpParams * 4, cudaMemcpyHostToDevice, c->stream));
+  if (get) MC_CUDA(cudaMemcpyAsync(get, c->m_w.p, kMlpParams * 4, cudaMemcpyDeviceToHost, c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_grads(mc_ctx_t *c, int32_t m, const float *x, const float *t, double *loss,
+                                           float *grads, float *y) {
+  if (!c || !c->m_ready || m < 1 || !x || !t) return set_error(MC_ERR_ARG, "bad surrogate gradient arguments");
+  cudaStream_t s = c->stream;
+  DBuf dx, dt;
+  MC_CUDA(dx.alloc((size_t)m * kMlpIn * 4));
+  MC_CUDA(dt.alloc((size_t)m * kMlpOut * 4));
+  MC_CUDA(cudaMemcpyAsync(dx.p, x, dx.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(dt.p, t, dt.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemsetAsync(c->m_loss.p, 0, 8, s));
+  mc_status st = mlp_backward(c, m, dx.as<float>(), dt.as<float>());
+  if (st) return st;
+  double l = 0.;
+  MC_CUDA(cudaMemcpyAsync(&l, c->m_loss.p, 8, cudaMemcpyDeviceToHost, s));
+  if (grads) MC_CUDA(cudaMemcpyAsync(grads, c->m_g.p, kMlpParams * 4, cudaMemcpyDeviceToHost, s));
+  if (y) MC_CUDA(cudaMemcpyAsync(y, c->m_y.p, (size_t)m * kMlpOut * 4, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  if (loss) *loss = l / ((double)m * mcg::kMlpTargets);
   return MC_OK;
 }
 

@@ -71,6 +71,20 @@ def library():
                                             C.POINTER(abi.McUpdateStats)]
         lib.mc_ctx_opacity_from_state.restype = C.c_int
         lib.mc_ctx_opacity_from_state.argtypes = [C.c_void_p, C.c_int32, ip, fp, C.c_int32, dp]
+        u64 = C.c_uint64
+        lib.mc_ctx_surrogate_init.restype = C.c_int
+        lib.mc_ctx_surrogate_init.argtypes = [C.c_void_p, u64, C.c_int64]
+        lib.mc_ctx_surrogate_collect.restype = C.c_int
+        lib.mc_ctx_surrogate_collect.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        lib.mc_ctx_surrogate_train.restype = C.c_int
+        lib.mc_ctx_surrogate_train.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_float, u64, dp, dp]
+        lib.mc_ctx_update_cells_warm.restype = C.c_int
+        lib.mc_ctx_update_cells_warm.argtypes = [C.c_void_p, fp, C.c_double, C.c_double, C.c_int32,
+                                                 C.POINTER(abi.McUpdateStats)]
+        lib.mc_ctx_surrogate_params.restype = C.c_int
+        lib.mc_ctx_surrogate_params.argtypes = [C.c_void_p, fp, fp]
+        lib.mc_ctx_surrogate_grads.restype = C.c_int
+        lib.mc_ctx_surrogate_grads.argtypes = [C.c_void_p, C.c_int32, fp, fp, dp, fp, fp]
         lib.mc_ctx_get_opacity.restype = C.c_int
         lib.mc_ctx_get_opacity.argtypes = [C.c_void_p, fp]
         lib.mc_ctx_destroy.restype = None
@@ -249,15 +263,50 @@ class TransportContext:
                                               ip(flags)))
         return te, ne, X, conv, niter, flags
 
-    def update_cells(self, w, scale, xhi_limit=0.05, precision="fp64"):
+    def update_cells(self, w, scale, xhi_limit=0.05, precision="fp64", warm=False):
+        """One cell update from the resident Jste; warm=True starts it from the
+        trained surrogate's prediction (mc_ctx_update_cells_warm)."""
         w = np.ascontiguousarray(w, dtype=np.float32)
         if w.shape != (self.neb.nbins, 67):
             raise ValueError("w must be (nbins, 67)")
         prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
         st = abi.McUpdateStats()
-        _check(self.lib.mc_ctx_update_cells(self.handle, _fptr(w), float(scale), float(xhi_limit), prec,
-                                            C.byref(st)))
+        fn = self.lib.mc_ctx_update_cells_warm if warm else self.lib.mc_ctx_update_cells
+        _check(fn(self.handle, _fptr(w), float(scale), float(xhi_limit), prec, C.byref(st)))
         return st.as_dict()
+
+    # ---- the learned warm start ----
+    N_PARAMS = 33072
+
+    def surrogate_init(self, seed=1, capacity=2_000_000):
+        _check(self.lib.mc_ctx_surrogate_init(self.handle, int(seed), int(capacity)))
+
+    def surrogate_collect(self):
+        n = C.c_int64()
+        _check(self.lib.mc_ctx_surrogate_collect(self.handle, C.byref(n)))
+        return n.value
+
+    def surrogate_train(self, steps=300, batch=8192, lr=2e-3, seed=1):
+        loss, ms = C.c_double(), C.c_double()
+        _check(self.lib.mc_ctx_surrogate_train(self.handle, int(steps), int(batch), float(lr), int(seed),
+                                               C.byref(loss), C.byref(ms)))
+        return loss.value, ms.value
+
+    def surrogate_params(self, set=None):
+        out = np.empty(self.N_PARAMS, dtype=np.float32)
+        s = None if set is None else np.ascontiguousarray(set, dtype=np.float32)
+        _check(self.lib.mc_ctx_surrogate_params(self.handle, _fptr(out), _fptr(s)))
+        return out
+
+    def surrogate_grads(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        m = x.shape[0]
+        g = np.empty(self.N_PARAMS, dtype=np.float32)
+        y = np.empty((m, 48), dtype=np.float32)
+        loss = C.c_double()
+        _check(self.lib.mc_ctx_surrogate_grads(self.handle, m, _fptr(x), _fptr(t), C.byref(loss), _fptr(g), _fptr(y)))
+        return loss.value, g, y
 
     def get_opacity(self):
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)

@@ -1,0 +1,106 @@
+"""The learned warm start: the CPU oracle of the MLP pinned by finite
+differences, the GPU's own forward/backward kernels against it, training on
+cell states the update produced, and what the warm start saves."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from mocassin_gb300 import balance, nebula, transport
+from oracle import mlp_oracle as O
+
+
+def _random_params(seed):
+    rng = np.random.default_rng(seed)
+    d = {}
+    for k, (off, shape) in O.OFF.items():
+        fan = shape[1] if len(shape) == 2 else 1
+        d[k] = rng.normal(0, 1.0 / np.sqrt(fan), shape) if len(shape) == 2 else rng.normal(0, 0.1, shape)
+    return O.pack(d)
+
+
+def test_oracle_gradients_by_finite_differences():
+    p = _random_params(1).astype(np.float64)
+    rng = np.random.default_rng(2)
+    x = rng.normal(0, 1, (16, O.NI))
+    t = rng.normal(0, 1, (16, O.NO))
+    _, g, _ = O.loss_and_grads(p, x, t, rounding=False)
+    flat = O.pack(g).astype(np.float64)
+    for k in rng.choice(O.NPARAM, 40, replace=False):
+        h = 1e-5
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        fd = (O.loss_and_grads(pp, x, t, False)[0] - O.loss_and_grads(pm, x, t, False)[0]) / (2 * h)
+        assert abs(fd - flat[k]) <= 1e-6 + 1e-4 * abs(fd), (k, fd, flat[k])
+
+
+def _ions():
+    return [tuple(int(v) for v in r) for r in nebula.atomic_table()["ions"]]
+
+
+@pytest.mark.gpu
+def test_gpu_gradients_match_oracle(gpu_lib):
+    neb = nebula.build(nebula.small_cases()[0])
+    ctx = transport.TransportContext(neb)
+    ctx.surrogate_init(seed=3, capacity=16)
+    p = _random_params(4)
+    ctx.surrogate_params(set=p)
+    np.testing.assert_array_equal(ctx.surrogate_params(), p)
+    rng = np.random.default_rng(5)
+    x = rng.normal(0, 1, (300, O.NI)).astype(np.float32)
+    t = rng.normal(0, 1, (300, O.NO)).astype(np.float32)
+    loss, g, y = ctx.surrogate_grads(x, t)
+    ctx.close()
+    oloss, og, oy = O.loss_and_grads(p, x, t)
+    np.testing.assert_allclose(y, oy, rtol=2e-5, atol=2e-5)
+    assert abs(loss - oloss) <= 1e-5 * oloss
+    gd = O.unpack(g)
+    for k in og:
+        scale = np.abs(og[k]).max()
+        assert np.abs(gd[k] - og[k]).max() <= 1e-4 * scale + 1e-12, k
+
+
+def _clumpy(n=31, packets=2_000_000):
+    return nebula.build(dataclasses.replace(nebula.clumpy61(packets), name="clumpy%d" % n, n=n))
+
+
+@pytest.mark.gpu
+def test_trained_warm_start_saves_temperature_steps(gpu_lib):
+    neb = _clumpy()
+    ctx = transport.TransportContext(neb)
+    ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+    te, ne, X = balance.initial_state(neb)
+    ctx.set_cell_state(te, ne, X)
+    ions = _ions()
+    w = balance.moment_weights(neb.xs, neb.nu, ions)
+    sp = np.array(ions, dtype=np.int32)
+    ctx.surrogate_init(seed=1, capacity=200_000)
+    for it in range(4):
+        ctx.run(seed=50 + it, precision="fp32", zero_first=True)
+        ctx.update_cells(w, 1e-9, precision="fp32")
+        ctx.opacity_from_state(sp, neb.xs)
+        if it >= 1:
+            ctx.surrogate_collect()
+    first, _ = ctx.surrogate_train(steps=1, batch=4096, lr=2e-3)
+    loss, train_ms = ctx.surrogate_train(steps=2000, batch=4096, lr=3e-3)
+    assert loss < 0.2 * first, (first, loss)
+    # the same update, cold and warm, from the same state and Jste
+    ctx.run(seed=99, precision="fp32", zero_first=True)
+    s0 = ctx.get_cell_state()
+    cold = ctx.update_cells(w, 1e-9, precision="fp32")
+    te_c = ctx.get_cell_state()[0]
+    ctx.set_cell_state(s0[0], s0[1], s0[2])
+    warm = ctx.update_cells(w, 1e-9, precision="fp32", warm=True)
+    te_w = ctx.get_cell_state()[0]
+    ctx.close()
+    assert warm["hit"] == cold["hit"]
+    gain = {"t_steps": (cold["t_iterations"], warm["t_iterations"]), "ms": (cold["update_ms"], warm["update_ms"]),
+            "no_te": (cold["no_te_balance"], warm["no_te_balance"]), "loss": (first, loss), "train_ms": train_ms}
+    assert warm["t_iterations"] < 0.75 * cold["t_iterations"], gain
+    assert warm["update_ms"] < cold["update_ms"], gain
+    assert warm["no_te_balance"] <= cold["no_te_balance"] * 1.1 + 10, gain
+    c = np.nonzero(s0[3][1:] >= 0)[0] + 1
+    d = np.abs(te_w[c] / te_c[c] - 1)
+    assert np.median(d) < 0.02, (np.median(d), gain)
+    print("warm start", gain)
