@@ -175,17 +175,22 @@ def converged_model(neb, args):
     """Wall time to a converged model: Lambda iterations (transport, cell
     update, opacity rebuild) until 95 % of the cells have |dX(H0)/X(H0)| <=
     5 % (the reference's minConvergence / XHILimit), for the chosen form
-    (persistent wave march, FP32 cell update) and the plain form (one thread
-    per history, FP64 cell update), from the same initial state."""
+    (persistent wave march, FP32 cell update started from the learned
+    surrogate after two iterations), the same without the surrogate, and the
+    plain form (one thread per history, FP64 cell update), from the same
+    initial state."""
     from mocassin_gb300 import iterate
     out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
            "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
-    for name, form, upd in (("chosen", "wave", "fp32"), ("plain", "plain", "fp64")):
-        li = iterate.LambdaIteration(neb, form=form, update=upd)
+    forms = (("chosen", "wave", "fp32", {"train_after": 2}), ("chosen_no_surrogate", "wave", "fp32", None),
+             ("plain", "plain", "fp64", None))
+    for name, form, upd, sur in forms:
+        li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
         wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
         li.close()
         last = hist[-1]
-        out[name] = {"transport": form, "update": upd, "wall_s": wall, "iterations": len(hist),
+        out[name] = {"transport": form, "update": upd, "surrogate": sur is not None, "wall_s": wall,
+                     "iterations": len(hist), "surrogate_s": sum(h["surrogate_s"] for h in hist),
                      "converged": last["converged_pct"] >= 95.0, "converged_pct": last["converged_pct"],
                      "dte_lt_1pc_pct": last["dte_lt_1pc_pct"],
                      "transport_s": sum(h["transport_s"] for h in hist), "update_s": sum(h["update_s"] for h in hist),

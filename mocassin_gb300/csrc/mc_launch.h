@@ -109,11 +109,13 @@ cudaError_t launch_mlp_wgrad(int M, int nin, int nout, const float *dz, const fl
                              float *db, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_loss(int M, int nt, int ld, const float *y, const float *tn, float *dy, double *loss,
                             cudaStream_t s);
-cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, float lr, float b1t, float b2t,
-                            cudaStream_t s);
-cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, int step, const float *xs, const float *ts,
+cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, const int *dstep, int step0,
+                            int steps, float lr, cudaStream_t s);
+cudaError_t launch_mlp_step(int *dstep, cudaStream_t s);
+cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dstep, const float *xs, const float *ts,
                               const float *fmean, const float *fstd, const float *tmean, const float *tstd, float *xb,
                               float *tb, cudaStream_t s);
+cudaError_t mlp_prepare();
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s);
 cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
                                const double *X, long long cap, unsigned long long *count, float *xs, float *ts,

@@ -122,7 +122,7 @@ struct mc_ctx {
   int u_ncel = 0, u_ndirec = 0, u_naldro = 0, u_maxlev = 1;
   int u_bal_z[7] = {}, u_bal_first[7] = {};
   // learned warm start: parameters, Adam state, training buffer, work arrays
-  DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss;
+  DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss, m_dstep;
   DBuf m_xb, m_tb, m_a1, m_a2, m_y, m_dy, m_d2, m_d1, m_xi, m_h1, m_h2, m_yi, m_te_prev, m_xh0_prev;
   long long m_cap = 0, m_n = 0;
   int m_step = 0, m_B = 0;
@@ -1350,8 +1350,11 @@ extern "C" mc_status mc_ctx_surrogate_init(mc_ctx_t *c, uint64_t seed, int64_t c
       (st = put_buf(c->m_m1, nullptr, kMlpParams * 4, s)) || (st = put_buf(c->m_m2, nullptr, kMlpParams * 4, s)) ||
       (st = put_buf(c->m_xs, nullptr, (size_t)capacity * kMlpIn * 4, s)) ||
       (st = put_buf(c->m_ts, nullptr, (size_t)capacity * kMlpOut * 4, s)) ||
-      (st = put_buf(c->m_count, nullptr, 8, s)) || (st = put_buf(c->m_loss, nullptr, 8, s)))
+      (st = put_buf(c->m_count, nullptr, 8, s)) || (st = put_buf(c->m_loss, nullptr, 8, s)) ||
+      (st = put_buf(c->m_dstep, nullptr, sizeof(int), s)))
     return st;
+  MC_CUDA(mcg::mlp_prepare());
+  MC_CUDA(cudaMemsetAsync(c->m_dstep.p, 0, sizeof(int), s));
   MC_CUDA(cudaMemsetAsync(c->m_m1.p, 0, c->m_m1.bytes, s));
   MC_CUDA(cudaMemsetAsync(c->m_m2.p, 0, c->m_m2.bytes, s));
   MC_CUDA(cudaMemsetAsync(c->m_count.p, 0, 8, s));
@@ -1397,22 +1400,42 @@ extern "C" mc_status mc_ctx_surrogate_train(mc_ctx_t *c, int32_t steps, int32_t 
   MC_CUDA(cudaEventRecord(e0, s));
   const long long n = std::min(c->m_n, c->m_cap);
   double last = 0.;
-  for (int k = 0; k < steps; ++k) {
-    const bool tail = k == steps - 1;
-    if (tail) MC_CUDA(cudaMemsetAsync(c->m_loss.p, 0, 8, s));
-    cudaError_t e = mcg::launch_mlp_gather(batch, n, (uint32_t)seed, c->m_step, c->m_xs.as<float>(), c->m_ts.as<float>(),
-                                           c->m_fmean.as<float>(), c->m_fstd.as<float>(), c->m_tmean.as<float>(),
-                                           c->m_tstd.as<float>(), c->m_xb.as<float>(), c->m_tb.as<float>(), s);
+  const int step0 = c->m_step;
+  // one training step: minibatch, forward, loss, backward, Adam, t += 1
+  auto one_step = [&]() -> mc_status {
+    MC_CUDA(cudaMemsetAsync(c->m_loss.p, 0, 8, s));
+    cudaError_t e = mcg::launch_mlp_gather(batch, n, (uint32_t)seed, c->m_dstep.as<int>(), c->m_xs.as<float>(),
+                                           c->m_ts.as<float>(), c->m_fmean.as<float>(), c->m_fstd.as<float>(),
+                                           c->m_tmean.as<float>(), c->m_tstd.as<float>(), c->m_xb.as<float>(),
+                                           c->m_tb.as<float>(), s);
     if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "gather failed: %s", cudaGetErrorString(e));
-    if ((st = mlp_backward(c, batch, c->m_xb.as<float>(), c->m_tb.as<float>()))) return st;
-    ++c->m_step;
-    const float b1t = std::pow(0.9f, (float)c->m_step), b2t = std::pow(0.999f, (float)c->m_step);
-    // cosine decay over the call's steps, to 5 % of lr
-    const float lrk = lr * (0.05f + 0.95f * 0.5f * (1.f + std::cos(3.14159265f * (float)k / (float)steps)));
+    mc_status bs = mlp_backward(c, batch, c->m_xb.as<float>(), c->m_tb.as<float>());
+    if (bs) return bs;
     e = mcg::launch_mlp_adam(kMlpParams, c->m_w.as<float>(), c->m_g.as<float>(), c->m_m1.as<float>(),
-                             c->m_m2.as<float>(), lrk, b1t, b2t, s);
+                             c->m_m2.as<float>(), c->m_dstep.as<int>(), step0, steps, lr, s);
+    if (e == cudaSuccess) e = mcg::launch_mlp_step(c->m_dstep.as<int>(), s);
     if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "adam failed: %s", cudaGetErrorString(e));
+    return MC_OK;
+  };
+  // the first step runs eagerly (it sizes the work arrays); the rest replay
+  // a captured graph of one step
+  if (steps > 0 && (st = one_step())) return st;
+  if (steps > 1) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    MC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    mc_status cs = one_step();
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (cs) { if (graph) cudaGraphDestroy(graph); return cs; }
+    if (ce != cudaSuccess) return set_error(MC_ERR_CUDA, "training capture failed: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return set_error(MC_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce));
+    for (int k = 1; k < steps && ce == cudaSuccess; ++k) ce = cudaGraphLaunch(exec, s);
+    cudaGraphExecDestroy(exec);
+    if (ce != cudaSuccess) return set_error(MC_ERR_CUDA, "graph launch failed: %s", cudaGetErrorString(ce));
   }
+  c->m_step += steps;
   MC_CUDA(cudaEventRecord(e1, s));
   if (steps > 0) MC_CUDA(cudaMemcpyAsync(&last, c->m_loss.p, 8, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));

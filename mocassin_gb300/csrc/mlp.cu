@@ -39,19 +39,21 @@ __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__floa
 constexpr int kRows = 128;
 
 // act: 0 linear, 1 ReLU.  mask (data gradient): inputs are multiplied by
-// (maskv[m][i] > 0), the ReLU derivative of the layer output they belong to.
+// (mask[m][i] > 0), the ReLU derivative of the layer output they belong to.
+// Block (x, y): rows 128 x .. 128 x + 127, outputs 16 y .. 16 y + 15.
+constexpr int kOC = 16;
 __global__ void __launch_bounds__(kRows) mlp_dense_kernel(int M, int nin, int nout, const float *in, int ldin,
                                                           const float *mask, const float *W, bool transposed,
                                                           const float *bias, int act, bool round_in, float *out,
                                                           int ldout) {
   extern __shared__ float sh[];
-  float *S = sh;                        // [nin][nout]
-  float *X = sh + (size_t)nin * nout;   // [nin][kRows]
-  const int t = threadIdx.x, m0 = blockIdx.x * kRows, m = m0 + t;
+  float *S = sh;                        // [nin][kOC]
+  float *X = sh + (size_t)nin * kOC;    // [nin][kRows]
+  const int t = threadIdx.x, m = blockIdx.x * kRows + t, o0 = blockIdx.y * kOC;
   // weights: forward S[i][o] = W[o][i] (W is [nout][nin]); data gradient
   // S[i][o] = W[i][o] (W is [nin][nout] = the forward layer's [out][in])
-  for (int q = t; q < nin * nout; q += kRows) {
-    const int i = q / nout, o = q % nout;
+  for (int q = t; q < nin * kOC; q += kRows) {
+    const int i = q / kOC, o = o0 + q % kOC;
     S[q] = bf16r(transposed ? W[(size_t)i * nout + o] : W[(size_t)o * nin + i]);
   }
   for (int i = 0; i < nin; ++i) {
@@ -65,22 +67,20 @@ __global__ void __launch_bounds__(kRows) mlp_dense_kernel(int M, int nin, int no
   }
   __syncthreads();
   if (m >= M) return;
-  for (int o0 = 0; o0 < nout; o0 += 16) {
-    float acc[16];
+  float acc[kOC];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) acc[j] = (bias && o0 + j < nout) ? bias[o0 + j] : 0.f;
-    for (int i = 0; i < nin; ++i) {
-      const float x = X[i * kRows + t];
-      const float *s = S + (size_t)i * nout + o0;
+  for (int j = 0; j < kOC; ++j) acc[j] = bias ? bias[o0 + j] : 0.f;
+  for (int i = 0; i < nin; ++i) {
+    const float x = X[i * kRows + t];
+    const float *sr = S + (size_t)i * kOC;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) acc[j] += x * s[j];
-    }
+    for (int j = 0; j < kOC; ++j) acc[j] += x * sr[j];
+  }
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float v = acc[j];
-      if (act == 1) v = v > 0.f ? v : 0.f;
-      out[(size_t)m * ldout + o0 + j] = v;
-    }
+  for (int j = 0; j < kOC; ++j) {
+    float v = acc[j];
+    if (act == 1) v = v > 0.f ? v : 0.f;
+    out[(size_t)m * ldout + o0 + j] = v;
   }
 }
 
@@ -147,7 +147,14 @@ __global__ void mlp_loss_kernel(int M, int nt, int ld, const float *y, const flo
   if ((threadIdx.x & 31) == 0 && s != 0.) atomicAdd(loss, s);
 }
 
-__global__ void mlp_adam_kernel(int n, float *w, const float *g, float *m1, float *m2, float lr, float b1t, float b2t) {
+// the step count t lives on the device so that a captured training step can
+// be replayed: bias corrections 0.9^t, 0.999^t and the cosine decay of the
+// learning rate over the call (to 5 %) are formed here
+__global__ void mlp_adam_kernel(int n, float *w, const float *g, float *m1, float *m2, const int *dstep, int step0,
+                                int steps, float lr0) {
+  const int t = *dstep + 1;
+  const float b1t = powf(0.9f, (float)t), b2t = powf(0.999f, (float)t);
+  const float lr = lr0 * (0.05f + 0.95f * 0.5f * (1.f + cosf(3.14159265f * (float)(t - 1 - step0) / (float)steps)));
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float a = 0.9f * m1[i] + 0.1f * gi, b = 0.999f * m2[i] + 0.001f * gi * gi;
@@ -159,9 +166,12 @@ __global__ void mlp_adam_kernel(int n, float *w, const float *g, float *m1, floa
 }
 
 // a minibatch of training rows: row r = the Philox draw of (step, r) modulo n
-__global__ void mlp_gather_kernel(int B, long long n, uint32_t seed, int step, const float *xs, const float *ts,
+__global__ void mlp_step_kernel(int *dstep) { *dstep += 1; }
+
+__global__ void mlp_gather_kernel(int B, long long n, uint32_t seed, const int *dstep, const float *xs, const float *ts,
                                   const float *fmean, const float *fstd, const float *tmean, const float *tstd,
                                   float *xb, float *tb) {
+  const int step = *dstep;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < B; r += gridDim.x * blockDim.x) {
     const uint4 v = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)step, 0x4d4c50u, 0u), seed, 0x9e3779b9u);
     const long long src = (long long)(((unsigned long long)v.x << 32 | v.y) % (unsigned long long)n);
@@ -268,17 +278,19 @@ __global__ void mlp_apply_kernel(int nc, const float *mom, const float *y, const
 
 }  // namespace
 
-size_t mlp_dense_smem(int nin, int nout) { return ((size_t)nin * nout + (size_t)nin * kRows) * sizeof(float); }
+size_t mlp_dense_smem(int nin, int nout) {
+  (void)nout;
+  return ((size_t)nin * kOC + (size_t)nin * kRows) * sizeof(float);
+}
 
 cudaError_t launch_mlp_dense(int M, int nin, int nout, const float *in, int ldin, const float *mask, const float *W,
                              bool transposed, const float *bias, int act, bool round_in, float *out, int ldout,
                              cudaStream_t s) {
-  if (nout % 16 != 0) return cudaErrorInvalidValue;
-  const size_t sh = mlp_dense_smem(nin, nout);
-  cudaError_t e = cudaFuncSetAttribute(mlp_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
-  if (e != cudaSuccess) return e;
-  mlp_dense_kernel<<<(M + kRows - 1) / kRows, kRows, sh, s>>>(M, nin, nout, in, ldin, mask, W, transposed, bias, act,
-                                                              round_in, out, ldout);
+  if (nout % 16 != 0 || nin > kMlpHid) return cudaErrorInvalidValue;
+  const size_t sh = mlp_dense_smem(nin, nout);  // within the limit mlp_prepare set
+  mlp_dense_kernel<<<dim3((M + kRows - 1) / kRows, nout / kOC), kRows, sh, s>>>(M, nin, nout, in, ldin, mask, W,
+                                                                                transposed, bias, act, round_in, out,
+                                                                                ldout);
   return cudaGetLastError();
 }
 
@@ -298,17 +310,27 @@ cudaError_t launch_mlp_loss(int M, int nt, int ld, const float *y, const float *
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, float lr, float b1t, float b2t,
-                            cudaStream_t s) {
-  mlp_adam_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, w, g, m1, m2, lr, b1t, b2t);
+cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, const int *dstep, int step0,
+                            int steps, float lr, cudaStream_t s) {
+  mlp_adam_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, w, g, m1, m2, dstep, step0, steps, lr);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, int step, const float *xs, const float *ts,
+cudaError_t launch_mlp_step(int *dstep, cudaStream_t s) {
+  mlp_step_kernel<<<1, 1, 0, s>>>(dstep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dstep, const float *xs, const float *ts,
                               const float *fmean, const float *fstd, const float *tmean, const float *tstd, float *xb,
                               float *tb, cudaStream_t s) {
-  mlp_gather_kernel<<<(B + 255) / 256, 256, 0, s>>>(B, n, seed, step, xs, ts, fmean, fstd, tmean, tstd, xb, tb);
+  mlp_gather_kernel<<<(B + 255) / 256, 256, 0, s>>>(B, n, seed, dstep, xs, ts, fmean, fstd, tmean, tstd, xb, tb);
   return cudaGetLastError();
+}
+
+cudaError_t mlp_prepare() {
+  return cudaFuncSetAttribute(mlp_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)mlp_dense_smem(kMlpHid, kMlpHid));
 }
 
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s) {

@@ -18,8 +18,9 @@ step (emission_mod.f90:905-1311) is not part of this path.
 ``form`` picks the transport ("wave": the frequency-sorted persistent march;
 "plain": one thread per history) and ``update`` the arithmetic of the cell
 update ("fp64": the FP64 method; "fp32": the reference's own 4-byte
-precision).  ``warm_start`` is an optional callable that sets the cell state
-(Te, ionic fractions) before each update from the Jste sums.
+precision).  ``surrogate`` adds the learned warm start: the cell states of
+the first iterations train an MLP on the GPU, which then predicts the state
+each later update starts from (mc_ctx_update_cells_warm).
 """
 import time
 
@@ -35,7 +36,11 @@ def _ions():
 class LambdaIteration:
     """A nebula resident on the GPU with its cell state."""
 
-    def __init__(self, neb, form="wave", update="fp32", xhi_limit=0.05, opacity_method="bf16x3"):
+    def __init__(self, neb, form="wave", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None):
+        """surrogate: None (updates start from the previous state, as the
+        reference's) or a dict with train_after (cold iterations whose cell
+        states train the MLP first), steps, batch, lr, finetune_steps (after
+        every later iteration), capacity (training rows kept)."""
         self.neb = neb
         self.form = form
         self.update = update
@@ -49,19 +54,37 @@ class LambdaIteration:
         self.w = balance.moment_weights(neb.xs, neb.nu, self.species)
         self.scale = 1e-9 / (8.0 if neb.flags & nebula.FLAG_SYMMETRIC_XYZ else 1.0)
         self.history = []
+        self.sur = None
+        self.trained = False
+        if surrogate is not None:
+            self.sur = dict({"train_after": 2, "steps": 500, "batch": 4096, "lr": 3e-3, "finetune_steps": 0,
+                             "capacity": 1_000_000, "seed": 1}, **surrogate)
+            self.ctx.surrogate_init(seed=self.sur["seed"], capacity=self.sur["capacity"])
 
-    def step(self, seed, n_packets=None, warm_start=None):
+    def step(self, seed, n_packets=None):
         t0 = time.perf_counter()
         tr = self.ctx.run(n_packets=n_packets, seed=seed, iteration=len(self.history) + 1, precision="fp32",
                           zero_first=True, form=self.form)
         t1 = time.perf_counter()
-        if warm_start is not None:
-            warm_start(self)
-        up = self.ctx.update_cells(self.w, self.scale, xhi_limit=self.xhi, precision=self.update)
+        warm = self.trained
+        up = self.ctx.update_cells(self.w, self.scale, xhi_limit=self.xhi, precision=self.update, warm=warm)
         t2 = time.perf_counter()
+        train_ms, loss = 0.0, None
+        if self.sur is not None:
+            self.ctx.surrogate_collect()
+            if not self.trained and len(self.history) + 1 >= self.sur["train_after"]:
+                loss, train_ms = self.ctx.surrogate_train(self.sur["steps"], self.sur["batch"], self.sur["lr"],
+                                                          self.sur["seed"])
+                self.trained = True
+            elif self.trained and self.sur["finetune_steps"] > 0:
+                loss, train_ms = self.ctx.surrogate_train(self.sur["finetune_steps"], self.sur["batch"],
+                                                          0.3 * self.sur["lr"], self.sur["seed"])
+        t2b = time.perf_counter()
         op_ms = self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
         t3 = time.perf_counter()
-        rec = {"iteration": len(self.history) + 1, "transport_s": t1 - t0, "update_s": t2 - t1, "opacity_s": t3 - t2,
+        rec = {"iteration": len(self.history) + 1, "transport_s": t1 - t0, "update_s": t2 - t1,
+               "surrogate_s": t2b - t2, "surrogate_train_ms": train_ms, "surrogate_loss": loss, "warm": warm,
+               "opacity_s": t3 - t2b,
                "wall_s": t3 - t0, "crossings": tr["crossings"], "transport_kernel_ms": tr["kernel_ms"],
                "update_ms": up["update_ms"], "moments_ms": up["moments_ms"], "opacity_ms": op_ms,
                "hit": up["hit"], "converged_pct": 100.0 * up["converged"] / max(up["hit"], 1),
@@ -70,11 +93,11 @@ class LambdaIteration:
         self.history.append(rec)
         return rec
 
-    def run(self, seed=1, max_iterations=30, min_convergence=95.0, n_packets=None, warm_start=None):
+    def run(self, seed=1, max_iterations=30, min_convergence=95.0, n_packets=None):
         """Iterates until converged_pct >= min_convergence; returns the wall time and the history."""
         t0 = time.perf_counter()
         for it in range(max_iterations):
-            rec = self.step(seed + it, n_packets=n_packets, warm_start=warm_start)
+            rec = self.step(seed + it, n_packets=n_packets)
             if rec["converged_pct"] >= min_convergence:
                 break
         return time.perf_counter() - t0, self.history
