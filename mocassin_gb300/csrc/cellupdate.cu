@@ -56,12 +56,12 @@ __global__ void species_kernel(int nc, int nsp, const int *sp_e, const int *sp_s
 
 }  // namespace
 
-cudaError_t launch_cell_update(const UpdArgs &a, int fp32, int num_sms, cudaStream_t stream) {
+cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int num_sms, cudaStream_t stream) {
+  if (fp32) return launch_cell_update_fp32(a, scratch, num_sms, stream);
   const int cells = a.nc;
   int blocks = (cells + kW - 1) / kW;
   if (blocks > num_sms * 16) blocks = num_sms * 16;
   if (blocks < 1) blocks = 1;
-  if (fp32) return launch_cell_update_fp32(a, blocks, stream);
   cell_update_kernel<double, false><<<blocks, kW * 32, 0, stream>>>(a);
   return cudaGetLastError();
 }

@@ -1,17 +1,293 @@
-// cellupdate_fp32.cu -- the FP32 instantiation of the cell-update kernel
-// (the reference's own updateCell arithmetic is 4-byte `real`); compiled
-// with the default contraction into FMA.
+// cellupdate_fp32.cu -- the FP32 form of the cell update as T-step
+// wavefronts over all cells (the reference's own updateCell arithmetic is
+// 4-byte `real`); compiled with the default contraction into FMA.
+//
+// The FP64 form (cellupdate.cuh, one warp per cell) follows the oracle
+// operation by operation.  This form runs the same per-cell algorithm --
+// iterateT's bracketed secant around ionBalance and thermBalance
+// (update_mod.f90:339-1622) -- but batched across cells one T step at a
+// time, so every lane of a warp does the same work:
+//   wave_ion_kernel    one thread per active cell: calcAlpha and the
+//                      ionBalance passes (at most 25) at the cell's Te;
+//   wave_cel_kernel    one thread per (line ion, active cell): the level
+//                      populations and forbidden-line cooling of that ion
+//                      (equilibrium, emission_mod.f90:1913-2115); the 32
+//                      lanes of a warp are 32 cells of one ion, so the level
+//                      count and every loop bound are uniform;
+//   wave_therm_kernel  one thread per active cell: the heating and cooling
+//                      totals, the residual test and the secant step; a cell
+//                      that is done writes its state, the others go on to
+//                      the next T step's active list.
+// State between the kernels is structure-of-arrays over cells (coalesced).
+// The host issues the 25 possible T steps without synchronising: each
+// kernel reads the active count from device memory.
 #include "cellupdate.cuh"
 
 namespace mcg {
 
-// the level-population matrices of a block's warps in shared memory
-cudaError_t launch_cell_update_fp32(const UpdArgs &a, int blocks, cudaStream_t stream) {
-  const size_t smem = (size_t)kW * a.ncel * a.mat_stride * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(cell_update_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+namespace {
+
+constexpr int kX = kNE * kNX;  // 56 ion slots per cell
+
+struct WaveArgs {
+  UpdArgs a;
+  float *Xs;          // [56][nc+1] ion fractions, slot-major
+  float *Te, *Ne;     // [nc+1]
+  float *sec;         // [5][nc+1]: Thigh, Tlow, resHigh, resLow, fstep
+  int *nit, *flags;   // [nc+1]: T steps, bit 1 = ion balance not converged in the last step
+  float *cool;        // [ncel][nc+1] forbidden-line cooling per H
+  int *act[2];        // active lists
+  int *count;         // [2] their lengths
+};
+
+__device__ __forceinline__ float &XS(const WaveArgs &w, int slot, int c) {
+  return w.Xs[(size_t)slot * (w.a.nc + 1) + c];
+}
+
+__global__ void wave_init_kernel(const __grid_constant__ WaveArgs w) {
+  const UpdArgs &a = w.a;
+  const size_t nc1 = (size_t)a.nc + 1;
+  for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= a.nc; c += gridDim.x * blockDim.x) {
+    if (!(a.mom[c] > 0.f)) {
+      a.conv[c] = 0; a.niter[c] = 0; a.flags[c] = 0; a.dte[c] = -1.;
+      continue;
+    }
+    const double *Xc = a.X + (size_t)c * kX;
+    for (int i = 0; i < kX; ++i) w.Xs[i * nc1 + c] = (float)Xc[i];
+    w.Te[c] = (float)a.te[c];
+    w.Ne[c] = (float)a.ne[c];
+    for (int k = 0; k < 4; ++k) w.sec[k * nc1 + c] = 0.f;
+    w.sec[4 * nc1 + c] = (float)a.step0;
+    w.nit[c] = 0;
+    w.flags[c] = 0;
+    w.act[0][atomicAdd(&w.count[0], 1)] = c;
+  }
+}
+
+// calcAlpha and ionBalance of every active cell at its current Te
+__global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  const UpdArgs &a = w.a;
+  const UpdTabs<float> &T = a.f;
+  const int n = w.count[cur];
+  const float xMax = 0.99999f;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int c = w.act[cur][k];
+    const float Te = w.Te[c], hden = (float)a.hden[c];
+    float X[kNE][kNX];
+    for (int e = 0; e < kNE; ++e)
+      for (int s = 0; s < kNX; ++s) X[e][s] = XS(w, e * kNX + s, c);
+    float alpha[kNB];
+    for (int b = 0; b < kNB; ++b) alpha[b] = alpha_of<float>(a, T.bal[b], Te);
+    float Ne = w.Ne[c];
+    float expFact = 157893.94f / Te;
+    if (expFact > 75.f) expFact = 75.f;
+    const float collIon0 = 2.75E-16f * Te * sqrtf(Te) * (157893.94f / Te + 2.f) * expf(-expFact);
+    const float t4 = Te / 10000.f;
+    // the charge-exchange rates depend on Te only
+    float ch[kNB], rev[kNB];
+    for (int b = 0; b < kNB; ++b) {
+      const UpdIonT<float> &B = T.bal[b];
+      float x = B.chex[0] * powf(t4, B.chex[1]) * (1.f + B.chex[2] * expf(B.chex[3] * t4));
+      if (x < 0.f) x = 0.f;
+      if (Te < 6000.f || Te > 5.e4f) x = 0.f;
+      ch[b] = x;
+      rev[b] = B.dek > 1.f ? x * hden * 2.f * expf(-B.dek / Te) / B.g0g1 : 0.f;
+    }
+    bool conv = true;
+    for (int pass = 1;; ++pass) {
+      conv = true;
+      const float HIOld = X[0][1], HeIOld = X[1][1], HeIIOld = X[1][2];
+      float ratio[kNB];
+      for (int b = 0; b < kNB; ++b) {
+        const float P = a.mom[(size_t)(1 + b) * a.mstride + c] + 1e-20f;
+        const float collIon = b == 0 ? collIon0 : 0.f;
+        ratio[b] = (P + collIon + rev[b] * (1.f - HIOld)) / (Ne * alpha[b] + ch[b] * hden * HIOld);
+      }
+      float ne = 0.f;
+      for (int e = 0; e < kNE; ++e) {
+        const int z = a.bal_z[e], b0 = a.bal_first[e], ni = nion_of(z), ns = nstage_of(z);
+        float prod[kNS + 1];
+        float p = 1.f, den = 1.f;
+        for (int ion = 1; ion <= ni; ++ion) {
+          p *= ratio[b0 + ion - 1];
+          prod[ion] = p;
+          den += p;
+        }
+        for (int ion = 1; ion <= ns; ++ion) {
+          float v = ion == 1 ? 1.f / den : prod[ion - 1] / den;
+          v = fminf(fmaxf(v, 1.e-20f), xMax);
+          X[e][ion] = v;
+          if (ion >= 2 && v >= 1.e-10f) ne += (float)(ion - 1) * T.ab[e] * v;
+        }
+      }
+      Ne = ne * hden;
+      if (Ne == 0.f) Ne = 1.f;
+      const bool off = fabsf((X[0][1] - HIOld) / HIOld) > 0.01f || fabsf((X[1][1] - HeIOld) / HeIOld) > 0.01f ||
+                       fabsf((X[1][2] - HeIIOld) / HeIIOld) > 0.01f;
+      if (off && pass < 25) continue;
+      if (off) conv = false;
+      break;
+    }
+    for (int e = 0; e < kNE; ++e)
+      for (int s = 1; s < kNX; ++s) XS(w, e * kNX + s, c) = X[e][s];
+    w.Ne[c] = Ne;
+    w.flags[c] = conv ? 0 : 2;
+  }
+}
+
+// forbidden-line cooling per H of line ion `ion` in every active cell
+__global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  const UpdArgs &a = w.a;
+  const UpdTabs<float> &T = a.f;
+  const int n = w.count[cur];
+  const long long total = (long long)n * a.ncel;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(q / n), c = w.act[cur][q % n];
+    const UpdCelT<float> &C = T.cel[k];
+    const float Te = w.Te[c], Ne = w.Ne[c];
+    const float xi = XS(w, C.e * kNX + C.ion, c);
+    const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
+    float x[kNL * kNL];
+    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, kNL);
+    w.cool[(size_t)k * (a.nc + 1) + c] = cool * T.ab[C.e] * xi * 1.9865e-16f;
+  }
+}
+
+// heating and cooling totals, the residual test and the secant step
+__global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  const UpdArgs &a = w.a;
+  const UpdTabs<float> &T = a.f;
+  const int n = w.count[cur];
+  const size_t nc1 = (size_t)a.nc + 1;
+  const float kB = 1.380658e-16f, hcRyd = 2.1799153e-11f;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int c = w.act[cur][k];
+    float Te = w.Te[c];
+    const float Ne = w.Ne[c];
+    const float log10Te = log10f(Te), Te4 = Te / 1.e4f;
+    auto poly4 = [](float x, float c0, float c1, float c2, float c3, float c4) {
+      return c0 + x * (c1 + x * (c2 + x * (c3 + x * c4)));
+    };
+    auto bff = [&](float x) { return poly4(x, 1.0108464E-11f, 9.7930778E-13f, -6.6433144E-13f, 2.4793747E-13f, -2.3938215E-14f); };
+    auto brec = [&](float x) { return poly4(x, 9.4255985E-11f, -4.04794384E-12f, -1.0055237E-11f, 1.99266862E-12f, -1.06681387E-13f); };
+    const float xH1 = XS(w, 1, c), xH2 = XS(w, 2, c), xHe2 = XS(w, kNX + 2, c), xHe3 = XS(w, kNX + 3, c);
+    float Np = xH2 * T.ab[0];
+    float coolFF = Np * Ne * bff(log10Te) * kB * Te / sqrtf(Te);
+    float coolRec = Np * Ne * brec(log10Te) * kB * Te / sqrtf(Te);
+    Np = xHe3 * T.ab[1];
+    const float lts = log10f(Te / 4.f);
+    coolFF += Np * Ne * (2.f * bff(lts)) * kB * Te / sqrtf(Te / 4.f);
+    coolRec += Np * Ne * (2.f * brec(lts)) * kB * Te / sqrtf(Te / 4.f);
+    Np = xHe2 * T.ab[1];
+    coolFF += Np * Ne * (1.070073e-11f - 2.5730207e-13f * log10Te + 2.109134e-13f * log10Te * log10Te) * kB * Te / sqrtf(Te);
+    coolRec += Np * Ne * brec(log10Te) * kB * Te / sqrtf(Te);
+    float coolColl = 0.f;
+    if (Te > 5000.f)
+      coolColl = (2.47e-8f * expf(-118338.f / Te) * powf(Te4, -0.228f) + 1.32e-8f * expf(-140252.f / Te) * powf(Te4, -0.460f)) *
+                 hcRyd * xH1 * Ne;
+    for (int i = 0; i < a.ncel; ++i) coolColl += w.cool[(size_t)i * nc1 + c];
+    float heat = 0.f;
+    for (int b = 0; b < kNB; ++b) {
+      const UpdIonT<float> &B = T.bal[b];
+      heat += a.mom[(size_t)(1 + kNB + b) * a.mstride + c] * XS(w, B.e * kNX + B.ion, c) * T.ab[B.e];
+    }
+    const float cool = coolFF + coolRec + coolColl;
+    const float res = heat - cool;
+    float Thigh = w.sec[0 * nc1 + c], Tlow = w.sec[1 * nc1 + c];
+    float resHigh = w.sec[2 * nc1 + c], resLow = w.sec[3 * nc1 + c], fstep = w.sec[4 * nc1 + c];
+    const int nIterT = ++w.nit[c];
+    bool again = false, noTe = false;
+    if (fabsf(res) >= 0.01f * heat) {
+      if (nIterT < 25) {
+        bool open = false;
+        if (res < 0.f) {
+          resLow = res;
+          Tlow = Te;
+          if (Thigh != 0.f) Te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+          else { Te = Te / fstep; open = true; }
+        } else {
+          resHigh = res;
+          Thigh = Te;
+          if (Tlow != 0.f) Te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
+          else { Te = Te * fstep; open = true; }
+        }
+        if (open && a.step_grow) fstep = fstep - 1.f < 0.1f ? 1.f + 2.f * (fstep - 1.f) : 1.2f;
+        if (nIterT >= 6 && fabsf(Thigh - Tlow) <= 0.002f * (Thigh + Tlow)) {
+          if (res < 0.f) { Te = Thigh - 100.f; Thigh = 0.f; }
+          else { Te = Tlow + 100.f; Tlow = 0.f; }
+        }
+        if (Te <= 0.f) Te = 1.f;
+        again = true;
+      } else {
+        if (Thigh == 0.f) Te = Tlow;
+        else if (Tlow == 0.f) Te = Thigh;
+        else Te = (Thigh + Tlow) * 0.5f;
+        noTe = true;
+      }
+    }
+    if (again) {
+      w.Te[c] = Te;
+      w.sec[0 * nc1 + c] = Thigh; w.sec[1 * nc1 + c] = Tlow;
+      w.sec[2 * nc1 + c] = resHigh; w.sec[3 * nc1 + c] = resLow; w.sec[4 * nc1 + c] = fstep;
+      w.act[cur ^ 1][atomicAdd(&w.count[cur ^ 1], 1)] = c;
+      continue;
+    }
+    // done: the state goes back to the cell arrays (which still hold the
+    // state the update started from: the convergence test compares with it)
+    double *Xc = a.X + (size_t)c * kX;
+    const double te0 = a.te_prev ? a.te_prev[c] : a.te[c];
+    const double x0 = a.xh0_prev ? a.xh0_prev[c] : Xc[1];
+    for (int e = 0; e < kNE; ++e)
+      for (int s = 1; s < kNX; ++s) Xc[e * kNX + s] = (double)XS(w, e * kNX + s, c);
+    a.te[c] = (double)Te;
+    a.ne[c] = (double)Ne;
+    const double xh = (double)xH1;
+    a.conv[c] = fabs((xh - x0) / x0) <= a.xhi ? 1 : 0;
+    a.niter[c] = nIterT;
+    a.flags[c] = (noTe ? 1 : 0) | (w.flags[c] & 2);
+    a.dte[c] = fabs((double)Te - te0) / te0;
+  }
+}
+
+__global__ void wave_reset_kernel(int *count, int slot) { count[slot] = 0; }
+
+}  // namespace
+
+size_t cell_update_fp32_scratch(int nc, int ncel) {
+  const size_t nc1 = (size_t)nc + 1;
+  // the arrays of launch_cell_update_fp32, each rounded up to 256 bytes
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  return r(nc1 * kX * 4) + 2 * r(nc1 * 4) + r(nc1 * 5 * 4) + r(nc1 * (size_t)ncel * 4) + 4 * r(nc1 * 4) + r(8);
+}
+
+cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream) {
+  const size_t nc1 = (size_t)a.nc + 1;
+  WaveArgs w{};
+  w.a = a;
+  char *p = (char *)scratch;
+  auto take = [&](size_t bytes) { char *q = p; p += (bytes + 255) / 256 * 256; return q; };
+  w.Xs = (float *)take(nc1 * kX * sizeof(float));
+  w.Te = (float *)take(nc1 * sizeof(float));
+  w.Ne = (float *)take(nc1 * sizeof(float));
+  w.sec = (float *)take(nc1 * 5 * sizeof(float));
+  w.cool = (float *)take(nc1 * (size_t)a.ncel * sizeof(float));
+  w.nit = (int *)take(nc1 * sizeof(int));
+  w.flags = (int *)take(nc1 * sizeof(int));
+  w.act[0] = (int *)take(nc1 * sizeof(int));
+  w.act[1] = (int *)take(nc1 * sizeof(int));
+  w.count = (int *)take(2 * sizeof(int));
+  cudaError_t e = cudaMemsetAsync(w.count, 0, 2 * sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  cell_update_kernel<float, true><<<blocks, kW * 32, smem, stream>>>(a);
+  const int blocks = num_sms * 8;
+  wave_init_kernel<<<blocks, 256, 0, stream>>>(w);
+  for (int t = 0; t < 25; ++t) {
+    const int cur = t & 1;
+    wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
+    wave_ion_kernel<<<blocks, 128, 0, stream>>>(w, cur);
+    wave_cel_kernel<<<blocks * 4, 128, 0, stream>>>(w, cur);
+    wave_therm_kernel<<<blocks, 128, 0, stream>>>(w, cur);
+  }
   return cudaGetLastError();
 }
 

@@ -88,8 +88,9 @@ struct UpdArgs {
   double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
   int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
 };
-cudaError_t launch_cell_update(const UpdArgs &a, int fp32, int num_sms, cudaStream_t stream);
-cudaError_t launch_cell_update_fp32(const UpdArgs &a, int blocks, cudaStream_t stream);
+cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int num_sms, cudaStream_t stream);
+cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream);
+size_t cell_update_fp32_scratch(int nc, int ncel);
 cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const int *flags, const double *dte,
                                 UpdStatsDev *s, int num_sms, cudaStream_t stream);
 cudaError_t launch_species(int nc, int nsp, const int *sp_e, const int *sp_s, const double *X, const double *ab,

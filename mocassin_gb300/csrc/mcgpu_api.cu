@@ -118,7 +118,7 @@ struct mc_ctx {
   // cell update: atomic tables, per-cell state and scratch
   DBuf u_bal, u_cel, u_rrec, u_rnew, u_direc, u_aldro, u_logt, u_g, u_e, u_A, u_qq, u_q2, u_ab, u_hden;
   DBuf f_bal, f_cel, f_rrec, f_rnew, f_direc, f_aldro, f_logt, f_g, f_e, f_A, f_qq, f_q2, f_ab;  // float copies
-  DBuf s_te, s_ne, s_X, s_conv, s_niter, s_flags, s_dte, s_mom, s_w, s_ustats, s_err, s_den, s_xs, s_spe, s_sps;
+  DBuf s_te, s_ne, s_X, s_conv, s_niter, s_flags, s_dte, s_mom, s_w, s_ustats, s_err, s_den, s_xs, s_spe, s_sps, s_wave;
   int u_ncel = 0, u_ndirec = 0, u_naldro = 0, u_maxlev = 1;
   int u_bal_z[7] = {}, u_bal_first[7] = {};
   // learned warm start: parameters, Adam state, training buffer, work arrays
@@ -1165,7 +1165,12 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   a.xhi = xhi_limit;
   a.mat_rows = c->u_maxlev;
   a.mat_stride = (c->u_maxlev * c->u_maxlev) | 1;
-  e = mcg::launch_cell_update(a, precision == MC_PREC_FP32, c->num_sms, s);
+  if (precision == MC_PREC_FP32) {
+    const size_t need = mcg::cell_update_fp32_scratch(c->nc, c->u_ncel);
+    mc_status ss = c->s_wave.bytes == need ? MC_OK : put_buf(c->s_wave, nullptr, need, s);
+    if (ss) return ss;
+  }
+  e = mcg::launch_cell_update(a, precision == MC_PREC_FP32, c->s_wave.p, c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "cell update launch failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(e2, s));
   e = mcg::launch_update_stats(c->nc, a.conv, a.niter, a.flags, a.dte, c->s_ustats.as<mcg::UpdStatsDev>(),
