@@ -1385,7 +1385,8 @@ extern "C" mc_status mc_ctx_surrogate_collect(mc_ctx_t *c, int64_t *rows) {
   MC_CUDA(cudaMemcpyAsync(&n, c->m_count.p, 8, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
   c->m_n = (long long)n;
-  c->m_norm = false;
+  // the normalisation is fixed by the first training: the network's
+  // weights depend on it, so later rows are scaled the same way
   if (rows) *rows = std::min((long long)n, c->m_cap);
   return MC_OK;
 }

@@ -104,3 +104,15 @@ def test_trained_warm_start_saves_temperature_steps(gpu_lib):
     d = np.abs(te_w[c] / te_c[c] - 1)
     assert np.median(d) < 0.02, (np.median(d), gain)
     print("warm start", gain)
+
+
+@pytest.mark.gpu
+def test_lambda_iteration_with_surrogate_keeps_warm_starting(gpu_lib):
+    from mocassin_gb300 import iterate
+    neb = _clumpy(n=21, packets=500_000)
+    li = iterate.LambdaIteration(neb, form="wave", update="fp32",
+                                 surrogate={"train_after": 2, "steps": 200, "batch": 2048})
+    _, hist = li.run(seed=7, max_iterations=5, min_convergence=101.0)
+    li.close()
+    assert [h["warm"] for h in hist] == [False, False, True, True, True]
+    assert hist[1]["surrogate_train_ms"] > 0
