@@ -217,6 +217,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-opacity", action="store_true")
     ap.add_argument("--lambda-max", type=int, default=12, help="Lambda iterations at most per form (0: skip)")
+    ap.add_argument("--lambda-only", default="", choices=["", "chosen", "plain"],
+                    help="run only the Lambda iteration of one form and print its record (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -239,6 +241,15 @@ def main():
         spec.n = args.grid
     neb = nebula.build(spec)
     npk = sum(neb.n_packets)
+    if args.lambda_only:
+        from mocassin_gb300 import iterate
+        form, upd = ("wave", "fp32") if args.lambda_only == "chosen" else ("plain", "fp64")
+        li = iterate.LambdaIteration(neb, form=form, update=upd)
+        wall, hist = li.run(seed=1000, max_iterations=max(args.lambda_max, 1))
+        li.close()
+        print(json.dumps({"lambda_only": args.lambda_only, "workload": neb.spec.name, "wall_s": wall,
+                          "iterations": hist}))
+        return 0
 
     ctx = transport.TransportContext(neb)
     for w in range(args.warmup):

@@ -162,9 +162,15 @@ cudaError_t launch_jmoments(int nc1, int nb, int nout, const double *J, const fl
   const size_t sh = (size_t)2 * kJM * kJK * 2 + (size_t)2 * a.N * kJK * 2 + 64;
   cudaError_t e = cudaFuncSetAttribute(jmoment_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jmoment_tc_kernel, 128, sh);
+  // the whole carveout as shared memory, so several CTAs (each holding at
+  // most 128 of the SM's 512 TMEM columns) share an SM and overlap their
+  // Jste streams with each other's MMAs
+  e = cudaFuncSetAttribute(jmoment_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
+  // CTAs per SM from the shared-memory (227 KB) and TMEM (512 columns) budgets
+  const int ncols = a.N <= 32 ? 32 : (a.N <= 64 ? 64 : 128);
+  int per_sm = (int)((227 * 1024) / (sh + 1024));
+  if (per_sm > 512 / ncols) per_sm = 512 / ncols;
   if (per_sm > 4) per_sm = 4;
   if (per_sm < 1) per_sm = 1;
   const int ntiles = (nc1 + kJM - 1) / kJM;

@@ -247,10 +247,12 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
   if (e != cudaSuccess) return e;
   const int nvt = (nb + kOpN - 1) / kOpN;
   const int ntiles = (nc1 + kOpM - 1) / kOpM;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, opacity_tc_kernel, 128, sh);
+  e = cudaFuncSetAttribute(opacity_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
-  int want_sm = 2;  // CTAs per SM (at most 4: 4 x 128 TMEM columns = 512)
+  // CTAs per SM from the shared-memory budget (227 KB), at most 4 (4 x 128
+  // TMEM columns = 512)
+  int per_sm = (int)((227 * 1024) / (sh + 1024));
+  int want_sm = 4;
   if (const char *e2 = getenv("MC_OPAC_CTAS_PER_SM")) want_sm = atoi(e2);
   if (per_sm > want_sm) per_sm = want_sm;
   if (per_sm > 4) per_sm = 4;
