@@ -344,6 +344,14 @@ mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
 mc_status mc_ctx_surrogate_grads(mc_ctx_t *ctx, int32_t m, const float *x, const float *t, double *loss, float *grads,
                                  float *y);
 
+/* Scheduling parameters of the persistent march (results do not depend on
+ * them beyond the order of the FP64 sums): refill_min = free lanes a warp
+ * collects before it takes new packets from the queue (1..32, default 8);
+ * inner_steps = cell crossings a lane takes between refill checks (1..64,
+ * default 4).  mocassin_gb300/autotune.py picks them by timing. */
+mc_status mc_ctx_set_tuning(mc_ctx_t *ctx, int32_t refill_min, int32_t inner_steps);
+mc_status mc_ctx_get_tuning(mc_ctx_t *ctx, int32_t *refill_min, int32_t *inner_steps);
+
 /* Copies the resident opacity [nbins][Nc+1] (cell fastest) to the host. */
 mc_status mc_ctx_get_opacity(mc_ctx_t *ctx, float *opacity);
 

@@ -1483,6 +1483,22 @@ extern "C" mc_status mc_ctx_surrogate_grads(mc_ctx_t *c, int32_t m, const float 
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_set_tuning(mc_ctx_t *c, int32_t refill_min, int32_t inner_steps) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  if (refill_min < 1 || refill_min > 32 || inner_steps < 1 || inner_steps > 64)
+    return set_error(MC_ERR_ARG, "refill_min must be 1..32 and inner_steps 1..64");
+  c->refill_min = refill_min;
+  c->inner_steps = inner_steps;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_get_tuning(mc_ctx_t *c, int32_t *refill_min, int32_t *inner_steps) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  if (refill_min) *refill_min = c->refill_min;
+  if (inner_steps) *inner_steps = c->inner_steps;
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_get_opacity(mc_ctx_t *c, float *out) {
   if (!c || !out) return set_error(MC_ERR_ARG, "ctx and opacity are required");
   MC_CUDA(cudaMemcpyAsync(out, c->opacity.p, (size_t)(c->nc + 1) * c->nb * sizeof(float), cudaMemcpyDeviceToHost,

@@ -85,6 +85,10 @@ def library():
         lib.mc_ctx_surrogate_params.argtypes = [C.c_void_p, fp, fp]
         lib.mc_ctx_surrogate_grads.restype = C.c_int
         lib.mc_ctx_surrogate_grads.argtypes = [C.c_void_p, C.c_int32, fp, fp, dp, fp, fp]
+        lib.mc_ctx_set_tuning.restype = C.c_int
+        lib.mc_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        lib.mc_ctx_get_tuning.restype = C.c_int
+        lib.mc_ctx_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         lib.mc_ctx_get_opacity.restype = C.c_int
         lib.mc_ctx_get_opacity.argtypes = [C.c_void_p, fp]
         lib.mc_ctx_destroy.restype = None
@@ -307,6 +311,14 @@ class TransportContext:
         loss = C.c_double()
         _check(self.lib.mc_ctx_surrogate_grads(self.handle, m, _fptr(x), _fptr(t), C.byref(loss), _fptr(g), _fptr(y)))
         return loss.value, g, y
+
+    def set_tuning(self, refill_min, inner_steps):
+        _check(self.lib.mc_ctx_set_tuning(self.handle, int(refill_min), int(inner_steps)))
+
+    def get_tuning(self):
+        r, i = C.c_int32(), C.c_int32()
+        _check(self.lib.mc_ctx_get_tuning(self.handle, C.byref(r), C.byref(i)))
+        return r.value, i.value
 
     def get_opacity(self):
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
