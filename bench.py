@@ -200,6 +200,23 @@ def converged_model(neb, args):
     return out
 
 
+def batched_models(args):
+    """The 64-model batch (grid sizes 17^3-65^3, 30-100 kK stars, log nH
+    1-4, outer radius 1e18-1e19 cm, 33 packets per cell: 2e8 over the 64)
+    served by the request loop of mocassin_gb300.serve: the first
+    ``--batch-models`` of them, 3 Lambda iterations each, admitted by device
+    memory, ``--batch-workers`` models resident at a time."""
+    from mocassin_gb300 import nebula, serve
+    specs = nebula.batch64()[: args.batch_models]
+    srv = serve.ModelServer(memory_budget=200e9, workers=args.batch_workers, iterations=3,
+                            autotune_packets=200_000)
+    for sp in specs:
+        srv.submit(sp)
+    rep = srv.run()
+    rep["batch"] = "%d of the 64-model batch (seed 1)" % len(specs)
+    return rep
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -217,6 +234,9 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-opacity", action="store_true")
     ap.add_argument("--lambda-max", type=int, default=12, help="Lambda iterations at most per form (0: skip)")
+    ap.add_argument("--batch-models", type=int, default=16,
+                    help="batched serving: models of the 64-model batch to serve (0: skip)")
+    ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--lambda-only", default="", choices=["", "chosen", "plain"],
                     help="run only the Lambda iteration of one form and print its record (profiling)")
     args = ap.parse_args()
@@ -412,6 +432,8 @@ def main():
         line["jste_moments"] = moments
     if args.lambda_max > 0 and rank == 0:
         line["converged_model"] = converged_model(neb, args)
+    if args.batch_models > 0 and rank == 0:
+        line["batched_models"] = batched_models(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(neb)
     if rank == 0:

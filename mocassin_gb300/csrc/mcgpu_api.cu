@@ -128,6 +128,10 @@ struct mc_ctx {
   int m_step = 0, m_B = 0;
   bool m_ready = false, m_norm = false;
   bool u_ready = false, s_ready = false;
+  // the FP32 update's launch sequence, captured once per argument set
+  cudaGraphExec_t wave_exec = nullptr;
+  mcg::UpdArgs wave_args{};
+  void *wave_scratch = nullptr;
   DBuf counters, src_cdf, replay;
   // chosen form: march-indexed views and the sorted packet queue
   int identity = 1;
@@ -754,6 +758,7 @@ void mc_ctx_destroy(mc_ctx_t *c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->evm0) cudaEventDestroy(c->evm0);
   if (c->evm1) cudaEventDestroy(c->evm1);
+  if (c->wave_exec) cudaGraphExecDestroy(c->wave_exec);
   cudaStream_t s = c->stream;
   delete c;  // frees the device buffers
   if (s) cudaStreamDestroy(s);
@@ -1170,7 +1175,31 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
     mc_status ss = c->s_wave.bytes == need ? MC_OK : put_buf(c->s_wave, nullptr, need, s);
     if (ss) return ss;
   }
-  e = mcg::launch_cell_update(a, precision == MC_PREC_FP32, c->s_wave.p, c->num_sms, s);
+  if (precision == MC_PREC_FP32) {
+    // the 101 launches of the T-step wavefronts replay as one graph; it is
+    // captured again only when the arguments (state, tables, warm start) change
+    const bool same = c->wave_exec && c->wave_scratch == c->s_wave.p &&
+                      std::memcmp(&c->wave_args, &a, sizeof a) == 0;
+    if (!same) {
+      if (c->wave_exec) { cudaGraphExecDestroy(c->wave_exec); c->wave_exec = nullptr; }
+      cudaGraph_t graph = nullptr;
+      MC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = mcg::launch_cell_update(a, 1, c->s_wave.p, c->num_sms, s);
+      cudaError_t ee = cudaStreamEndCapture(s, &graph);
+      if (ce == cudaSuccess) ce = ee;
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&c->wave_exec, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        c->wave_exec = nullptr;
+        return set_error(MC_ERR_CUDA, "cell update capture failed: %s", cudaGetErrorString(ce));
+      }
+      c->wave_args = a;
+      c->wave_scratch = c->s_wave.p;
+    }
+    e = cudaGraphLaunch(c->wave_exec, s);
+  } else {
+    e = mcg::launch_cell_update(a, 0, c->s_wave.p, c->num_sms, s);
+  }
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "cell update launch failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(e2, s));
   e = mcg::launch_update_stats(c->nc, a.conv, a.niter, a.flags, a.dte, c->s_ustats.as<mcg::UpdStatsDev>(),

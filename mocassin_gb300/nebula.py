@@ -420,6 +420,28 @@ def twostar101(n_packets: int = 100_000_000) -> NebulaSpec:
                       nh_median=1000.0, sigma_ln=1.0, smooth_cells=3.0, seed=1)
 
 
+def batch64(n_models: int = 64, seed: int = 1, packets_total: int = 200_000_000, n_min: int = 17,
+            n_max: int = 65) -> List[NebulaSpec]:
+    """Independent nebulae for batched serving: grid sizes odd and uniform in
+    n_min..n_max, star temperatures uniform in 30-100 kK, log nH uniform in
+    [1, 4], outer radius uniform in 1e18-1e19 cm (the grid spans +/- the
+    outer radius), the abundances of the other workloads, packets in
+    proportion to the cell count (packets_total over all models)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.choice(np.arange(n_min, n_max + 1, 2), n_models)
+    tstar = rng.uniform(30000.0, 100000.0, n_models)
+    lognh = rng.uniform(1.0, 4.0, n_models)
+    rout = rng.uniform(1.0e18, 1.0e19, n_models)
+    cells = ns.astype(np.float64) ** 3 * (np.pi / 6.0)   # the sphere inside the cube
+    npk = np.maximum((packets_total * cells / cells.sum()).astype(np.int64), 1000)
+    specs = []
+    for i in range(n_models):
+        specs.append(NebulaSpec("batch%02d_n%d" % (i, ns[i]), int(ns[i]), float(rout[i]), False,
+                                [Star(float(tstar[i]), 10.0, (0, 0, 0), int(npk[i]))],
+                                nh_median=float(10.0 ** lognh[i]), r_out=float(rout[i]), r_in=0.0))
+    return specs
+
+
 def small_cases():
     """Small grids the oracle finishes in seconds: every branch of the march."""
     return [

@@ -1,0 +1,141 @@
+"""Batched models served on one GPU: a request loop that admits nebulae by
+device memory and runs their Lambda iterations concurrently.
+
+Each request is a nebula (NebulaSpec) and a number of Lambda iterations
+(transport, cell update, opacity rebuild; mocassin_gb300.iterate).  A pool
+of worker threads takes requests in order; a worker builds the nebula on the
+host, waits until the model's device footprint fits in the memory budget
+next to the models already resident, creates its context (own CUDA stream),
+picks the march's scheduling parameters (autotuned once per grid size and
+reused), runs the iterations, and frees the device memory.  The C-ABI calls
+release the Python interpreter lock, so the models' kernels run concurrently
+on their streams and the host-side builds overlap with the GPU work.
+
+Reported: wall time, aggregate cell crossings per second, the p50 / p99 of
+the per-iteration latency, the peak number of resident models and bytes.
+"""
+import threading
+import time
+
+import numpy as np
+
+from . import autotune, iterate, nebula
+
+
+def device_bytes(neb):
+    """Device footprint of a resident model: opacity (4 B), recPDF as given
+    and re-laid out (8 B), Jste (8 B), escapedPackets (8 B), the moments of
+    the cell update (67 x 4 B per cell), the cell state and scratch, the
+    per-packet queues (~120 B per packet)."""
+    nc1, nb = neb.ncells + 1, neb.nbins
+    per_cell_bin = 4 + 8 + 8 + 8
+    per_cell = 67 * 4 + 56 * 8 * 2 + 56 * 4 + 26 * 4 + 200
+    return int(nc1 * nb * per_cell_bin + nc1 * per_cell + sum(neb.n_packets) * 120 + (64 << 20))
+
+
+class ModelServer:
+    def __init__(self, memory_budget=200e9, workers=4, iterations=3, form="wave", update="fp32",
+                 autotune_packets=0):
+        self.budget = float(memory_budget)
+        self.workers = int(workers)
+        self.iterations = int(iterations)
+        self.form, self.update = form, update
+        self.autotune_packets = int(autotune_packets)
+        self.requests = []
+        self._lock = threading.Condition()
+        self._resident = 0
+        self._resident_models = 0
+        self.peak_bytes = 0
+        self.peak_models = 0
+        self.tuning = {}
+        self.results = []
+        self.errors = []
+
+    def submit(self, spec, iterations=None):
+        self.requests.append((spec, self.iterations if iterations is None else int(iterations)))
+
+    def _admit(self, nbytes):
+        with self._lock:
+            while self._resident > 0 and self._resident + nbytes > self.budget:
+                self._lock.wait()
+            self._resident += nbytes
+            self._resident_models += 1
+            self.peak_bytes = max(self.peak_bytes, self._resident)
+            self.peak_models = max(self.peak_models, self._resident_models)
+
+    def _release(self, nbytes):
+        with self._lock:
+            self._resident -= nbytes
+            self._resident_models -= 1
+            self._lock.notify_all()
+
+    def _serve_one(self, spec, iters):
+        t_req = time.perf_counter()
+        neb = nebula.build(spec)
+        nbytes = device_bytes(neb)
+        self._admit(nbytes)
+        try:
+            li = iterate.LambdaIteration(neb, form=self.form, update=self.update)
+            key = neb.nx
+            with self._lock:
+                tuned = self.tuning.get(key)
+            if tuned is None and self.autotune_packets > 0:
+                tuned, _ = autotune.autotune(li.ctx, min(self.autotune_packets, sum(neb.n_packets)), repeats=1,
+                                             candidates=((4, 4), (8, 4), (8, 8), (8, 16), (16, 8)))
+                with self._lock:
+                    self.tuning[key] = tuned
+            if tuned is not None:
+                li.ctx.set_tuning(*tuned)
+            t0 = time.perf_counter()
+            lat = []
+            cross = 0
+            for it in range(iters):
+                rec = li.step(seed=1000 + it)
+                lat.append(rec["wall_s"])
+                cross += rec["crossings"]
+            t1 = time.perf_counter()
+            li.close()
+            self.results.append({"model": spec.name, "cells": neb.ncells, "packets": int(sum(neb.n_packets)),
+                                 "iterations": iters, "latency_s": lat, "crossings": cross,
+                                 "converged_pct": rec["converged_pct"], "run_s": t1 - t0,
+                                 "queue_s": t0 - t_req, "bytes": nbytes})
+        finally:
+            self._release(nbytes)
+
+    def run(self):
+        """Serves every submitted request; returns the report."""
+        todo = list(self.requests)
+        idx = [0]
+        lock = threading.Lock()
+
+        def worker():
+            while True:
+                with lock:
+                    if idx[0] >= len(todo):
+                        return
+                    spec, iters = todo[idx[0]]
+                    idx[0] += 1
+                try:
+                    self._serve_one(spec, iters)
+                except Exception as exc:  # reported, the other models go on
+                    self.errors.append("%s: %s" % (spec.name, exc))
+
+        t0 = time.perf_counter()
+        threads = [threading.Thread(target=worker) for _ in range(self.workers)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        wall = time.perf_counter() - t0
+        lat = np.array([x for r in self.results for x in r["latency_s"]]) * 1e3
+        cross = sum(r["crossings"] for r in self.results)
+        return {"models": len(self.results), "errors": self.errors, "wall_s": wall,
+                "cells": int(sum(r["cells"] for r in self.results)),
+                "packets_per_iteration": int(sum(r["packets"] for r in self.results)),
+                "iterations": int(sum(r["iterations"] for r in self.results)),
+                "crossings_per_s": cross / wall if wall > 0 else 0.0,
+                "latency_ms_p50": float(np.percentile(lat, 50)) if len(lat) else None,
+                "latency_ms_p99": float(np.percentile(lat, 99)) if len(lat) else None,
+                "peak_resident_models": self.peak_models, "peak_resident_bytes": self.peak_bytes,
+                "workers": self.workers, "memory_budget_bytes": self.budget,
+                "tuning": {str(k): list(v) for k, v in self.tuning.items()}}
