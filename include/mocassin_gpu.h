@@ -253,6 +253,17 @@ mc_status mc_ctx_build_opacity(mc_ctx_t *ctx, int32_t nspecies, const float *den
 mc_status mc_ctx_jste_moments(mc_ctx_t *ctx, int32_t nout, const float *w, double scale, float *out,
                               double *kernel_ms);
 
+/* Grain temperatures of getDustT (source/update_mod.f90:1836-1945) on the
+ * resident Jste: per size bin k the absorbed integral sum_nu Jste w_abs(nu, k)
+ * (w_abs = xSecAbs / pi, host [nbins][nsizes]; scale = the Jste normalisation)
+ * located in the emission table em_table [nsizes][ntemps] (T = 1..ntemps K,
+ * dust_mod.f90:150-178) as locate does, with a linear step.  tdust: host
+ * [nsizes+1][Nc+1]; row 0 = sum_k grain_weight(k) Tdust(k) (Tdust(nS,0) of the
+ * reference for one species); cells no packet reached get 0. */
+mc_status mc_ctx_dust_temperatures(mc_ctx_t *ctx, int32_t nsizes, const float *w_abs, const float *em_table,
+                                   int32_t ntemps, const float *grain_weight, double scale, float *tdust,
+                                   double *kernel_ms);
+
 /* ---- the cell update (ionisation and thermal balance) ----------------------
  * updateCell (source/update_mod.f90:15-525) for every active cell of the
  * context, in FP64 on the GPU, after a transport: one warp per cell runs the

@@ -153,6 +153,52 @@ __global__ void __launch_bounds__(128, 4) jmoment_tc_kernel(const __grid_constan
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
+// Grain temperatures of getDustT (update_mod.f90:1899-1925): per cell and
+// size bin, the absorbed integral A (a moment of Jste) located in the
+// emission table E(T), T = 1..nt K, with locate's rules (interpolation_mod
+// locate: nt above the table, 0 below it, else the last entry <= A, and 1
+// when no entry exceeds A), then T = i + (A - E(i)) / (E(i+1) - E(i));
+// below the table T = 1, above it T = nt.  Row 0 of tdust is the
+// weighted mean over sizes; cells no packet reached get 0.
+__global__ void dust_temperature_kernel(int nc1, int nsizes, int nt, const float *A, const float *E,
+                                        const float *gw, const float *hit, float *tdust) {
+  for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c < nc1; c += gridDim.x * blockDim.x) {
+    const bool reached = hit[c] > 0.f;
+    float mean = 0.f;
+    for (int k = 0; k < nsizes; ++k) {
+      const float x = A[(size_t)k * nc1 + c];
+      const float *e = E + (size_t)k * nt;
+      float t = 0.f;
+      if (reached) {
+        int ns;
+        if (x > e[nt - 1]) ns = nt;
+        else if (x < e[0]) ns = 0;
+        else {
+          int lo = 0, hi = nt;  // first index with e > x (0-based), nt if none
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (e[mid] > x) hi = mid;
+            else lo = mid + 1;
+          }
+          ns = lo == nt ? 1 : (lo > 1 ? lo : 1);  // 1-based: the entry before the first larger one
+        }
+        if (ns <= 0) t = 1.f;
+        else if (ns >= nt) t = (float)nt;
+        else t = (float)ns + (x - e[ns - 1]) * ((float)(ns + 1) - (float)ns) / (e[ns] - e[ns - 1]);
+      }
+      tdust[(size_t)(1 + k) * nc1 + c] = t;
+      mean += t * gw[k];
+    }
+    tdust[c] = mean;
+  }
+}
+
+cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
+                                    const float *hit, float *tdust, int num_sms, cudaStream_t stream) {
+  dust_temperature_kernel<<<num_sms * 4, 256, 0, stream>>>(nc1, nsizes, nt, A, E, gw, hit, tdust);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_jmoments(int nc1, int nb, int nout, const double *J, const float *W, double scale, float *out,
                             int *error, int num_sms, cudaStream_t stream) {
   JMomentArgs a{};

@@ -126,6 +126,9 @@ cudaError_t launch_mlp_infer_features(int nc, const float *mom, long long ms, co
 cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const float *tmean, const float *tstd, double *te,
                              double *X, double *te_prev, double *xh0_prev, int num_sms, cudaStream_t s);
 
+cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
+                                    const float *hit, float *tdust, int num_sms, cudaStream_t stream);
+
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);
 

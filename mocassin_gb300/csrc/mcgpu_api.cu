@@ -851,6 +851,51 @@ extern "C" mc_status mc_ctx_jste_moments(mc_ctx_t *c, int32_t nout, const float 
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const float *w_abs,
+                                              const float *em_table, int32_t ntemps, const float *grain_weight,
+                                              double scale, float *tdust, double *kernel_ms) {
+  if (!c || !w_abs || !em_table || !grain_weight || !tdust)
+    return set_error(MC_ERR_ARG, "ctx, w_abs, em_table, grain_weight and tdust are required");
+  if (nsizes < 1 || nsizes > 127) return set_error(MC_ERR_ARG, "nsizes must be 1..127 (got %d)", nsizes);
+  if (ntemps < 2) return set_error(MC_ERR_ARG, "ntemps must be >= 2");
+  const int nc1 = c->nc + 1, nb = c->nb, nout = nsizes + 1;
+  // column 0 = 1: the hit test of updateCell (any Jste > 0)
+  std::vector<float> w((size_t)nb * nout);
+  for (int i = 0; i < nb; ++i) {
+    w[(size_t)i * nout] = 1.f;
+    for (int k = 0; k < nsizes; ++k) w[(size_t)i * nout + 1 + k] = w_abs[(size_t)i * nsizes + k];
+  }
+  DBuf dw, dm, de, dg, dt, err;
+  MC_CUDA(dw.alloc(w.size() * sizeof(float)));
+  MC_CUDA(dm.alloc((size_t)nout * nc1 * sizeof(float)));
+  MC_CUDA(de.alloc((size_t)nsizes * ntemps * sizeof(float)));
+  MC_CUDA(dg.alloc((size_t)nsizes * sizeof(float)));
+  MC_CUDA(dt.alloc((size_t)nout * nc1 * sizeof(float)));
+  MC_CUDA(err.alloc(sizeof(int)));
+  cudaStream_t s = c->stream;
+  MC_CUDA(cudaMemcpyAsync(dw.p, w.data(), dw.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(de.p, em_table, de.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync(dg.p, grain_weight, dg.bytes, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  MC_CUDA(cudaEventRecord(c->evm0, s));
+  cudaError_t e = mcg::launch_jmoments(nc1, nb, nout, c->jste.as<double>(), dw.as<float>(), scale, dm.as<float>(),
+                                       err.as<int>(), c->num_sms, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_dust_temperature(nc1, nsizes, ntemps, dm.as<float>() + nc1, de.as<float>(), dg.as<float>(),
+                                     dm.as<float>(), dt.as<float>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "dust temperature launch failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(c->evm1, s));
+  int herr = 0;
+  MC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaMemcpyAsync(tdust, dt.p, dt.bytes, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->evm0, c->evm1);
+  if (kernel_ms) *kernel_ms = ms;
+  if (herr) return set_error((mc_status)herr, "moment kernel: tensor-core wait timed out");
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_build_opacity(mc_ctx_t *c, int32_t nspecies, const float *den, const float *xs,
                                           const float *ff, int32_t method, int32_t sca, double *kernel_ms) {
   if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");

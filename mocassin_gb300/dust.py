@@ -1,0 +1,64 @@
+"""Host side of the grain temperatures (getDustT, source/update_mod.f90:1836-1945).
+
+The grains of the dusty workloads are one silicate-like species in 10 MRN
+size bins (mocassin_gb300.nebula._dust_kappa).  Per size bin a the
+reference forms, for every cell,
+    absorbed(a) = sum_i xSecAbs(a, i) Jste(i) / pi             (:1858-1866)
+on the normalised Jste, and finds the temperature whose emission
+    dustEmIntegral(a, T) = 4 h sum_i xSecAbs(a, i) B(nu_i, T) fr1Ryd widFlx(i),
+    T = 1 .. 3000 K                                             (dust_mod.f90:150-178)
+equals it, by `locate` and a linear step (:1899-1915).  The absorbed
+integrals are moments of Jste (the tensor-core moment kernel); this module
+builds their weights and the emission table.
+"""
+import numpy as np
+
+from . import nebula
+
+NTEMPS = 3000                      # constants_mod.f90:55
+HPLANCK = 6.6262e-27               # constants_mod.f90:14
+FR1RYD = 3.28984e15                # constants_mod.f90:13
+HCRYD_K = 157893.94                # continuum_mod.f90:10
+
+
+def grains(nu):
+    """(xs_abs [nsizes, nbins] cm^2 per grain, number weights [nsizes], radii [nsizes] cm)."""
+    a = np.logspace(np.log10(0.005e-4), np.log10(0.25e-4), 10)
+    w = a ** -3.5 * np.gradient(a)
+    w = w / w.sum()
+    lam = 2.9979250e10 / (nu.astype(np.float64) * FR1RYD)
+    x = 2.0 * np.pi * a[:, None] / lam[None, :]
+    qa = 1.0 - np.exp(-0.5 * x)
+    return np.pi * a[:, None] ** 2 * qa, w, a
+
+
+def planck_over_h(energy, t):
+    """getFlux(energy [Ryd], T, 'blackbody') (continuum_mod.f90:359-394), FP64."""
+    constant = 0.5250229 / HPLANCK
+    e = np.asarray(energy, dtype=np.float64)
+    u = HCRYD_K * e / t
+    out = np.empty_like(u)
+    big = u > 86.0
+    out[big] = constant * e[big] ** 3 * np.exp(-u[big])
+    den = np.expm1(u[~big])
+    small = den <= 0
+    val = constant * e[~big] ** 3 / np.where(small, 1.0, den)
+    val[small] = (3.32154e-6 * e[~big] ** 2 * t / HPLANCK)[small]
+    out[~big] = val
+    return out
+
+
+def emission_table(xs_abs, nu):
+    """dustEmIntegral [nsizes, NTEMPS] for T = 1 .. NTEMPS K."""
+    wf = nebula.wid_flx(nu).astype(np.float64)
+    nu64 = nu.astype(np.float64)
+    tab = np.zeros((xs_abs.shape[0], NTEMPS))
+    for k in range(NTEMPS):
+        b = planck_over_h(nu64, float(k + 1))
+        tab[:, k] = (xs_abs * (b * FR1RYD * wf)[None, :]).sum(1)
+    return tab * HPLANCK * 4.0
+
+
+def absorption_weights(xs_abs):
+    """Moment weights [nbins, nsizes]: xSecAbs / pi."""
+    return np.ascontiguousarray((xs_abs / np.pi).T.astype(np.float32))

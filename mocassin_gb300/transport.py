@@ -89,6 +89,8 @@ def library():
         lib.mc_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.mc_ctx_get_tuning.restype = C.c_int
         lib.mc_ctx_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        lib.mc_ctx_dust_temperatures.restype = C.c_int
+        lib.mc_ctx_dust_temperatures.argtypes = [C.c_void_p, C.c_int32, fp, fp, C.c_int32, fp, C.c_double, fp, dp]
         lib.mc_ctx_get_opacity.restype = C.c_int
         lib.mc_ctx_get_opacity.argtypes = [C.c_void_p, fp]
         lib.mc_ctx_destroy.restype = None
@@ -319,6 +321,19 @@ class TransportContext:
         r, i = C.c_int32(), C.c_int32()
         _check(self.lib.mc_ctx_get_tuning(self.handle, C.byref(r), C.byref(i)))
         return r.value, i.value
+
+    def dust_temperatures(self, w_abs, em_table, grain_weight, scale):
+        """Grain temperatures (getDustT) on the resident Jste: (nsizes+1, Nc+1),
+        row 0 the weighted mean over sizes; and the kernel time."""
+        w_abs = np.ascontiguousarray(w_abs, dtype=np.float32)
+        em = np.ascontiguousarray(em_table, dtype=np.float32)
+        gw = np.ascontiguousarray(grain_weight, dtype=np.float32)
+        nsizes = w_abs.shape[1]
+        out = np.empty((nsizes + 1, self.neb.ncells + 1), dtype=np.float32)
+        ms = C.c_double()
+        _check(self.lib.mc_ctx_dust_temperatures(self.handle, nsizes, _fptr(w_abs), _fptr(em), em.shape[1], _fptr(gw),
+                                                 float(scale), _fptr(out), C.byref(ms)))
+        return out, ms.value
 
     def get_opacity(self):
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
