@@ -77,6 +77,9 @@ typedef enum mc_status {
                                the transport (iteration_mod.f90:458-472)      */
 #define MC_RUN_FORM_PLAIN 2 /* one thread per packet history (the plain form)
                                instead of the frequency-sorted persistent march */
+#define MC_RUN_GRAPH 4      /* the chosen form's rounds inside one CUDA graph (a
+                               WHILE node on the device's absorbed count): no
+                               host round trip per round; march_ms is then 0 */
 
 /* Read-only description of one (mother) grid for one iteration.  All
  * pointers are HOST pointers owned by the caller; they are read during the

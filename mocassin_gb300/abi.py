@@ -16,6 +16,7 @@ MC_RNG_PHILOX = 0
 MC_RNG_REPLAY = 1
 MC_RUN_ZERO_FIRST = 1
 MC_RUN_FORM_PLAIN = 2
+MC_RUN_GRAPH = 4
 
 STATUS_NAMES = {0: "MC_OK", 1: "MC_ERR_ARG", 2: "MC_ERR_CUDA", 3: "MC_ERR_BOUNDS", 4: "MC_ERR_NAN",
                 5: "MC_ERR_REPLAY", 6: "MC_ERR_TIMEOUT", 7: "MC_ERR_UNSUPPORTED", 8: "MC_ERR_NOMEM",

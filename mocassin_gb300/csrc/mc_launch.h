@@ -129,6 +129,8 @@ cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const flo
 cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
                                     const float *hit, float *tdust, int num_sms, cudaStream_t stream);
 
+cudaError_t launch_wave_round_control(const WaveLaunch &L, cudaGraphConditionalHandle h);
+
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);
 

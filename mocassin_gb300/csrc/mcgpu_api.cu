@@ -546,14 +546,13 @@ mc_status wave_buffers(mc_ctx_t *c, size_t n) {
   return MC_OK;
 }
 
-mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S, const mcg::DevReplay &rp,
-                   int precision, float *march_ms, int *rounds_out) {
-  if (S.total > 0xFFFFFFFFll) return set_error(MC_ERR_ARG, "more than 2^32-1 packets in one call");
+mc_status wave_setup(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S, const mcg::DevReplay &rp,
+                     mcg::WaveLaunch &L) {
+  if (S.total >= 0xFFFFFFFFll) return set_error(MC_ERR_ARG, "2^32-1 or more packets in one call");
   if (g.nb > 0xFFFF) return set_error(MC_ERR_UNSUPPORTED, "nbins above 65535");
   if (c->nx > 1023 || c->ny > 1023 || c->nz > 1023) return set_error(MC_ERR_UNSUPPORTED, "grid axes above 1023");
   mc_status st = wave_buffers(c, (size_t)S.total);
   if (st) return st;
-  mcg::WaveLaunch L{};
   L.g = g;
   L.S = S;
   L.rp = rp;
@@ -602,6 +601,118 @@ mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S,
   w.a_words = c->a_words.as<uint32_t>();
   w.a_run = c->a_run.as<uint16_t>();
   w.a_r = c->a_r.p;
+  w.n_round = w.a_count + 1;
+  w.round_ctr = (int *)(w.a_count + 2);
+  return MC_OK;
+}
+
+// The chosen form with every round inside one CUDA graph: round 0 (stellar
+// packets), then a WHILE node whose body is one re-emission round (sample,
+// sort, emit, march) ending in wave_round_control_kernel, which sets the
+// loop condition from the device's own absorbed count.  No host round trip
+// between rounds.  The march is not timed on its own here.
+mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S, const mcg::DevReplay &rp,
+                         int precision, int *rounds_out) {
+  mcg::WaveLaunch L{};
+  mc_status st = wave_setup(c, g, S, rp, L);
+  if (st) return st;
+  const bool f64 = precision == MC_PREC_FP64;
+  cudaStream_t s = c->stream;
+  MC_CUDA(cudaMemsetAsync(L.w.round_ctr, 0, sizeof(int), s));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto fail = [&](cudaError_t e, const char *what) {
+    if (graph) cudaGraphDestroy(graph);
+    return set_error(MC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  };
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  if (e != cudaSuccess) return fail(e, "graph creation failed");
+  cudaGraphConditionalHandle handle;
+  e = cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "conditional handle creation failed");
+  // round 0, then the condition for round 1
+  e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture failed");
+  auto round0 = [&]() -> cudaError_t {
+    cudaError_t r = cudaMemsetAsync(c->bins.p, 0, (size_t)c->nb * 2 * sizeof(unsigned int), s);
+    if (r == cudaSuccess) r = f64 ? mcg::launch_wave_sample_stellar_fp64(L) : mcg::launch_wave_sample_stellar_fp32(L);
+    if (r == cudaSuccess) r = mcg::launch_wave_sort(L, (unsigned int)S.total);
+    if (r == cudaSuccess) r = f64 ? mcg::launch_wave_emit_fp64(L, 0) : mcg::launch_wave_emit_fp32(L, 0);
+    if (r == cudaSuccess) r = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
+    if (r == cudaSuccess) r = mcg::launch_wave_round_control(L, handle);
+    return r;
+  };
+  cudaError_t ce = round0();
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(s, &captured);
+  if (ce != cudaSuccess) return fail(ce, "round 0 capture failed");
+  if (e != cudaSuccess) return fail(e, "round 0 capture failed");
+  // the WHILE node after round 0
+  cudaGraphNode_t last = nullptr;
+  size_t nsink = 0;
+  e = cudaGraphGetNodes(graph, nullptr, &nsink);
+  std::vector<cudaGraphNode_t> nodes(nsink);
+  if (e == cudaSuccess && nsink) e = cudaGraphGetNodes(graph, nodes.data(), &nsink);
+  if (e != cudaSuccess) return fail(e, "graph inspection failed");
+  // the round-control kernel is the one node nothing depends on
+  for (cudaGraphNode_t n : nodes) {
+    size_t nd = 0;
+    cudaGraphNodeGetDependentNodes(n, nullptr, nullptr, &nd);
+    if (nd == 0) last = n;
+  }
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cond = nullptr;
+  e = cudaGraphAddNode(&cond, graph, last ? &last : nullptr, nullptr, last ? 1 : 0, &cp);
+  if (e != cudaSuccess) return fail(e, "conditional node failed");
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "body capture failed");
+  auto round_k = [&]() -> cudaError_t {
+    cudaError_t r = cudaMemsetAsync(c->bins.p, 0, (size_t)c->nb * 2 * sizeof(unsigned int), s);
+    if (r == cudaSuccess)
+      r = f64 ? mcg::launch_wave_sample_reemit_fp64(L, mcg::kDeviceCount)
+              : mcg::launch_wave_sample_reemit_fp32(L, mcg::kDeviceCount);
+    if (r == cudaSuccess) r = mcg::launch_wave_sort(L, mcg::kDeviceCount);
+    if (r == cudaSuccess) r = f64 ? mcg::launch_wave_emit_fp64(L, 1) : mcg::launch_wave_emit_fp32(L, 1);
+    if (r == cudaSuccess) r = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
+    if (r == cudaSuccess) r = mcg::launch_wave_round_control(L, handle);
+    return r;
+  };
+  ce = round_k();
+  cudaGraph_t cbody = nullptr;
+  e = cudaStreamEndCapture(s, &cbody);
+  if (ce != cudaSuccess) return fail(ce, "round capture failed");
+  if (e != cudaSuccess) return fail(e, "round capture failed");
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) return fail(e, "graph instantiation failed");
+  e = cudaGraphLaunch(exec, s);
+  cudaGraphExecDestroy(exec);
+  if (e != cudaSuccess) return fail(e, "graph launch failed");
+  if (!c->identity) {
+    MC_CUDA(mcg::launch_wave_fold(c->jste_m.as<double>(), c->jste.as<double>(), L.w.lin2cell, c->ncell3, c->nc + 1,
+                                  c->nb, s));
+    if (c->jdif_m.p)
+      MC_CUDA(mcg::launch_wave_fold(c->jdif_m.as<double>(), c->jdif.as<double>(), L.w.lin2cell, c->ncell3,
+                                    c->nc + 1, c->nb, s));
+  }
+  int rounds = 0;
+  MC_CUDA(cudaMemcpyAsync(&rounds, L.w.round_ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  cudaGraphDestroy(graph);
+  *rounds_out = rounds;
+  return MC_OK;
+}
+
+mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S, const mcg::DevReplay &rp,
+                   int precision, float *march_ms, int *rounds_out) {
+  mcg::WaveLaunch L{};
+  mc_status st = wave_setup(c, g, S, rp, L);
+  if (st) return st;
+  mcg::WaveGrid &w = L.w;
   const bool f64 = precision == MC_PREC_FP64;
   unsigned int n_abs = 0;
   float total_ms = 0.f;
@@ -688,7 +799,8 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
       if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "transport launch failed: %s", cudaGetErrorString(e));
       MC_CUDA(cudaEventRecord(c->evm1, c->stream));
     } else {
-      mc_status ws = run_wave(c, g, S, rp, o->precision, &wave_ms, &c->rounds);
+      mc_status ws = (o->run_flags & MC_RUN_GRAPH) ? run_wave_graph(c, g, S, rp, o->precision, &c->rounds)
+                                                    : run_wave(c, g, S, rp, o->precision, &wave_ms, &c->rounds);
       if (ws) return ws;
     }
   } else {

@@ -236,7 +236,9 @@ __global__ void __launch_bounds__(256) wave_sample_reemit_kernel(const __grid_co
                                                                 const __grid_constant__ DevSources S,
                                                                 const __grid_constant__ DevReplay rp,
                                                                 const __grid_constant__ WaveGrid w,
-                                                                unsigned int n_abs, DevCounters *cnt) {
+                                                                unsigned int n_param, DevCounters *cnt) {
+  const unsigned int n_abs = n_param == kDeviceCount ? *w.a_count : n_param;
+  if (n_param == kDeviceCount && blockIdx.x == 0 && threadIdx.x == 0) *w.n_round = n_abs;
   extern __shared__ unsigned int sh[];  // [nb] counts
   for (int i = threadIdx.x; i < g.nb; i += blockDim.x) sh[i] = 0u;
   __syncthreads();

@@ -8,6 +8,11 @@
 
 namespace mcg {
 
+// Round entry counts passed as this value are read from the device (the
+// previous march's a_count) instead: the form whose rounds run inside one
+// CUDA graph.
+constexpr unsigned int kDeviceCount = 0xFFFFFFFFu;
+
 struct WaveGrid {
   // march-indexed views of the grid
   const float *opac;        // [nb][S] opacity
@@ -35,6 +40,8 @@ struct WaveGrid {
   void *q_r, *q_v, *q_pass; // Real[3], Real[3], Real
   // packets absorbed in this round (the next round's input)
   unsigned int *a_count;
+  unsigned int *n_round;    // the round's entry count, kept before the scan resets a_count (graph form)
+  int *round_ctr;           // rounds run so far (graph form)
   uint32_t *a_id, *a_cell, *a_words;
   uint16_t *a_run;
   void *a_r;                // Real[3]

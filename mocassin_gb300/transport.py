@@ -124,9 +124,12 @@ def _check_shapes(neb, jste, jdif, escaped):
 
 
 def _flags(form, zero_first=False):
-    if form not in ("wave", "plain"):
-        raise ValueError("form must be 'wave' or 'plain'")
-    return (abi.MC_RUN_FORM_PLAIN if form == "plain" else 0) | (abi.MC_RUN_ZERO_FIRST if zero_first else 0)
+    """form: "wave" (rounds driven by the host), "graph" (the same rounds
+    inside one CUDA graph) or "plain" (one thread per history)."""
+    if form not in ("wave", "plain", "graph"):
+        raise ValueError("form must be 'wave', 'graph' or 'plain'")
+    f = {"wave": 0, "graph": abi.MC_RUN_GRAPH, "plain": abi.MC_RUN_FORM_PLAIN}[form]
+    return f | (abi.MC_RUN_ZERO_FIRST if zero_first else 0)
 
 
 def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None,
