@@ -182,7 +182,7 @@ def converged_model(neb, args):
     from mocassin_gb300 import iterate
     out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
            "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
-    forms = (("chosen", "wave", "fp32", {"train_after": 2}), ("chosen_no_surrogate", "wave", "fp32", None),
+    forms = (("chosen", "graph", "fp32", {"train_after": 2}), ("chosen_no_surrogate", "graph", "fp32", None),
              ("plain", "plain", "fp64", None))
     for name, form, upd, sur in forms:
         li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
@@ -230,7 +230,11 @@ def main():
     ap.add_argument("--ref-packets", type=int, default=200000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--form", default="wave", choices=["wave", "plain"])
+    ap.add_argument("--form", default="graph", choices=["graph", "wave", "plain"],
+                    help="graph: the chosen form with its rounds in one CUDA graph; wave: the same with host-driven "
+                         "rounds; plain: one thread per history")
+    ap.add_argument("--roof-steps", type=int, default=2,
+                    help="host-driven steps that time the march alone for the roofline (graph form)")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-opacity", action="store_true")
     ap.add_argument("--lambda-max", type=int, default=12, help="Lambda iterations at most per form (0: skip)")
@@ -263,7 +267,7 @@ def main():
     npk = sum(neb.n_packets)
     if args.lambda_only:
         from mocassin_gb300 import iterate
-        form, upd = ("wave", "fp32") if args.lambda_only == "chosen" else ("plain", "fp64")
+        form, upd = ("graph", "fp32") if args.lambda_only == "chosen" else ("plain", "fp64")
         li = iterate.LambdaIteration(neb, form=form, update=upd)
         wall, hist = li.run(seed=1000, max_iterations=max(args.lambda_max, 1))
         li.close()
@@ -301,8 +305,16 @@ def main():
         cross_all = float(cross)
     value = cross_all / t_dev
     march_ms = np.array([s["march_ms"] for s in stats])
+    if args.form == "graph":
+        # the march alone is timed only with host-driven rounds: the same work
+        rs = [ctx.run(seed=1 + rank * 1000003 + k, iteration=1, precision=args.precision, zero_first=True,
+                      form="wave") for k in range(max(args.roof_steps, 1))]
+        march_ms = np.array([s["march_ms"] for s in rs])
+        roof_cross = int(sum(s["crossings"] for s in rs))
+    else:
+        roof_cross = cross
     plain = None
-    if args.form == "wave" and args.plain_steps > 0:
+    if args.form in ("wave", "graph") and args.plain_steps > 0:
         ctx.run(seed=999, iteration=1, precision=args.precision, zero_first=True, form="plain")
         ps = [ctx.run(seed=2 + k, iteration=1, precision=args.precision, zero_first=True, form="plain")
               for k in range(args.plain_steps)]
@@ -378,11 +390,13 @@ def main():
     js = torch.zeros((neb.nbins, neb.ncells + 1), dtype=torch.float64).pin_memory()
     es = torch.zeros((neb.nbins + 1, neb.ncells + 1), dtype=torch.float64).pin_memory()
     d2h = (js.numel() + es.numel()) * 8
-    h2d += d2h  # the estimators' current values go up too (the call accumulates into them)
+    # the estimators start each iteration at zero (MC_RUN_ZERO_FIRST: not uploaded)
     e2e_t, e2e_c = 0.0, 0
     for k in range(args.e2e_steps + 1):
         opts = abi.make_opts(seed=77 + k, iteration=1, precision=abi.MC_PREC_FP32 if args.precision == "fp32"
-                             else abi.MC_PREC_FP64, run_flags=abi.MC_RUN_FORM_PLAIN if args.form == "plain" else 0)
+                             else abi.MC_PREC_FP64,
+                             run_flags={"plain": abi.MC_RUN_FORM_PLAIN, "graph": abi.MC_RUN_GRAPH}.get(args.form, 0)
+                             | abi.MC_RUN_ZERO_FIRST)
         st = abi.McStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -396,17 +410,18 @@ def main():
             e2e_t += dt
             e2e_c += st.crossings
     e2e = {"value": e2e_c / e2e_t if e2e_t > 0 else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-           "call": "mc_transport_run (host pinned buffers: grid and estimator upload, CDF re-layout, transport, "
-                   "estimator download; device buffers kept between calls of the same grid shape)"}
+           "call": "mc_transport_run (host pinned buffers: grid upload, CDF re-layout, transport, estimator "
+                   "download; the estimators start at zero (MC_RUN_ZERO_FIRST); device buffers kept between calls "
+                   "of the same grid shape)"}
 
     peak, peak_kind = measured_peak()
     # dominant kernel: the march (its own CUDA events on the library stream)
-    achieved = cross / (float(march_ms.sum()) / 1e3) * BYTES_PER_CROSSING / 1e9
+    achieved = roof_cross / (float(march_ms.sum()) / 1e3) * BYTES_PER_CROSSING / 1e9
     tpc = traffic_per_crossing()
     per_launch_cross = cross / max(len(stats), 1)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (tpc * per_launch_cross) if tpc else None,
-            "kernel": "wave_march_kernel<float,true>" if args.form == "wave" else "transport_plain_kernel<float>",
+            "kernel": "transport_plain_kernel<float>" if args.form == "plain" else "wave_march_kernel<float,true>",
             "kernel_ms_per_step": float(march_ms.mean()), "peak_kind": peak_kind + " hbm_gbs (copy)",
             "algorithmic_bytes_per_crossing": BYTES_PER_CROSSING}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -419,9 +434,10 @@ def main():
                        "l2": "inputs larger than L2 (opacity %.0f MB, Jste %.0f MB)"
                              % (neb.opacity.nbytes / 1e6, neb.opacity.size * 8 / 1e6),
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
-            # per step and round: sample, scan, scatter, emit, march (wave form) or one kernel (plain)
+            # per step and round: sample, scan, scatter, emit, march (+ the round control in the graph
+            # form), or one kernel (plain)
             "roofline": roof, "e2e": e2e,
-            "gpu_launches": int(sum(s["rounds"] for s in stats) * (5 if args.form == "wave" else 1)),
+            "gpu_launches": int(sum(s["rounds"] for s in stats) * {"wave": 5, "graph": 6, "plain": 1}[args.form]),
             "rounds_per_step": float(np.mean([s["rounds"] for s in stats])),
             "clocks": clk}
     if plain:

@@ -74,7 +74,10 @@ typedef enum mc_status {
 
 /* Run flags (mc_run_opts_t.run_flags). */
 #define MC_RUN_ZERO_FIRST 1 /* zero the device estimators inside the call, before
-                               the transport (iteration_mod.f90:458-472)      */
+                               the transport (iteration_mod.f90:458-472); in
+                               mc_transport_run: the caller's arrays hold zeros,
+                               so they are not uploaded (the result overwrites
+                               them)                                          */
 #define MC_RUN_FORM_PLAIN 2 /* one thread per packet history (the plain form)
                                instead of the frequency-sorted persistent march */
 #define MC_RUN_GRAPH 4      /* the chosen form's rounds inside one CUDA graph (a

@@ -1761,11 +1761,15 @@ mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t n
   }
   // the estimators accumulate into the caller's arrays: their current
   // values go to the device first, the kernels add to them, and the sums
-  // come back (no host-side pass over the arrays)
+  // come back (no host-side pass over the arrays).  With MC_RUN_ZERO_FIRST
+  // the caller states that its arrays hold zeros (the Fortran driver zeroes
+  // them before each iteration, iteration_mod.f90:458-472): the device
+  // copies are cleared instead of uploaded.
+  const bool zero = o->run_flags & MC_RUN_ZERO_FIRST;
   struct Item { double *h; DBuf *d; } items[3] = {{jste, &c->jste}, {jdif, &c->jdif}, {escaped, &c->esc}};
   for (auto &it : items) {
     if (!it.d->p) continue;
-    if (it.h) MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, c->stream));
+    if (it.h && !zero) MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, c->stream));
     else MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, c->stream));
   }
   mc_run_opts_t o2 = *o;

@@ -15,7 +15,8 @@ Each iteration runs, on the grid resident in HBM,
 The re-emission CDFs (recPDF) stay those of the input grid: the emission
 step (emission_mod.f90:905-1311) is not part of this path.
 
-``form`` picks the transport ("wave": the frequency-sorted persistent march;
+``form`` picks the transport ("graph": the frequency-sorted persistent march
+with its rounds in one CUDA graph; "wave": the same with host-driven rounds;
 "plain": one thread per history) and ``update`` the arithmetic of the cell
 update ("fp64": the FP64 method; "fp32": the reference's own 4-byte
 precision).  ``surrogate`` adds the learned warm start: the cell states of
@@ -36,7 +37,7 @@ def _ions():
 class LambdaIteration:
     """A nebula resident on the GPU with its cell state."""
 
-    def __init__(self, neb, form="wave", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None):
+    def __init__(self, neb, form="graph", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None):
         """surrogate: None (updates start from the previous state, as the
         reference's) or a dict with train_after (cold iterations whose cell
         states train the MLP first), steps, batch, lr, finetune_steps (after

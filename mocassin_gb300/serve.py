@@ -34,7 +34,7 @@ def device_bytes(neb):
 
 
 class ModelServer:
-    def __init__(self, memory_budget=200e9, workers=4, iterations=3, form="wave", update="fp32",
+    def __init__(self, memory_budget=200e9, workers=4, iterations=3, form="graph", update="fp32",
                  autotune_packets=0):
         self.budget = float(memory_budget)
         self.workers = int(workers)
@@ -81,7 +81,7 @@ class ModelServer:
                 tuned = self.tuning.get(key)
             if tuned is None and self.autotune_packets > 0:
                 tuned, _ = autotune.autotune(li.ctx, min(self.autotune_packets, sum(neb.n_packets)), repeats=1,
-                                             candidates=((4, 4), (8, 4), (8, 8), (8, 16), (16, 8)))
+                                             candidates=((4, 4), (8, 4), (8, 8), (8, 16), (16, 8)), form=self.form)
                 with self._lock:
                     self.tuning[key] = tuned
             if tuned is not None:

@@ -133,20 +133,24 @@ def _flags(form, zero_first=False):
 
 
 def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None,
-                         jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0, form="wave"):
+                         jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0, form="wave",
+                         zero_first=False):
     """Runs every packet of every star of ``neb`` through the GPU transport.
 
     Accumulates into ``jste`` / ``jdif`` / ``escaped`` (created zeroed when not
     given; shapes ``(nbins, Nc+1)`` and ``(nbins+1, Nc+1)``, i.e. Fortran
     ``(0:Nc, 1:nbins)`` cell fastest) and returns ``(jste, jdif, escaped,
     stats)``.  ``form`` selects the frequency-sorted persistent march
-    ("wave", the default) or one thread per history ("plain").
+    ("wave", the default; "graph" with its rounds in one CUDA graph) or one
+    thread per history ("plain").  zero_first: the arrays are overwritten
+    with this transport's sums instead of accumulated into (they are not
+    uploaded).
     """
     lib = library()
     m = abi.Marshalled(neb, n_packets=n_packets)
     prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
     opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
-                         recursion_limit=recursion_limit, safe_limit=safe_limit, run_flags=_flags(form))
+                         recursion_limit=recursion_limit, safe_limit=safe_limit, run_flags=_flags(form, zero_first))
     js0, jd0, es0 = abi.estimator_arrays(neb)
     jste = js0 if jste is None else jste
     escaped = es0 if escaped is None else escaped

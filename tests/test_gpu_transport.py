@@ -183,3 +183,13 @@ def test_drop_in_call_accumulates_and_reuses_its_buffers(gpu_lib):
     assert helpers.rel_err(js, a[0] + b[0]) < RTOL
     assert helpers.rel_err(es, a[2] + b[2]) < RTOL
     assert gpu_lib.mc_transport_release() == 0
+
+
+def test_drop_in_zero_first_overwrites(gpu_lib):
+    neb = nebula.build(CASES[2])
+    ref = transport.energy_packet_driver(neb, precision="fp64", seed=41)
+    js, jd, es = helpers.zeros_like_estimators(neb)
+    js[:] = 1.0
+    es[:] = 2.0
+    got = transport.energy_packet_driver(neb, precision="fp64", seed=41, jste=js, escaped=es, zero_first=True)
+    assert helpers.rel_err(got[0], ref[0]) < 1e-12 and helpers.rel_err(got[2], ref[2]) < 1e-12
