@@ -106,5 +106,20 @@ class LambdaIteration:
     def state(self):
         return self.ctx.get_cell_state()
 
+    def write_grid(self, path):
+        """Snapshot of the cell state in the reference's grid files (writeGrid)."""
+        from . import gridio
+        te, ne, X, conv, niter, flags = self.ctx.get_cell_state()
+        gridio.write_grid(path, self.neb, te, ne, X, conv=conv, black=(flags != 0).astype(np.int32))
+
+    def restart_from(self, path):
+        """Sets the cell state from grid files (resetGrid), e.g. for a warm restart."""
+        from . import gridio
+        g = gridio.read_grid(path)
+        if (g["nx"], g["ny"], g["nz"], g["ncells"]) != (self.neb.nx, self.neb.ny, self.neb.nz, self.neb.ncells):
+            raise ValueError("the snapshot is of another grid")
+        self.ctx.set_cell_state(g["te"], g["ne"], g["X"])
+        self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
+
     def close(self):
         self.ctx.close()
