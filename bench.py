@@ -364,11 +364,11 @@ def main():
     # e2e: the drop-in call with host (pinned) buffers, copies inside the timed region
     import ctypes as C
     from mocassin_gb300 import abi
-    pinned = {}
+    pinned = []  # keeps every pinned buffer alive while the grid struct points at it
 
     def pin(a):
         t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-        pinned[id(a)] = t
+        pinned.append(t)
         return t
 
     lib = transport.library()
