@@ -171,6 +171,11 @@ def run_reference(args):
     return 0
 
 
+# Lambda-iteration forms: (transport form, cell update, surrogate options)
+LAMBDA_FORMS = {"chosen": ("graph", "fp32", {"train_after": 2}), "chosen_no_surrogate": ("graph", "fp32", None),
+                "plain": ("plain", "fp64", None)}
+
+
 def converged_model(neb, args):
     """Wall time to a converged model: Lambda iterations (transport, cell
     update, opacity rebuild) until 95 % of the cells have |dX(H0)/X(H0)| <=
@@ -182,9 +187,7 @@ def converged_model(neb, args):
     from mocassin_gb300 import iterate
     out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
            "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
-    forms = (("chosen", "graph", "fp32", {"train_after": 2}), ("chosen_no_surrogate", "graph", "fp32", None),
-             ("plain", "plain", "fp64", None))
-    for name, form, upd, sur in forms:
+    for name, (form, upd, sur) in LAMBDA_FORMS.items():
         li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
         wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
         li.close()
@@ -197,6 +200,7 @@ def converged_model(neb, args):
                      "opacity_s": sum(h["opacity_s"] for h in hist),
                      "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist]))}
     out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
+    out["speedup_chosen_no_surrogate_vs_plain"] = out["plain"]["wall_s"] / out["chosen_no_surrogate"]["wall_s"]
     return out
 
 
@@ -241,7 +245,7 @@ def main():
     ap.add_argument("--batch-models", type=int, default=16,
                     help="batched serving: models of the 64-model batch to serve (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4)
-    ap.add_argument("--lambda-only", default="", choices=["", "chosen", "plain"],
+    ap.add_argument("--lambda-only", default="", choices=["", "chosen", "chosen_no_surrogate", "plain"],
                     help="run only the Lambda iteration of one form and print its record (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -267,8 +271,8 @@ def main():
     npk = sum(neb.n_packets)
     if args.lambda_only:
         from mocassin_gb300 import iterate
-        form, upd = ("graph", "fp32") if args.lambda_only == "chosen" else ("plain", "fp64")
-        li = iterate.LambdaIteration(neb, form=form, update=upd)
+        form, upd, sur = LAMBDA_FORMS[args.lambda_only]
+        li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
         wall, hist = li.run(seed=1000, max_iterations=max(args.lambda_max, 1))
         li.close()
         print(json.dumps({"lambda_only": args.lambda_only, "workload": neb.spec.name, "wall_s": wall,

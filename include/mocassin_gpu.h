@@ -310,13 +310,17 @@ typedef struct mc_update_stats {
   double dte_max;            /* max |Te_new - Te_old| / Te_old over hit cells  */
   double frac_dte_1pc;       /* fraction of hit cells with |dTe| / Te < 1 %    */
   double moments_ms, update_ms;
+  int64_t warm_fallback;     /* warm start: predictions sent back to the cold
+                                solve (residual >= near_res x the heating)     */
 } mc_update_stats_t;
 
 /* Uploads the atomic tables, the per-cell Hden and the abundances of
  * H, He, C, N, O, Ne, S (number, relative to H). */
 mc_status mc_ctx_set_update_tables(mc_ctx_t *ctx, const mc_update_tables_t *tables, const double *hden,
                                    const double *abund);
-/* Cell state: te, ne [Nc+1]; ionden [Nc+1][7][8] (element, stage 1..7). */
+/* Cell state: te, ne [Nc+1]; ionden [Nc+1][7][8] (element, stage 1..7);
+ * flags per cell: 1 = no Te balance, 2 = no ion balance, 4 = the warm start's
+ * prediction was sent back to the cold solve. */
 mc_status mc_ctx_set_cell_state(mc_ctx_t *ctx, const double *te, const double *ne, const double *ionden);
 mc_status mc_ctx_get_cell_state(mc_ctx_t *ctx, double *te, double *ne, double *ionden, int32_t *conv,
                                 int32_t *niter, int32_t *flags);
@@ -342,18 +346,24 @@ mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32
  * log10 Te and log10 of the 40 ionic fractions.  Trained on cell states the
  * update produced (collect after mc_ctx_update_cells), it warm-starts the
  * update: mc_ctx_update_cells_warm writes the prediction into the state and
- * runs the same solve from there; the solve accepts the prediction when the
- * thermal residual is below 1 % of the heating at its first step, and
- * otherwise brackets the balance with steps of 3 %, 6 %, 12 %, then the
- * reference's 20 %, before its secant; every result meets the reference's
- * 1 % residual test.  No counterpart in the reference (updateCell starts
- * from the previous iteration's state with 20 % steps). */
+ * runs the same solve from there.  At the first T step the solve accepts
+ * the prediction when the thermal residual is below 1 % of the heating;
+ * below 30 % it brackets the balance from the prediction with steps of 3 %,
+ * 6 %, 12 %, then the reference's 20 %, before its secant; otherwise the
+ * cell falls back to the plain solve from the state before the prediction
+ * (20 % steps, the full 25 T steps; counted in warm_fallback).  Every result
+ * meets the reference's 1 % residual test.  No counterpart in the reference
+ * (updateCell starts from the previous iteration's state with 20 % steps). */
 mc_status mc_ctx_surrogate_init(mc_ctx_t *ctx, uint64_t seed, int64_t capacity);
 mc_status mc_ctx_surrogate_collect(mc_ctx_t *ctx, int64_t *rows);
 mc_status mc_ctx_surrogate_train(mc_ctx_t *ctx, int32_t steps, int32_t batch, float lr, uint64_t seed, double *loss,
                                  double *train_ms);
 mc_status mc_ctx_update_cells_warm(mc_ctx_t *ctx, const float *w, double scale, double xhi_limit, int32_t precision,
                                    mc_update_stats_t *stats);
+/* The warm start's fallback threshold: a prediction whose residual is at
+ * least near_res x the heating (>= 0.01; default 0.3) goes back to the
+ * plain solve. */
+mc_status mc_ctx_surrogate_fallback(mc_ctx_t *ctx, double near_res);
 /* Parameters (33072 floats: W1[128][80] b1 W2[128][128] b2 W3[48][128] b3). */
 mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
 /* Loss and gradients of one batch (x [m][80], normalised targets t [m][48];

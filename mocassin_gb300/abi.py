@@ -70,7 +70,8 @@ class McUpdateTables(C.Structure):
 class McUpdateStats(C.Structure):
     _fields_ = [("hit", C.c_int64), ("converged", C.c_int64), ("no_te_balance", C.c_int64),
                 ("no_ion_balance", C.c_int64), ("t_iterations", C.c_int64), ("dte_max", C.c_double),
-                ("frac_dte_1pc", C.c_double), ("moments_ms", C.c_double), ("update_ms", C.c_double)]
+                ("frac_dte_1pc", C.c_double), ("moments_ms", C.c_double), ("update_ms", C.c_double),
+                ("warm_fallback", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -10,7 +10,7 @@ namespace {
 
 __global__ void update_stats_kernel(int nc, const int *conv, const int *niter, const int *flags, const double *dte,
                                     UpdStatsDev *s) {
-  unsigned long long hit = 0, cv = 0, nte = 0, nio = 0, it = 0, small = 0;
+  unsigned long long hit = 0, cv = 0, nte = 0, nio = 0, it = 0, small = 0, fb = 0;
   double dmax = 0.;
   for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x) {
     if (dte[c] < 0.) continue;
@@ -18,6 +18,7 @@ __global__ void update_stats_kernel(int nc, const int *conv, const int *niter, c
     cv += conv[c];
     nte += flags[c] & 1;
     nio += (flags[c] >> 1) & 1;
+    fb += (flags[c] >> 2) & 1;
     it += niter[c];
     small += dte[c] < 0.01;
     dmax = fmax(dmax, dte[c]);
@@ -29,6 +30,7 @@ __global__ void update_stats_kernel(int nc, const int *conv, const int *niter, c
     nio += __shfl_xor_sync(0xffffffffu, nio, o);
     it += __shfl_xor_sync(0xffffffffu, it, o);
     small += __shfl_xor_sync(0xffffffffu, small, o);
+    fb += __shfl_xor_sync(0xffffffffu, fb, o);
     dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
   }
   if ((threadIdx.x & 31) == 0) {
@@ -38,6 +40,7 @@ __global__ void update_stats_kernel(int nc, const int *conv, const int *niter, c
     atomicAdd(&s->no_ion, nio);
     atomicAdd(&s->iters, it);
     atomicAdd(&s->small, small);
+    atomicAdd(&s->fallback, fb);
     atomicMax(&s->dmax_bits, (unsigned long long)__double_as_longlong(dmax));
   }
 }

@@ -318,9 +318,9 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       }
     }
     __syncwarp();
-    const Real XOldHI = a.xh0_prev ? (Real)a.xh0_prev[c] : sX[w][0][1];
+    const Real XOldHI = a.x_prev ? (Real)a.x_prev[(size_t)c * kNE * kNX + 1] : sX[w][0][1];
     int nIterT = 0, noTe = 0;
-    bool ionConv = true;
+    bool ionConv = true, warm = a.x_prev != nullptr, grow = a.step_grow != 0, cold = false;
     Real thResHigh = 0., thResLow = 0., Thigh = 0., Tlow = 0.;
     Real fstep = (Real)a.step0;
     for (;;) {
@@ -456,6 +456,23 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       coolInt = __shfl_sync(0xffffffffu, coolInt, 0);
       const Real thResidual = heatInt - coolInt;
       bool again = false;
+      if (warm) {
+        warm = false;
+        // a prediction far from balance: the cold solve from the state
+        // before the prediction, with the full T-step allowance
+        if (fabs(thResidual) >= (Real)a.near_res * heatInt) {
+          const double *Xp = a.x_prev + (size_t)c * kNE * kNX;
+          for (int i = lane; i < kNE * kNX; i += 32) sX[w][i / kNX][i % kNX] = (Real)Xp[i];
+          Te = (Real)a.te_prev[c];
+          Ne = (Real)a.ne_prev[c];
+          fstep = (Real)1.2;
+          grow = false;
+          cold = true;
+          nIterT = 0;
+          __syncwarp();
+          continue;
+        }
+      }
       if (fabs(thResidual) >= (Real)0.01 * heatInt) {
         if (nIterT < 25) {
           bool open = false;
@@ -470,7 +487,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
             if (Tlow != (Real)0.) Te = Tlow - (Thigh - Tlow) * thResLow / (thResHigh - thResLow);
             else { Te = Te * fstep; open = true; }
           }
-          if (open && a.step_grow) fstep = fstep - (Real)1. < (Real)0.1 ? (Real)1. + (Real)2. * (fstep - (Real)1.) : (Real)1.2;
+          if (open && grow) fstep = fstep - (Real)1. < (Real)0.1 ? (Real)1. + (Real)2. * (fstep - (Real)1.) : (Real)1.2;
           if (nIterT >= 6 && fabs(Thigh - Tlow) <= (Real)0.002 * (Thigh + Tlow)) {
             if (thResidual < (Real)0) { Te = Thigh - (Real)100.; Thigh = (Real)0.; }
             else { Te = Tlow + (Real)100.; Tlow = (Real)0.; }
@@ -493,7 +510,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       a.ne[c] = (double)Ne;
       a.conv[c] = fabs((sX[w][0][1] - XOldHI) / XOldHI) <= (Real)a.xhi ? 1 : 0;
       a.niter[c] = nIterT;
-      a.flags[c] = (noTe ? 1 : 0) | (ionConv ? 0 : 2);
+      a.flags[c] = (noTe ? 1 : 0) | (ionConv ? 0 : 2) | (cold ? 4 : 0);
       a.dte[c] = fabs((double)Te - (double)Te0) / (double)Te0;
     }
     __syncwarp();

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ W
     for (int e = 0; e < kNE; ++e)
       for (int s = 1; s < kNX; ++s) XS(w, e * kNX + s, c) = X[e][s];
     w.Ne[c] = Ne;
-    w.flags[c] = conv ? 0 : 2;
+    w.flags[c] = (w.flags[c] & 4) | (conv ? 0 : 2);
   }
 }
 
@@ -196,8 +196,22 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
     const float res = heat - cool;
     float Thigh = w.sec[0 * nc1 + c], Tlow = w.sec[1 * nc1 + c];
     float resHigh = w.sec[2 * nc1 + c], resLow = w.sec[3 * nc1 + c], fstep = w.sec[4 * nc1 + c];
-    const int nIterT = ++w.nit[c];
+    int nIterT = ++w.nit[c];
     bool again = false, noTe = false;
+    if (a.x_prev && nIterT == 1 && !(w.flags[c] & 4) && fabsf(res) >= (float)a.near_res * heat) {
+      // a prediction far from balance: the cold solve from the state before
+      // the prediction, with the full T-step allowance (one extra T step)
+      const double *Xp = a.x_prev + (size_t)c * kX;
+      for (int i = 0; i < kX; ++i) XS(w, i, c) = (float)Xp[i];
+      w.Te[c] = (float)a.te_prev[c];
+      w.Ne[c] = (float)a.ne_prev[c];
+      for (int k = 0; k < 4; ++k) w.sec[k * nc1 + c] = 0.f;
+      w.sec[4 * nc1 + c] = 1.2f;
+      w.nit[c] = 0;
+      w.flags[c] |= 4;
+      w.act[cur ^ 1][atomicAdd(&w.count[cur ^ 1], 1)] = c;
+      continue;
+    }
     if (fabsf(res) >= 0.01f * heat) {
       if (nIterT < 25) {
         bool open = false;
@@ -212,7 +226,7 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
           if (Tlow != 0.f) Te = Tlow - (Thigh - Tlow) * resLow / (resHigh - resLow);
           else { Te = Te * fstep; open = true; }
         }
-        if (open && a.step_grow) fstep = fstep - 1.f < 0.1f ? 1.f + 2.f * (fstep - 1.f) : 1.2f;
+        if (open && a.step_grow && !(w.flags[c] & 4)) fstep = fstep - 1.f < 0.1f ? 1.f + 2.f * (fstep - 1.f) : 1.2f;
         if (nIterT >= 6 && fabsf(Thigh - Tlow) <= 0.002f * (Thigh + Tlow)) {
           if (res < 0.f) { Te = Thigh - 100.f; Thigh = 0.f; }
           else { Te = Tlow + 100.f; Tlow = 0.f; }
@@ -237,7 +251,7 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
     // state the update started from: the convergence test compares with it)
     double *Xc = a.X + (size_t)c * kX;
     const double te0 = a.te_prev ? a.te_prev[c] : a.te[c];
-    const double x0 = a.xh0_prev ? a.xh0_prev[c] : Xc[1];
+    const double x0 = a.x_prev ? a.x_prev[(size_t)c * kX + 1] : Xc[1];
     for (int e = 0; e < kNE; ++e)
       for (int s = 1; s < kNX; ++s) Xc[e * kNX + s] = (double)XS(w, e * kNX + s, c);
     a.te[c] = (double)Te;
@@ -245,7 +259,7 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
     const double xh = (double)xH1;
     a.conv[c] = fabs((xh - x0) / x0) <= a.xhi ? 1 : 0;
     a.niter[c] = nIterT;
-    a.flags[c] = (noTe ? 1 : 0) | (w.flags[c] & 2);
+    a.flags[c] = (noTe ? 1 : 0) | (w.flags[c] & 6);
     a.dte[c] = fabs((double)Te - te0) / te0;
   }
 }
@@ -281,7 +295,9 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
   if (e != cudaSuccess) return e;
   const int blocks = num_sms * 8;
   wave_init_kernel<<<blocks, 256, 0, stream>>>(w);
-  for (int t = 0; t < 25; ++t) {
+  // a warm start may send a cell back to the cold solve after its first step
+  const int steps = a.x_prev ? 26 : 25;
+  for (int t = 0; t < steps; ++t) {
     const int cur = t & 1;
     wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
     wave_ion_kernel<<<blocks, 128, 0, stream>>>(w, cur);

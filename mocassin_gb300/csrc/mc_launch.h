@@ -69,7 +69,7 @@ template <typename Real> struct UpdTabs {
   const Real *ab;
 };
 struct UpdStatsDev {
-  unsigned long long hit, converged, no_te, no_ion, iters, small, dmax_bits;
+  unsigned long long hit, converged, no_te, no_ion, iters, small, dmax_bits, fallback;
 };
 struct UpdArgs {
   int nc, ncel, ndirec, naldro;
@@ -84,7 +84,12 @@ struct UpdArgs {
   double *dte;
   double xhi;
   int mat_rows, mat_stride;  // FP32 form: matrix row length (max levels) and odd per-lane stride
-  const double *te_prev, *xh0_prev;  // warm start: the state before the prediction (null: cold)
+  // warm start: the state before the prediction (null: cold).  At the first
+  // T step a prediction whose thermal residual is below 1 % of the heating is
+  // accepted; below near_res it is bracketed with small steps; otherwise the
+  // cell restarts the cold solve from this state (the plain solve as fallback).
+  const double *te_prev, *ne_prev, *x_prev;  // x_prev [nc+1][7][8]
+  double near_res;
   double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
   int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
 };
@@ -119,12 +124,13 @@ cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dste
 cudaError_t mlp_prepare();
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s);
 cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
-                               const double *X, long long cap, unsigned long long *count, float *xs, float *ts,
-                               int num_sms, cudaStream_t s);
+                               const double *X, const int *flags, long long cap, unsigned long long *count, float *xs,
+                               float *ts, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_infer_features(int nc, const float *mom, long long ms, const double *hden, const float *fmean,
                                       const float *fstd, float *x, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const float *tmean, const float *tstd, double *te,
-                             double *X, double *te_prev, double *xh0_prev, int num_sms, cudaStream_t s);
+                             double *ne, double *X, double *te_prev, double *ne_prev, double *x_prev, int num_sms,
+                             cudaStream_t s);
 
 cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
                                     const float *hit, float *tdust, int num_sms, cudaStream_t stream);

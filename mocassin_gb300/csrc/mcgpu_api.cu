@@ -123,10 +123,11 @@ struct mc_ctx {
   int u_bal_z[7] = {}, u_bal_first[7] = {};
   // learned warm start: parameters, Adam state, training buffer, work arrays
   DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss, m_dstep;
-  DBuf m_xb, m_tb, m_a1, m_a2, m_y, m_dy, m_d2, m_d1, m_xi, m_h1, m_h2, m_yi, m_te_prev, m_xh0_prev;
+  DBuf m_xb, m_tb, m_a1, m_a2, m_y, m_dy, m_d2, m_d1, m_xi, m_h1, m_h2, m_yi, m_te_prev, m_ne_prev, m_x_prev;
   long long m_cap = 0, m_n = 0;
   int m_step = 0, m_B = 0;
   bool m_ready = false, m_norm = false;
+  double m_near_res = 0.3;  // warm start: residual / heating below which a prediction is bracketed
   bool u_ready = false, s_ready = false;
   // the FP32 update's launch sequence, captured once per argument set
   cudaGraphExec_t wave_exec = nullptr;
@@ -1296,7 +1297,9 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   mcg::UpdArgs a{};
   a.nc = c->nc;
   a.te_prev = warm ? c->m_te_prev.as<double>() : nullptr;
-  a.xh0_prev = warm ? c->m_xh0_prev.as<double>() : nullptr;
+  a.ne_prev = warm ? c->m_ne_prev.as<double>() : nullptr;
+  a.x_prev = warm ? c->m_x_prev.as<double>() : nullptr;
+  a.near_res = c->m_near_res;
   // a predicted Te is near the balance: bracket it with small steps first
   a.step0 = warm ? 1.03 : 1.2;
   a.step_grow = warm ? 1 : 0;
@@ -1377,6 +1380,7 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
     stats->converged = (int64_t)hs.converged;
     stats->no_te_balance = (int64_t)hs.no_te;
     stats->no_ion_balance = (int64_t)hs.no_ion;
+    stats->warm_fallback = (int64_t)hs.fallback;
     stats->t_iterations = (int64_t)hs.iters;
     double dmax;
     std::memcpy(&dmax, &hs.dmax_bits, sizeof dmax);
@@ -1469,7 +1473,8 @@ mc_status surrogate_predict_state(mc_ctx_t *c) {
   mc_status st;
   if ((st = ensure(c->m_xi, (size_t)nc1 * kMlpIn * 4)) || (st = ensure(c->m_h1, (size_t)nc1 * kMlpHid * 4)) ||
       (st = ensure(c->m_h2, (size_t)nc1 * kMlpHid * 4)) || (st = ensure(c->m_yi, (size_t)nc1 * kMlpOut * 4)) ||
-      (st = ensure(c->m_te_prev, (size_t)nc1 * 8)) || (st = ensure(c->m_xh0_prev, (size_t)nc1 * 8)))
+      (st = ensure(c->m_te_prev, (size_t)nc1 * 8)) || (st = ensure(c->m_ne_prev, (size_t)nc1 * 8)) ||
+      (st = ensure(c->m_x_prev, (size_t)nc1 * 56 * 8)))
     return st;
   cudaError_t e = mcg::launch_mlp_infer_features(c->nc, c->s_mom.as<float>(), nc1, c->u_hden.as<double>(),
                                                  c->m_fmean.as<float>(), c->m_fstd.as<float>(), c->m_xi.as<float>(),
@@ -1478,8 +1483,9 @@ mc_status surrogate_predict_state(mc_ctx_t *c) {
   if ((st = mlp_forward(c, nc1, c->m_xi.as<float>(), c->m_h1.as<float>(), c->m_h2.as<float>(), c->m_yi.as<float>())))
     return st;
   e = mcg::launch_mlp_apply(c->nc, c->s_mom.as<float>(), c->m_yi.as<float>(), c->m_tmean.as<float>(),
-                            c->m_tstd.as<float>(), c->s_te.as<double>(), c->s_X.as<double>(), c->m_te_prev.as<double>(),
-                            c->m_xh0_prev.as<double>(), c->num_sms, s);
+                            c->m_tstd.as<float>(), c->s_te.as<double>(), c->s_ne.as<double>(), c->s_X.as<double>(),
+                            c->m_te_prev.as<double>(), c->m_ne_prev.as<double>(), c->m_x_prev.as<double>(),
+                            c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "apply failed: %s", cudaGetErrorString(e));
   return MC_OK;
 }
@@ -1516,6 +1522,12 @@ mc_status surrogate_normalise(mc_ctx_t *c) {
 }
 
 }  // namespace
+
+extern "C" mc_status mc_ctx_surrogate_fallback(mc_ctx_t *c, double near_res) {
+  if (!c || !(near_res >= 0.01)) return set_error(MC_ERR_ARG, "ctx and near_res >= 0.01 are required");
+  c->m_near_res = near_res;
+  return MC_OK;
+}
 
 extern "C" mc_status mc_ctx_surrogate_init(mc_ctx_t *c, uint64_t seed, int64_t capacity) {
   if (!c || capacity < 1) return set_error(MC_ERR_ARG, "ctx and a positive capacity are required");
@@ -1563,7 +1575,7 @@ extern "C" mc_status mc_ctx_surrogate_collect(mc_ctx_t *c, int64_t *rows) {
   if (!c->s_mom.p || !c->s_ready) return set_error(MC_ERR_ARG, "no cell update to learn from");
   cudaStream_t s = c->stream;
   cudaError_t e = mcg::launch_mlp_collect(c->nc, c->s_mom.as<float>(), c->nc + 1, c->u_hden.as<double>(),
-                                          c->s_te.as<double>(), c->s_X.as<double>(), c->m_cap,
+                                          c->s_te.as<double>(), c->s_X.as<double>(), c->s_flags.as<int>(), c->m_cap,
                                           c->m_count.as<unsigned long long>(), c->m_xs.as<float>(),
                                           c->m_ts.as<float>(), c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "collect failed: %s", cudaGetErrorString(e));

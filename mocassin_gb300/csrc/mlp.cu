@@ -216,9 +216,11 @@ __device__ __forceinline__ int stage_count(int e) { return e == 0 ? 2 : (e == 1 
 
 // appends (features, targets) of every hit cell to the training buffer
 __global__ void mlp_collect_kernel(int nc, const float *mom, long long ms, const double *hden, const double *te,
-                                   const double *X, long long cap, unsigned long long *count, float *xs, float *ts) {
+                                   const double *X, const int *flags, long long cap, unsigned long long *count,
+                                   float *xs, float *ts) {
   for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x) {
-    if (!(mom[c] > 0.f)) continue;
+    // only states the update balanced (no noTeBal, no noIonBal) teach the model
+    if (!(mom[c] > 0.f) || (flags[c] & 3)) continue;
     const unsigned long long k = atomicAdd(count, 1ull);
     if ((long long)k >= cap) continue;
     float f[kMlpIn];
@@ -245,13 +247,15 @@ __global__ void mlp_infer_features_kernel(int nc, const float *mom, long long ms
 }
 
 // writes the prediction into the cell state of every hit cell, keeping the
-// previous Te and X(H0) for the convergence test of the update
+// previous Te, Ne and X for the convergence test of the update and for the
+// fallback to the plain solve
 __global__ void mlp_apply_kernel(int nc, const float *mom, const float *y, const float *tmean, const float *tstd,
-                                 double *te, double *X, double *te_prev, double *xh0_prev) {
+                                 double *te, double *ne, double *X, double *te_prev, double *ne_prev, double *x_prev) {
   for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x) {
     double *Xc = X + (size_t)c * 56;
     te_prev[c] = te[c];
-    xh0_prev[c] = Xc[1];
+    ne_prev[c] = ne[c];
+    for (int i = 0; i < 56; ++i) x_prev[(size_t)c * 56 + i] = Xc[i];
     if (!(mom[c] > 0.f)) continue;
     const float *yc = y + (size_t)c * kMlpOut;
     double t = pow(10., (double)(yc[0] * tstd[0] + tmean[0]));
@@ -339,9 +343,9 @@ cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum,
 }
 
 cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
-                               const double *X, long long cap, unsigned long long *count, float *xs, float *ts,
-                               int num_sms, cudaStream_t s) {
-  mlp_collect_kernel<<<num_sms * 4, 256, 0, s>>>(nc, mom, ms, hden, te, X, cap, count, xs, ts);
+                               const double *X, const int *flags, long long cap, unsigned long long *count, float *xs,
+                               float *ts, int num_sms, cudaStream_t s) {
+  mlp_collect_kernel<<<num_sms * 4, 256, 0, s>>>(nc, mom, ms, hden, te, X, flags, cap, count, xs, ts);
   return cudaGetLastError();
 }
 
@@ -352,8 +356,9 @@ cudaError_t launch_mlp_infer_features(int nc, const float *mom, long long ms, co
 }
 
 cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const float *tmean, const float *tstd, double *te,
-                             double *X, double *te_prev, double *xh0_prev, int num_sms, cudaStream_t s) {
-  mlp_apply_kernel<<<num_sms * 4, 256, 0, s>>>(nc, mom, y, tmean, tstd, te, X, te_prev, xh0_prev);
+                             double *ne, double *X, double *te_prev, double *ne_prev, double *x_prev, int num_sms,
+                             cudaStream_t s) {
+  mlp_apply_kernel<<<num_sms * 4, 256, 0, s>>>(nc, mom, y, tmean, tstd, te, ne, X, te_prev, ne_prev, x_prev);
   return cudaGetLastError();
 }
 

@@ -90,7 +90,8 @@ class LambdaIteration:
                "update_ms": up["update_ms"], "moments_ms": up["moments_ms"], "opacity_ms": op_ms,
                "hit": up["hit"], "converged_pct": 100.0 * up["converged"] / max(up["hit"], 1),
                "dte_lt_1pc_pct": 100.0 * up["frac_dte_1pc"], "t_steps_per_cell": up["t_iterations"] / max(up["hit"], 1),
-               "no_te_balance": up["no_te_balance"], "no_ion_balance": up["no_ion_balance"]}
+               "no_te_balance": up["no_te_balance"], "no_ion_balance": up["no_ion_balance"],
+               "warm_fallback_pct": 100.0 * up["warm_fallback"] / max(up["hit"], 1)}
         self.history.append(rec)
         return rec
 

@@ -73,6 +73,8 @@ def library():
         lib.mc_ctx_opacity_from_state.argtypes = [C.c_void_p, C.c_int32, ip, fp, C.c_int32, dp]
         u64 = C.c_uint64
         lib.mc_ctx_surrogate_init.restype = C.c_int
+        lib.mc_ctx_surrogate_fallback.restype = C.c_int
+        lib.mc_ctx_surrogate_fallback.argtypes = [C.c_void_p, C.c_double]
         lib.mc_ctx_surrogate_init.argtypes = [C.c_void_p, u64, C.c_int64]
         lib.mc_ctx_surrogate_collect.restype = C.c_int
         lib.mc_ctx_surrogate_collect.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
@@ -293,6 +295,11 @@ class TransportContext:
 
     def surrogate_init(self, seed=1, capacity=2_000_000):
         _check(self.lib.mc_ctx_surrogate_init(self.handle, int(seed), int(capacity)))
+
+    def surrogate_fallback(self, near_res):
+        """Residual / heating at the prediction from which a warm start falls
+        back to the plain solve (mc_ctx_surrogate_fallback)."""
+        _check(self.lib.mc_ctx_surrogate_fallback(self.handle, float(near_res)))
 
     def surrogate_collect(self):
         n = C.c_int64()

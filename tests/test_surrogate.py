@@ -116,3 +116,42 @@ def test_lambda_iteration_with_surrogate_keeps_warm_starting(gpu_lib):
     li.close()
     assert [h["warm"] for h in hist] == [False, False, True, True, True]
     assert hist[1]["surrogate_train_ms"] > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_bad_prediction_falls_back_to_the_plain_solve(gpu_lib, precision):
+    """A prediction far from balance (Te forced to the 100 K clamp) is sent
+    back to the cold solve from the state before it: the result is the plain
+    update's, bit for bit, and every hit cell is counted as a fallback."""
+    neb = _clumpy(n=21, packets=400_000)
+    ctx = transport.TransportContext(neb)
+    ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+    te, ne, X = balance.initial_state(neb)
+    ctx.set_cell_state(te, ne, X)
+    ions = _ions()
+    w = balance.moment_weights(neb.xs, neb.nu, ions)
+    ctx.surrogate_init(seed=2, capacity=50_000)
+    ctx.run(seed=11, precision="fp32", zero_first=True)
+    ctx.update_cells(w, 1e-9, precision=precision)
+    ctx.surrogate_collect()
+    ctx.surrogate_train(steps=1, batch=1024, lr=1e-3)
+    p = ctx.surrogate_params()
+    p[O.OFF["b3"][0]] = -100.0  # log10 Te far below the data: Te = 100 K
+    ctx.surrogate_params(set=p)
+    s0 = ctx.get_cell_state()
+    cold = ctx.update_cells(w, 1e-9, precision=precision)
+    sc = ctx.get_cell_state()
+    ctx.set_cell_state(s0[0], s0[1], s0[2])
+    warm = ctx.update_cells(w, 1e-9, precision=precision, warm=True)
+    sw = ctx.get_cell_state()
+    ctx.close()
+    assert cold["warm_fallback"] == 0
+    assert warm["hit"] == cold["hit"] > 0
+    assert warm["warm_fallback"] == warm["hit"]
+    for k in range(5):  # te, ne, X, conv, niter
+        np.testing.assert_array_equal(sw[k], sc[k])
+    hit = sc[4] > 0
+    assert np.all((sw[5][hit] & 4) == 4)
+    np.testing.assert_array_equal(sw[5] & 3, sc[5] & 3)
+    assert warm["t_iterations"] == cold["t_iterations"]
