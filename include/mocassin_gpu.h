@@ -364,6 +364,46 @@ mc_status mc_ctx_update_cells_warm(mc_ctx_t *ctx, const float *w, double scale, 
  * least near_res x the heating (>= 0.01; default 0.3) goes back to the
  * plain solve. */
 mc_status mc_ctx_surrogate_fallback(mc_ctx_t *ctx, double near_res);
+
+/* ---- diffuse-emission CDF on the GPU ---------------------------------------
+ * emissionDriver + setDiffusePDF (emission_mod.f90:32-1311) for a gas grid:
+ * from the resident cell state, every cell's recPDF row (the cumulative f-b,
+ * f-f, two-photon and heavy-ion continua of HI, HeI and HeII, normalised,
+ * entries above 0.999998 set to 1) and totalLines (the fraction of the
+ * emitted energy in recombination and forbidden lines), written in place
+ * into the transport's CDF rows.  Replaces the per-cell host loop the
+ * Fortran runs before each transport (iteration_mod.f90, emissionDriver
+ * calls) and the allreduce of recPDF.  The tables are the reference's own
+ * module arrays; nu and wid_flx are the grid's nuArray and widFlx. */
+typedef struct mc_emission_tables {
+  int32_t nbins;             /* must equal the grid's                          */
+  const float *nu, *wid_flx; /* [nbins] nuArray [Ryd], widFlx                  */
+  const float *xs_h, *xs_hei, *xs_heii; /* [nbins] HI, HeI-singlet, HeII
+                                ground-state cross-sections [cm^2] at each bin */
+  int32_t ntk;               /* gamma temperature points (tkGamma)             */
+  const float *tk;           /* [ntk]                                          */
+  int32_t nlim_hi, nlim_hei, nlim_heii; /* nlimGammaHI & co. (even)            */
+  const float *nu_gamma_hi, *nu_gamma_hei, *nu_gamma_heii; /* [nlim] edges     */
+  const float *lg_hi, *lg_hei, *lg_heii; /* [ntk][nlim] log10 gamma (0: none) */
+  const float *y_ay;         /* [41][2] y_dat, Ay_dat (HeI 2^1S two-photon)    */
+  const float *hi_rec;       /* [16][9] HIRecLineData (iup, ilow)              */
+  const float *heii_rec;     /* [31][17] HeIIRecLineData                       */
+  const float *heii_lyman;   /* [4][2] HeIILymanData, HeIILymanNu              */
+  const float *hei_rec;      /* [34][3][4] HeIrecLineCoeff, first column x1e25 */
+  const double *gaunt_dd;    /* [88] getGauntFF's dd                           */
+  int32_t n_heavy;           /* recombining heavy ions (<= 32)                 */
+  const int32_t *heavy;      /* [n_heavy][8]: z, ion, nElec, outShell, g0, g1,
+                                IPnuP, highNuP (1-based bins)                  */
+  const float *xs_outer;     /* [n_heavy][nbins] outer-shell cross-section     */
+} mc_emission_tables_t;
+
+mc_status mc_ctx_set_emission_tables(mc_ctx_t *ctx, const mc_emission_tables_t *tables);
+/* Builds every cell's emission CDF from the resident Te, Ne and ionic
+ * fractions (needs mc_ctx_set_update_tables for the forbidden lines and the
+ * abundances, and a cell state); ms = device time, or NULL. */
+mc_status mc_ctx_build_emission(mc_ctx_t *ctx, float *ms);
+/* Downloads the CDF rows [Nc+1][nbins] and totalLines [Nc+1] (either NULL). */
+mc_status mc_ctx_get_emission(mc_ctx_t *ctx, float *rec_rows, float *total_lines);
 /* Parameters (33072 floats: W1[128][80] b1 W2[128][128] b2 W3[48][128] b3). */
 mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
 /* Loss and gradients of one batch (x [m][80], normalised targets t [m][48];

@@ -67,6 +67,42 @@ class McUpdateTables(C.Structure):
                 ("cel_e", _dp), ("cel_br", _dp), ("cel_z", _dp), ("cel_ar", _dp), ("cel_ad", _dp)]
 
 
+_fp = C.POINTER(C.c_float)
+
+
+class McEmissionTables(C.Structure):
+    _fields_ = [("nbins", C.c_int32), ("nu", _fp), ("wid_flx", _fp), ("xs_h", _fp), ("xs_hei", _fp),
+                ("xs_heii", _fp), ("ntk", C.c_int32), ("tk", _fp), ("nlim_hi", C.c_int32), ("nlim_hei", C.c_int32),
+                ("nlim_heii", C.c_int32), ("nu_gamma_hi", _fp), ("nu_gamma_hei", _fp), ("nu_gamma_heii", _fp),
+                ("lg_hi", _fp), ("lg_hei", _fp), ("lg_heii", _fp), ("y_ay", _fp), ("hi_rec", _fp),
+                ("heii_rec", _fp), ("heii_lyman", _fp), ("hei_rec", _fp), ("gaunt_dd", _dp), ("n_heavy", C.c_int32),
+                ("heavy", _ip), ("xs_outer", _fp)]
+
+
+def emission_tables_struct(t):
+    """McEmissionTables over the arrays of mocassin_gb300.emission.tables()."""
+    keep = {}
+
+    def f(name):
+        a = np.ascontiguousarray(t[name], dtype=np.float32)
+        keep[name] = a
+        return a.ctypes.data_as(_fp)
+
+    dd = np.ascontiguousarray(t["gaunt_dd"], dtype=np.float64)
+    hv = np.ascontiguousarray(t["shells"], dtype=np.int32)
+    keep["dd"], keep["hv"] = dd, hv
+    s = McEmissionTables(nbins=len(t["nu"]), nu=f("nu"), wid_flx=f("wid_flx"), xs_h=f("xs_h"), xs_hei=f("xs_hei"),
+                         xs_heii=f("xs_heii"), ntk=len(t["tk"]), tk=f("tk"), nlim_hi=len(t["nu_gamma_hi"]),
+                         nlim_hei=len(t["nu_gamma_hei"]), nlim_heii=len(t["nu_gamma_heii"]),
+                         nu_gamma_hi=f("nu_gamma_hi"), nu_gamma_hei=f("nu_gamma_hei"),
+                         nu_gamma_heii=f("nu_gamma_heii"), lg_hi=f("lg_hi"), lg_hei=f("lg_hei"),
+                         lg_heii=f("lg_heii"), y_ay=f("y_ay"), hi_rec=f("hi_rec"), heii_rec=f("heii_rec"),
+                         heii_lyman=f("heii_lyman"), hei_rec=f("hei_rec"), gaunt_dd=dd.ctypes.data_as(_dp),
+                         n_heavy=len(hv), heavy=hv.ctypes.data_as(_ip), xs_outer=f("xs_outer"))
+    s._keep = keep
+    return s
+
+
 class McUpdateStats(C.Structure):
     _fields_ = [("hit", C.c_int64), ("converged", C.c_int64), ("no_te_balance", C.c_int64),
                 ("no_ion_balance", C.c_int64), ("t_iterations", C.c_int64), ("dte_max", C.c_double),

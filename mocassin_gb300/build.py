@@ -31,6 +31,7 @@ UNITS = [
     ("cellupdate.cu", ["-fmad=false", "-Xcompiler=-ffp-contract=off"]),
     ("cellupdate_fp32.cu", []),
     ("mlp.cu", []),
+    ("emission.cu", []),
 ]
 
 

@@ -198,8 +198,13 @@ __device__ Real cel_cooling(const UpdArgs &a, int k, Real Te, Real Ne, Real up) 
 // fall in distinct banks), built pair by pair: each transition adds its
 // collision and radiative rates to the rows of both of its levels.  The sums
 // on the diagonal are formed in another order than the reference's row loop.
+// top_levels = 10 gives thermBalance's cooling (transitions among levels
+// 1..10).  With fscale > 0 each line is scaled by fscale and only lines above
+// 1e-35 count: setDiffusePDF's normFor over forbiddenLines (all levels,
+// emission_mod.f90:1151-1172).
 template <typename Real>
-__device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real up, Real *M, int L) {
+__device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real up, Real *M, int L,
+                                 int top_levels = 10, Real fscale = (Real)0.) {
   const UpdTabs<Real> &T = tabs<Real>(a);
   if (up != up) return (Real)0.;
   const UpdCelT<Real> &c = T.cel[k];
@@ -281,11 +286,15 @@ __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real
   Real sumN = (Real)0.;
   for (int i = 1; i <= n; ++i) sumN += y[i];
   Real cool = (Real)0.;
-  const int top = n < 10 ? n : 10;
+  const int top = n < top_levels ? n : top_levels;
   const Real inv = (Real)1. / sumN;
   for (int i = 1; i <= top - 1; ++i)
     for (int j = i + 1; j <= top; ++j)
-      if (A[j * kNL + i] != (Real)0.) cool += (Real)A[j * kNL + i] * ((Real)e[j] - (Real)e[i]) * (y[j] * inv);
+      if (A[j * kNL + i] != (Real)0.) {
+        const Real line = (Real)A[j * kNL + i] * ((Real)e[j] - (Real)e[i]) * (y[j] * inv);
+        if (!(fscale > (Real)0.)) cool += line;
+        else if (line * fscale > (Real)1e-35) cool += line * fscale;
+      }
   return cool;
 }
 

@@ -21,6 +21,8 @@
 // State between the kernels is structure-of-arrays over cells (coalesced).
 // The host issues the 25 possible T steps without synchronising: each
 // kernel reads the active count from device memory.
+#include <algorithm>
+
 #include "cellupdate.cuh"
 
 namespace mcg {
@@ -135,7 +137,10 @@ __global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ W
   }
 }
 
-// forbidden-line cooling per H of line ion `ion` in every active cell
+// forbidden-line cooling per H of line ion `ion` in every active cell.  The
+// level-population matrix of each thread is in local memory with the row
+// length of the largest ion (mat_rows): the fewer bytes a thread touches, the
+// more of the resident threads' matrices stay in the L1.
 __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ WaveArgs w, int cur) {
   const UpdArgs &a = w.a;
   const UpdTabs<float> &T = a.f;
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ W
     const float xi = XS(w, C.e * kNX + C.ion, c);
     const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
     float x[kNL * kNL];
-    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, kNL);
+    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows);
     w.cool[(size_t)k * (a.nc + 1) + c] = cool * T.ab[C.e] * xi * 1.9865e-16f;
   }
 }
@@ -268,6 +273,13 @@ __global__ void wave_reset_kernel(int *count, int slot) { count[slot] = 0; }
 
 }  // namespace
 
+// blocks per SM of the level-population kernels: as many as are resident
+int cel_blocks_per_sm() { return 32; }
+
+cudaError_t cell_update_fp32_prepare(const UpdArgs &) {
+  return cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+}
+
 size_t cell_update_fp32_scratch(int nc, int ncel) {
   const size_t nc1 = (size_t)nc + 1;
   // the arrays of launch_cell_update_fp32, each rounded up to 256 bytes
@@ -301,7 +313,7 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
     const int cur = t & 1;
     wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
     wave_ion_kernel<<<blocks, 128, 0, stream>>>(w, cur);
-    wave_cel_kernel<<<blocks * 4, 128, 0, stream>>>(w, cur);
+    wave_cel_kernel<<<num_sms * cel_blocks_per_sm(), 128, 0, stream>>>(w, cur);
     wave_therm_kernel<<<blocks, 128, 0, stream>>>(w, cur);
   }
   return cudaGetLastError();

@@ -95,6 +95,9 @@ struct UpdArgs {
 };
 cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int num_sms, cudaStream_t stream);
 cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream);
+// sets the cache preference of the FP32 form's kernels (before a capture)
+cudaError_t cell_update_fp32_prepare(const UpdArgs &a);
+int cel_blocks_per_sm();
 size_t cell_update_fp32_scratch(int nc, int ncel);
 cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const int *flags, const double *dte,
                                 UpdStatsDev *s, int num_sms, cudaStream_t stream);
@@ -136,6 +139,38 @@ cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A,
                                     const float *hit, float *tdust, int num_sms, cudaStream_t stream);
 
 cudaError_t launch_wave_round_control(const WaveLaunch &L, cudaGraphConditionalHandle h);
+
+// Diffuse-emission CDF (emission.cu): the tables derived from the frequency
+// grid on the host and the resident cell state they are applied to.
+constexpr int kEmiMaxBins = 4096, kEmiMaxLim = 32, kEmiMaxHeavy = 32;
+struct EmiArgs {
+  int nc, nb;
+  const double *te, *ne, *X;      // resident cell state [nc+1], [nc+1][7][8]
+  const float *forb;              // [ncel][nc+1] forbidden-line totals
+  int ncel;
+  const float *ab;                // [7] abundances (H He C N O Ne S)
+  const float *nu, *lnu, *wid;    // [nb]: frequency [Ryd], log10, cRyd widFlx / 1e15
+  const float *xs_h, *xs_hei, *xs_heii;        // [nb] ground-state cross-sections (Milne relation)
+  const float *tp_hi, *tp_hei, *tp_heii;       // [nb] two-photon spectral shapes
+  const int *pair;                // [3][nb] gamma edge pair covering each bin (-1: none)
+  int nlim[3];
+  const float *lg[3];             // [ntk][nlim] log10 gamma (HI, HeI, HeII)
+  const int *edge[3];             // [nlim] 0-based bins of the gamma edges
+  int ntk;
+  const float *tk;                // [ntk]
+  int p_from[3], p_milne[3];      // first bin of each Milne range; bin of each threshold
+  const float *gaunt_d;           // [8][11] Hummer's Chebyshev coefficients
+  int nheavy;
+  const int *h_e, *h_stage, *h_ip, *h_hi;      // element index, recombining stage, [ip, hi) bins
+  const float *h_g, *h_nuip, *xs_outer;        // g0/g1, nu at ip, [nheavy][nb] outer-shell cross-section
+  int j2, ly_bin[4];
+  float ly_data[4];
+  float hi_rec_sum, heii_rec_sum;
+  const float *hei_rec;           // [34][3][4] HeI line fits (first coefficient x 1e25)
+  float milne_c;                  // 4 pi h c Ryd (h^2 / 2 pi m k)^1.5 Ryd^2 1e40
+  float *rec_cdf, *total_lines;   // out: [nc+1][nb] rows, [nc+1]
+};
+cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int num_sms, cudaStream_t s);
 
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);

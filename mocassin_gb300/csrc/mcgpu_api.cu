@@ -128,6 +128,10 @@ struct mc_ctx {
   int m_step = 0, m_B = 0;
   bool m_ready = false, m_norm = false;
   double m_near_res = 0.3;  // warm start: residual / heating below which a prediction is bracketed
+  // diffuse-emission CDF: derived tables (one buffer) and forbidden-line totals
+  DBuf e_tab, e_forb;
+  mcg::EmiArgs emi{};
+  bool e_ready = false;
   bool u_ready = false, s_ready = false;
   // the FP32 update's launch sequence, captured once per argument set
   cudaGraphExec_t wave_exec = nullptr;
@@ -1264,6 +1268,33 @@ namespace {
 mc_status surrogate_predict_state(mc_ctx_t *c);
 }
 
+// The atomic tables and the resident cell state in the update's arguments.
+static void fill_update_tables(mc_ctx_t *c, mcg::UpdArgs &a) {
+  a.nc = c->nc;
+  a.ncel = c->u_ncel;
+  a.ndirec = c->u_ndirec;
+  a.naldro = c->u_naldro;
+  for (int i = 0; i < 7; ++i) { a.bal_z[i] = c->u_bal_z[i]; a.bal_first[i] = c->u_bal_first[i]; }
+  a.d.bal = c->u_bal.as<mcg::UpdIonDev>();
+  a.d.cel = c->u_cel.as<mcg::UpdCelDev>();
+  a.d.rrec = c->u_rrec.as<double>(); a.d.rnew = c->u_rnew.as<double>();
+  a.d.direc = c->u_direc.as<double>(); a.d.aldro = c->u_aldro.as<double>();
+  a.d.logt = c->u_logt.as<double>(); a.d.g = c->u_g.as<double>(); a.d.e = c->u_e.as<double>();
+  a.d.A = c->u_A.as<double>(); a.d.qq = c->u_qq.as<double>(); a.d.q2 = c->u_q2.as<double>();
+  a.d.ab = c->u_ab.as<double>();
+  a.f.bal = c->f_bal.as<mcg::UpdIonT<float>>();
+  a.f.cel = c->f_cel.as<mcg::UpdCelT<float>>();
+  a.f.rrec = c->f_rrec.as<float>(); a.f.rnew = c->f_rnew.as<float>();
+  a.f.direc = c->f_direc.as<float>(); a.f.aldro = c->f_aldro.as<float>();
+  a.f.logt = c->f_logt.as<float>(); a.f.g = c->f_g.as<float>(); a.f.e = c->f_e.as<float>();
+  a.f.A = c->f_A.as<float>(); a.f.qq = c->f_qq.as<float>(); a.f.q2 = c->f_q2.as<float>();
+  a.f.ab = c->f_ab.as<float>();
+  a.hden = c->u_hden.as<double>();
+  a.te = c->s_te.as<double>(); a.ne = c->s_ne.as<double>(); a.X = c->s_X.as<double>();
+  a.mat_rows = c->u_maxlev;
+  a.mat_stride = (c->u_maxlev * c->u_maxlev) | 1;
+}
+
 static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, double xhi_limit, int32_t precision,
                                    bool warm, mc_update_stats_t *stats) {
   if (!c || !w) return set_error(MC_ERR_ARG, "ctx and w are required");
@@ -1303,25 +1334,7 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   // a predicted Te is near the balance: bracket it with small steps first
   a.step0 = warm ? 1.03 : 1.2;
   a.step_grow = warm ? 1 : 0;
-  a.ncel = c->u_ncel;
-  a.ndirec = c->u_ndirec;
-  a.naldro = c->u_naldro;
-  for (int i = 0; i < 7; ++i) { a.bal_z[i] = c->u_bal_z[i]; a.bal_first[i] = c->u_bal_first[i]; }
-  a.d.bal = c->u_bal.as<mcg::UpdIonDev>();
-  a.d.cel = c->u_cel.as<mcg::UpdCelDev>();
-  a.d.rrec = c->u_rrec.as<double>(); a.d.rnew = c->u_rnew.as<double>();
-  a.d.direc = c->u_direc.as<double>(); a.d.aldro = c->u_aldro.as<double>();
-  a.d.logt = c->u_logt.as<double>(); a.d.g = c->u_g.as<double>(); a.d.e = c->u_e.as<double>();
-  a.d.A = c->u_A.as<double>(); a.d.qq = c->u_qq.as<double>(); a.d.q2 = c->u_q2.as<double>();
-  a.d.ab = c->u_ab.as<double>();
-  a.f.bal = c->f_bal.as<mcg::UpdIonT<float>>();
-  a.f.cel = c->f_cel.as<mcg::UpdCelT<float>>();
-  a.f.rrec = c->f_rrec.as<float>(); a.f.rnew = c->f_rnew.as<float>();
-  a.f.direc = c->f_direc.as<float>(); a.f.aldro = c->f_aldro.as<float>();
-  a.f.logt = c->f_logt.as<float>(); a.f.g = c->f_g.as<float>(); a.f.e = c->f_e.as<float>();
-  a.f.A = c->f_A.as<float>(); a.f.qq = c->f_qq.as<float>(); a.f.q2 = c->f_q2.as<float>();
-  a.f.ab = c->f_ab.as<float>();
-  a.hden = c->u_hden.as<double>();
+  fill_update_tables(c, a);
   a.mom = c->s_mom.as<float>();
   a.mstride = nc1;
   a.te = c->s_te.as<double>(); a.ne = c->s_ne.as<double>(); a.X = c->s_X.as<double>();
@@ -1342,6 +1355,7 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
                       std::memcmp(&c->wave_args, &a, sizeof a) == 0;
     if (!same) {
       if (c->wave_exec) { cudaGraphExecDestroy(c->wave_exec); c->wave_exec = nullptr; }
+      MC_CUDA(mcg::cell_update_fp32_prepare(a));
       cudaGraph_t graph = nullptr;
       MC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       cudaError_t ce = mcg::launch_cell_update(a, 1, c->s_wave.p, c->num_sms, s);
@@ -1678,6 +1692,252 @@ extern "C" mc_status mc_ctx_surrogate_grads(mc_ctx_t *c, int32_t m, const float 
   if (y) MC_CUDA(cudaMemcpyAsync(y, c->m_y.p, (size_t)m * kMlpOut * 4, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
   if (loss) *loss = l / ((double)m * mcg::kMlpTargets);
+  return MC_OK;
+}
+
+namespace {
+
+// locate (interpolation_mod.f90:48-81): 1-based index of the last entry <= x
+// (n above the grid, 0 below it, 1 for x equal to the last entry)
+int locate_host(const float *xa, int n, float x) {
+  if (x > xa[n - 1]) return n;
+  if (x < xa[0]) return 0;
+  for (int i = 0; i < n; ++i)
+    if (xa[i] > x) return std::max(i, 1);
+  return 1;
+}
+
+// HINuEdgeP & co. (initGammaCont, ph_mod.f90:135-197), 1-based
+std::vector<int> edge_pointers(const float *nu, int nb, const float *nug, int nlim) {
+  std::vector<int> p(nlim);
+  for (int i = 0; i < nlim; ++i) {
+    int k = locate_host(nu, nb, nug[i]);
+    if (k < nb && k >= 1 && nug[i] > (nu[k - 1] + nu[k]) / 2.f) ++k;
+    p[i] = k;
+  }
+  p[0] = 1;
+  return p;
+}
+
+// two-photon spectral distribution of a hydrogenic ion (hydro2phot,
+// emission_mod.f90:553-663) without its Te-dependent coefficient
+float hydro2phot_shape(float nu, int z) {
+  const float nu0 = z == 1 ? 0.7496f : 3.00f;
+  if (nu >= nu0) return 0.f;
+  const float y = nu / nu0, q = 4.f * y * (1.f - y);
+  const float ay0 = 202.0f * (y * (1 - y) * (1 - powf(q, 0.8f)) + 0.88f * powf(y * (1 - y), 1.53f) * powf(q, 0.8f));
+  const float z6 = (float)(z * z * z * z * z * z);
+  const float ay = z == 1 ? ay0 : z6 * 0.9994667f * ay0;
+  const float a2q = z == 1 ? 8.2249f : 8.226f * z6;
+  return 6.6262e-27f * y * ay / a2q * 1e27f;
+}
+
+}  // namespace
+
+extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_tables_t *t) {
+  if (!c || !t) return set_error(MC_ERR_ARG, "ctx and tables are required");
+  const int nb = c->nb;
+  if (t->nbins != nb) return set_error(MC_ERR_ARG, "emission tables: nbins %d, grid %d", t->nbins, nb);
+  if (nb > mcg::kEmiMaxBins) return set_error(MC_ERR_ARG, "emission tables: at most %d bins", mcg::kEmiMaxBins);
+  if (!t->nu || !t->wid_flx || !t->xs_h || !t->xs_hei || !t->xs_heii || !t->tk || !t->lg_hi || !t->lg_hei ||
+      !t->lg_heii || !t->nu_gamma_hi || !t->nu_gamma_hei || !t->nu_gamma_heii || !t->y_ay || !t->hi_rec ||
+      !t->heii_rec || !t->heii_lyman || !t->hei_rec || !t->gaunt_dd || (t->n_heavy > 0 && (!t->heavy || !t->xs_outer)))
+    return set_error(MC_ERR_ARG, "emission tables: an array is missing");
+  const int nlim[3] = {t->nlim_hi, t->nlim_hei, t->nlim_heii};
+  for (int k = 0; k < 3; ++k)
+    if (nlim[k] < 2 || nlim[k] > mcg::kEmiMaxLim || (nlim[k] & 1))
+      return set_error(MC_ERR_ARG, "emission tables: gamma limits must be even, 2..%d", mcg::kEmiMaxLim);
+  if (nlim[0] + nlim[1] + nlim[2] > 64) return set_error(MC_ERR_ARG, "emission tables: at most 64 gamma limits");
+  if (t->ntk < 2 || t->n_heavy < 0 || t->n_heavy > mcg::kEmiMaxHeavy)
+    return set_error(MC_ERR_ARG, "emission tables: ntk >= 2 and n_heavy <= %d required", mcg::kEmiMaxHeavy);
+  const float *nu = t->nu;
+  for (int i = 1; i < nb; ++i)
+    if (!(nu[i] > nu[i - 1])) return set_error(MC_ERR_ARG, "emission tables: nu must increase");
+  // everything derived goes into one float/int buffer
+  std::vector<float> F;
+  std::vector<int> I;
+  auto putf = [&](const float *p, size_t n) { size_t o = F.size(); F.insert(F.end(), p, p + n); return o; };
+  std::vector<float> lnu(nb), wid(nb), tph(nb), tphe(nb), tpheii(nb);
+  for (int i = 0; i < nb; ++i) {
+    lnu[i] = log10f(nu[i]);
+    wid[i] = 3.2898423e15f * t->wid_flx[i] / 1.e15f;
+    tph[i] = hydro2phot_shape(nu[i], 1);
+    tpheii[i] = hydro2phot_shape(nu[i], 2);
+  }
+  // HeI 2^1S -> 1^1S (HeI2photSub, emission_mod.f90:665-705): the table
+  // pointer moves on by at most one entry per bin
+  {
+    const float *ya = t->y_ay;
+    int j = 1;
+    for (int i = 0; i < nb; ++i) {
+      const float y = nu[i] / 1.514f;
+      if (y > ya[2 * (j - 1)]) ++j;
+      if (j >= 41) break;
+      const float fit1 = (ya[2 * j + 1] - ya[2 * (j - 1) + 1]) / (ya[2 * j] - ya[2 * (j - 1)]);
+      const float fit2 = ya[2 * (j - 1) + 1] - ya[2 * (j - 1)] * fit1;
+      float ay = fit1 * y + fit2;
+      if (ay < 9.2163086E-03f) ay = 0.f;
+      tphe[i] = ay * 0.66262f * y / 51.3f;
+    }
+  }
+  const size_t o_nu = putf(nu, nb), o_lnu = putf(lnu.data(), nb), o_wid = putf(wid.data(), nb);
+  const size_t o_xh = putf(t->xs_h, nb), o_xhei = putf(t->xs_hei, nb), o_xheii = putf(t->xs_heii, nb);
+  const size_t o_tph = putf(tph.data(), nb), o_tphe = putf(tphe.data(), nb), o_tpheii = putf(tpheii.data(), nb);
+  const size_t o_tk = putf(t->tk, t->ntk);
+  const float *lgs[3] = {t->lg_hi, t->lg_hei, t->lg_heii};
+  const float *nug[3] = {t->nu_gamma_hi, t->nu_gamma_hei, t->nu_gamma_heii};
+  size_t o_lg[3], o_edge[3];
+  std::vector<int> pair(3 * (size_t)nb, -1);
+  int last_edge[3];
+  for (int k = 0; k < 3; ++k) {
+    o_lg[k] = putf(lgs[k], (size_t)t->ntk * nlim[k]);
+    const std::vector<int> ep = edge_pointers(nu, nb, nug[k], nlim[k]);
+    for (int p = 0; p < nlim[k] / 2; ++p) {
+      const int ilow = ep[2 * p], iup = ep[2 * p + 1];
+      if (iup == ilow || ilow < 1 || iup > nb)
+        return set_error(MC_ERR_ARG, "emission tables: frequency grid too coarse for gamma edge %d", 2 * p + 1);
+      for (int j = ilow; j <= iup - 1; ++j) pair[(size_t)k * nb + j - 1] = p;
+    }
+    o_edge[k] = I.size();
+    for (int v : ep) I.push_back(v - 1);
+    last_edge[k] = ep[nlim[k] - 1];
+  }
+  const size_t o_pair = I.size();
+  I.insert(I.end(), pair.begin(), pair.end());
+  std::vector<float> d(88);
+  for (int j = 0; j < 8; ++j)
+    for (int k = 0; k < 11; ++k) d[j * 11 + k] = (float)t->gaunt_dd[k * 8 + j];  // d(8, 11) column-major
+  const size_t o_gd = putf(d.data(), 88);
+  const int nh = t->n_heavy;
+  std::vector<int> he(nh), hs(nh), hip(nh), hhi(nh);
+  std::vector<float> hg(nh), hnu(nh);
+  for (int h = 0; h < nh; ++h) {
+    const int32_t *r = t->heavy + 8 * h;
+    const int e = elem_index(r[0]);
+    if (e < 2 || r[1] < 1 || r[1] > 6 || r[4] < 1 || r[5] < 1 || r[6] < 1 || r[6] > nb || r[7] < 1 || r[7] > nb)
+      return set_error(MC_ERR_ARG, "emission tables: heavy ion row %d", h);
+    he[h] = e;
+    hs[h] = r[1] + 1;
+    hg[h] = (float)r[4] / (float)r[5];
+    hip[h] = r[6] - 1;
+    hhi[h] = r[7] - 1;
+    hnu[h] = nu[r[6] - 1];
+  }
+  const size_t o_he = I.size();
+  I.insert(I.end(), he.begin(), he.end());
+  const size_t o_hs = I.size();
+  I.insert(I.end(), hs.begin(), hs.end());
+  const size_t o_hip = I.size();
+  I.insert(I.end(), hip.begin(), hip.end());
+  const size_t o_hhi = I.size();
+  I.insert(I.end(), hhi.begin(), hhi.end());
+  const size_t o_hg = putf(hg.data(), nh), o_hnu = putf(hnu.data(), nh);
+  const size_t o_xso = putf(t->xs_outer, (size_t)nh * nb);
+  const size_t o_hei = putf(t->hei_rec, 34 * 3 * 4);
+  float hi_sum = 0.f, heii_sum = 0.f;
+  for (int iup = 3; iup <= 15; ++iup)
+    for (int ilow = 2; ilow <= std::min(8, iup - 1); ++ilow) hi_sum += t->hi_rec[iup * 9 + ilow];
+  for (int iup = 3; iup <= 30; ++iup)
+    for (int ilow = 2; ilow <= std::min(16, iup - 1); ++ilow) heii_sum += t->heii_rec[iup * 17 + ilow];
+  // one buffer: floats first, then ints (both 4-byte)
+  const size_t nf = F.size();
+  if (c->e_tab.bytes != (nf + I.size()) * 4) {
+    if (c->e_tab.p) { cudaFree(c->e_tab.p); c->e_tab.p = nullptr; c->e_tab.bytes = 0; }
+    MC_CUDA(c->e_tab.alloc((nf + I.size()) * 4));
+  }
+  cudaStream_t s = c->stream;
+  MC_CUDA(cudaMemcpyAsync(c->e_tab.p, F.data(), nf * 4, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaMemcpyAsync((char *)c->e_tab.p + nf * 4, I.data(), I.size() * 4, cudaMemcpyHostToDevice, s));
+  MC_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  const float *fb = c->e_tab.as<float>();
+  const int *ib = (const int *)(fb + nf);
+  mcg::EmiArgs &E = c->emi;
+  E = mcg::EmiArgs{};
+  E.nb = nb;
+  E.nu = fb + o_nu; E.lnu = fb + o_lnu; E.wid = fb + o_wid;
+  E.xs_h = fb + o_xh; E.xs_hei = fb + o_xhei; E.xs_heii = fb + o_xheii;
+  E.tp_hi = fb + o_tph; E.tp_hei = fb + o_tphe; E.tp_heii = fb + o_tpheii;
+  E.pair = ib + o_pair;
+  for (int k = 0; k < 3; ++k) { E.nlim[k] = nlim[k]; E.lg[k] = fb + o_lg[k]; E.edge[k] = ib + o_edge[k]; }
+  E.ntk = t->ntk;
+  E.tk = fb + o_tk;
+  const int pH = locate_host(nu, nb, 0.99946f), pHeI = locate_host(nu, nb, 1.80802f), pHeII = locate_host(nu, nb, 4.0f);
+  if (pH < 1 || pHeI < 1 || pHeII < 1) return set_error(MC_ERR_ARG, "emission tables: thresholds below the grid");
+  E.p_milne[0] = pH - 1; E.p_milne[1] = pHeI - 1; E.p_milne[2] = pHeII - 1;
+  // the HeI and HeII Milne ranges nest inside the HI one (fb_ff :438-470)
+  E.p_from[0] = pH - 1;
+  E.p_from[1] = std::max(pH, last_edge[1]) - 1;
+  E.p_from[2] = std::max(E.p_from[1] + 1, last_edge[2]) - 1;
+  E.gaunt_d = fb + o_gd;
+  E.nheavy = nh;
+  E.h_e = ib + o_he; E.h_stage = ib + o_hs; E.h_ip = ib + o_hip; E.h_hi = ib + o_hhi;
+  E.h_g = fb + o_hg; E.h_nuip = fb + o_hnu; E.xs_outer = fb + o_xso;
+  E.j2 = locate_host(nu, nb, 1.45673f) - 1;
+  for (int i = 0; i < 4; ++i) {
+    E.ly_bin[i] = locate_host(nu, nb, t->heii_lyman[2 * i + 1]) - 1;
+    E.ly_data[i] = t->heii_lyman[2 * i];
+  }
+  E.hi_rec_sum = hi_sum;
+  E.heii_rec_sum = heii_sum;
+  E.hei_rec = fb + o_hei;
+  // fourPi hcRyd constant 1e20 1e20 of fb_ff (:429-527), formed in FP64 (1e40 is not an FP32 number)
+  E.milne_c = (float)((double)(4.f * 3.141592654f) * 2.1799153e-11 * (double)4.9874105e-6f * 1e40);
+  c->e_ready = true;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is required");
+  if (!c->e_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_emission_tables has not been called");
+  if (!c->u_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_update_tables has not been called");
+  if (!c->s_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_cell_state has not been called");
+  const int nc1 = c->nc + 1, nb = c->nb;
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = put_buf(c->e_forb, nullptr, (size_t)std::max(c->u_ncel, 1) * nc1 * sizeof(float), s))) return st;
+  if (!c->rec_cdf.p) {
+    MC_CUDA(c->rec_cdf.alloc((size_t)nc1 * nb * sizeof(float)));
+    std::vector<float> one(nb, 1.f);  // row 0 (outside the nebula) is never sampled
+    MC_CUDA(cudaMemcpyAsync(c->rec_cdf.p, one.data(), nb * sizeof(float), cudaMemcpyHostToDevice, s));
+    MC_CUDA(cudaStreamSynchronize(s));
+    c->g.rec_cdf = c->rec_cdf.as<float>();
+  }
+  if (!c->tlines.p) {
+    MC_CUDA(c->tlines.alloc((size_t)nc1 * sizeof(float)));
+    MC_CUDA(cudaMemsetAsync(c->tlines.p, 0, (size_t)nc1 * sizeof(float), s));
+    c->g.total_lines = c->tlines.as<float>();
+  }
+  mcg::UpdArgs a{};
+  fill_update_tables(c, a);
+  mcg::EmiArgs E = c->emi;
+  E.nc = c->nc;
+  E.te = c->s_te.as<double>(); E.ne = c->s_ne.as<double>(); E.X = c->s_X.as<double>();
+  E.forb = c->e_forb.as<float>();
+  E.ncel = c->u_ncel;
+  E.ab = c->f_ab.as<float>();
+  E.rec_cdf = c->rec_cdf.as<float>();
+  E.total_lines = c->tlines.as<float>();
+  MC_CUDA(cudaEventRecord(c->ev0, s));
+  cudaError_t e = mcg::launch_emission(a, E, c->e_forb.as<float>(), c->num_sms, s);
+  if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "emission launch failed: %s", cudaGetErrorString(e));
+  MC_CUDA(cudaEventRecord(c->ev1, s));
+  MC_CUDA(cudaEventSynchronize(c->ev1));
+  if (ms) MC_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_get_emission(mc_ctx_t *c, float *rec_rows, float *total_lines) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is required");
+  const size_t nc1 = (size_t)c->nc + 1;
+  if (rec_rows) {
+    if (!c->rec_cdf.p) return set_error(MC_ERR_ARG, "no emission CDF on the device");
+    MC_CUDA(cudaMemcpyAsync(rec_rows, c->rec_cdf.p, nc1 * c->nb * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (total_lines) {
+    if (!c->tlines.p) return set_error(MC_ERR_ARG, "no totalLines on the device");
+    MC_CUDA(cudaMemcpyAsync(total_lines, c->tlines.p, nc1 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  MC_CUDA(cudaStreamSynchronize(c->stream));
   return MC_OK;
 }
 

@@ -11,9 +11,14 @@ Each iteration runs, on the grid resident in HBM,
      minConvergence (95 %, set_input_mod.f90:105; test :1135), at most
      maxIterateMC (30) iterations,
   4. the opacity of the next transport from the new ion densities
-     (ionizationDriver, ionization_mod.f90:26-129, on the tensor cores).
-The re-emission CDFs (recPDF) stay those of the input grid: the emission
-step (emission_mod.f90:905-1311) is not part of this path.
+     (ionizationDriver, ionization_mod.f90:26-129, on the tensor cores),
+  5. the re-emission CDFs of the next transport (recPDF rows and totalLines,
+     emissionDriver / setDiffusePDF, emission_mod.f90:32-1311, on the GPU),
+     built from the initial state before the first transport too, as the
+     reference builds them at the top of every iteration.  ``emission``
+     "auto" does this for a gas-only grid; a grid with dust keeps the input
+     CDFs (the dust emission of setDiffusePDF / setDustPDF is not on this
+     path).
 
 ``form`` picks the transport ("graph": the frequency-sorted persistent march
 with its rounds in one CUDA graph; "wave": the same with host-driven rounds;
@@ -37,7 +42,8 @@ def _ions():
 class LambdaIteration:
     """A nebula resident on the GPU with its cell state."""
 
-    def __init__(self, neb, form="graph", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None):
+    def __init__(self, neb, form="graph", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None,
+                 emission="auto"):
         """surrogate: None (updates start from the previous state, as the
         reference's) or a dict with train_after (cold iterations whose cell
         states train the MLP first), steps, batch, lr, finetune_steps (after
@@ -51,6 +57,12 @@ class LambdaIteration:
         self.ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
         te, ne, X = balance.initial_state(neb)
         self.ctx.set_cell_state(te, ne, X)
+        if emission == "auto":
+            emission = not (neb.flags & nebula.FLAG_DUST)
+        self.emission = bool(emission)
+        if self.emission:
+            self.ctx.set_emission_tables()
+            self.ctx.build_emission()
         self.species = _ions()
         self.w = balance.moment_weights(neb.xs, neb.nu, self.species)
         self.scale = 1e-9 / (8.0 if neb.flags & nebula.FLAG_SYMMETRIC_XYZ else 1.0)
@@ -82,12 +94,14 @@ class LambdaIteration:
                                                           0.3 * self.sur["lr"], self.sur["seed"])
         t2b = time.perf_counter()
         op_ms = self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
+        em_ms = self.ctx.build_emission() if self.emission else 0.0
         t3 = time.perf_counter()
         rec = {"iteration": len(self.history) + 1, "transport_s": t1 - t0, "update_s": t2 - t1,
                "surrogate_s": t2b - t2, "surrogate_train_ms": train_ms, "surrogate_loss": loss, "warm": warm,
                "opacity_s": t3 - t2b,
                "wall_s": t3 - t0, "crossings": tr["crossings"], "transport_kernel_ms": tr["kernel_ms"],
                "update_ms": up["update_ms"], "moments_ms": up["moments_ms"], "opacity_ms": op_ms,
+               "emission_ms": em_ms,
                "hit": up["hit"], "converged_pct": 100.0 * up["converged"] / max(up["hit"], 1),
                "dte_lt_1pc_pct": 100.0 * up["frac_dte_1pc"], "t_steps_per_cell": up["t_iterations"] / max(up["hit"], 1),
                "no_te_balance": up["no_te_balance"], "no_ion_balance": up["no_ion_balance"],
@@ -121,6 +135,8 @@ class LambdaIteration:
             raise ValueError("the snapshot is of another grid")
         self.ctx.set_cell_state(g["te"], g["ne"], g["X"])
         self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
+        if self.emission:
+            self.ctx.build_emission()
 
     def close(self):
         self.ctx.close()

@@ -62,6 +62,12 @@ def library():
         ip = C.POINTER(C.c_int32)
         lib.mc_ctx_set_update_tables.restype = C.c_int
         lib.mc_ctx_set_update_tables.argtypes = [C.c_void_p, C.POINTER(abi.McUpdateTables), dp, dp]
+        lib.mc_ctx_set_emission_tables.restype = C.c_int
+        lib.mc_ctx_set_emission_tables.argtypes = [C.c_void_p, C.POINTER(abi.McEmissionTables)]
+        lib.mc_ctx_build_emission.restype = C.c_int
+        lib.mc_ctx_build_emission.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+        lib.mc_ctx_get_emission.restype = C.c_int
+        lib.mc_ctx_get_emission.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.mc_ctx_set_cell_state.restype = C.c_int
         lib.mc_ctx_set_cell_state.argtypes = [C.c_void_p, dp, dp, dp]
         lib.mc_ctx_get_cell_state.restype = C.c_int
@@ -260,6 +266,29 @@ class TransportContext:
         h = np.ascontiguousarray(hden, dtype=np.float64)
         a = np.ascontiguousarray(abund, dtype=np.float64)
         _check(self.lib.mc_ctx_set_update_tables(self.handle, C.byref(self._ut), _dptr(h), _dptr(a)))
+
+    def set_emission_tables(self, tables=None):
+        """Uploads the diffuse-emission tables (mocassin_gb300.emission.tables()
+        by default) for build_emission."""
+        from . import emission
+        t = emission.tables(self.neb) if tables is None else tables
+        self._et = abi.emission_tables_struct(t)
+        _check(self.lib.mc_ctx_set_emission_tables(self.handle, C.byref(self._et)))
+
+    def build_emission(self):
+        """Rebuilds every cell's recPDF row and totalLines on the GPU from the
+        resident cell state; returns the device time [ms]."""
+        ms = C.c_float()
+        _check(self.lib.mc_ctx_build_emission(self.handle, C.byref(ms)))
+        return ms.value
+
+    def get_emission(self):
+        """The CDF rows (Nc+1, nbins) and totalLines (Nc+1,) on the device."""
+        nc1, nb = self.neb.ncells + 1, self.neb.nbins
+        rows = np.empty((nc1, nb), dtype=np.float32)
+        tl = np.empty(nc1, dtype=np.float32)
+        _check(self.lib.mc_ctx_get_emission(self.handle, rows.ctypes.data, tl.ctypes.data))
+        return rows, tl
 
     def set_cell_state(self, te, ne, X):
         te = np.ascontiguousarray(te, dtype=np.float64)

@@ -241,7 +241,11 @@ struct Cell {
 
   // forbidden-line emissivities of one ion (equilibrium), summed over the
   // transitions among levels 1..10 that thermBalance adds up [erg/s per ion]
-  double celCooling(int k, double ionDenUp) const {
+  // Forbidden-line cooling of line ion k: sum over the transitions among
+  // levels 1..top of A(j,i) (E_j - E_i) n_j (thermBalance, top = 10).  With
+  // fscale > 0 every line is scaled by fscale and only lines above 1e-35
+  // count (setDiffusePDF's normFor over forbiddenLines, top = all levels).
+  double celCooling(int k, double ionDenUp, int top_levels = 10, double fscale = 0.) const {
     if (ionDenUp != ionDenUp) return 0.;
     const int n = t->cel_nlev[k], nt = t->cel_ntemp[k];
     const double *logt = t->cel_logt + (size_t)k * kNT;
@@ -341,10 +345,14 @@ struct Cell {
     double sumN = 0.;
     for (int i = 1; i <= n; ++i) sumN += y[i];
     double cool = 0.;
-    const int top = std::min(n, 10);
+    const int top = std::min(n, top_levels);
     for (int i = 1; i <= top - 1; ++i)
       for (int j = i + 1; j <= top; ++j)
-        if (A(j, i) != 0.) cool += A(j, i) * (e[j] - e[i]) * (y[j] / sumN);
+        if (A(j, i) != 0.) {
+          const double line = A(j, i) * (e[j] - e[i]) * (y[j] / sumN);
+          if (fscale <= 0.) cool += line;
+          else if (line * fscale > 1e-35) cool += line * fscale;
+        }
     return cool;
   }
 
@@ -497,6 +505,32 @@ int oracle_update_pieces(const upd_tables_t *t, const double *abund, double hden
     cel_out[k] = C.celCooling(k, up);
   }
   C.thermBalance(heat_cool[0], heat_cool[1]);
+  return 0;
+}
+
+// setDiffusePDF's forbidden-line totals (forLines, emission_mod.f90:837-903,
+// and normFor, :1151-1172): per line ion k, the sum of its line
+// emissivities [1e-25 erg/s per H] at Te, Ne and the ionic fractions, lines
+// above 1e-35 only.  Ne below 1e-5 is taken as 1e-5 (emissionDriver :86-88).
+int oracle_forbidden_lines(const upd_tables_t *t, const double *abund, double te, double ne, const double *ionden,
+                           double *out) {
+  Cell C;
+  C.t = t;
+  C.ab = abund;
+  C.hden = 0.;
+  C.photo = nullptr;
+  C.heat = nullptr;
+  C.Te = te;
+  C.Ne = ne < 1e-5 ? 1e-5 : ne;
+  for (int e = 0; e < kNE; ++e)
+    for (int s = 0; s <= kNS; ++s) C.X[e][s] = ionden[e * (kNS + 1) + s];
+  for (int k = 0; k < t->ncel; ++k) {
+    const int z = t->cel_key[2 * k], ion = t->cel_key[2 * k + 1];
+    int e = 0;
+    while (e < kNE && kZ[e] != z) ++e;
+    const double up = ion < kNS ? C.X[e][ion + 1] / C.X[e][ion] : 0.;
+    out[k] = C.celCooling(k, up, 1 << 20, abund[e] * C.X[e][ion] * 1.9865e9);
+  }
   return 0;
 }
 

@@ -122,3 +122,22 @@ def pieces(tables, abund, hden, photo, heat, te, ne, X):
                              he.ctypes.data_as(_dp), C.c_double(te), C.c_double(ne), Xc.ctypes.data_as(_dp),
                              alpha.ctypes.data_as(_dp), cel.ctypes.data_as(_dp), hc.ctypes.data_as(_dp))
     return alpha, cel, hc
+
+
+def forbidden_lines(tables, abund, te, ne, X):
+    """Per cell and line ion, the summed forbidden-line emissivity
+    [1e-25 erg/s per H] of setDiffusePDF's normFor (lines above 1e-35), at the
+    cells' Te [n], Ne [n] and ionic fractions X [n][7][8]; returns [n][ncel]."""
+    lib = library()
+    lib.oracle_forbidden_lines.restype = C.c_int
+    t = marshal(tables)
+    ab = np.ascontiguousarray(abund, dtype=np.float64)
+    te = np.asarray(te, dtype=np.float64)
+    ne = np.asarray(ne, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    n = len(te)
+    out = np.zeros((n, len(tables["cel_key"])))
+    for c in range(n):
+        lib.oracle_forbidden_lines(C.byref(t), ab.ctypes.data_as(_dp), C.c_double(te[c]), C.c_double(ne[c]),
+                                   X[c].ctypes.data_as(_dp), out[c].ctypes.data_as(_dp))
+    return out
