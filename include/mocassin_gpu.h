@@ -336,6 +336,11 @@ mc_status mc_ctx_update_cells(mc_ctx_t *ctx, const float *w, double scale, doubl
  * ionden(elem_k, stage_k) * abund(elem_k) * Hden(cell) for the nspecies rows
  * (elem, stage) = species[k], then the contraction with xs [nspecies][nbins]
  * as mc_ctx_build_opacity. */
+/* Opacity rows that do not follow the cell state, appended to every
+ * mc_ctx_opacity_from_state contraction: den [nrows][Nc+1] (e.g. Ndust) and
+ * xs [nrows][nbins] (e.g. the grains' absorption + scattering per grain,
+ * the dust add of iteration_mod.f90:166-227); nrows 0 removes them. */
+mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *ctx, int32_t nrows, const float *den, const float *xs);
 mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32_t *species, const float *xs,
                                     int32_t method, double *kernel_ms);
 
@@ -395,15 +400,28 @@ typedef struct mc_emission_tables {
   const int32_t *heavy;      /* [n_heavy][8]: z, ion, nElec, outShell, g0, g1,
                                 IPnuP, highNuP (1-based bins)                  */
   const float *xs_outer;     /* [n_heavy][nbins] outer-shell cross-section     */
+  /* grains (0 sizes: no dust terms).  The grain temperatures are the ones
+   * mc_ctx_dust_temperatures left on the device (none yet: no dust emission). */
+  int32_t n_sizes;           /* grain size bins of the one species (<= 16)     */
+  const float *xs_abs;       /* [n_sizes][nbins] absorption cross-section per
+                                grain [cm^2] (xSecArray at dustAbsXsecP)       */
+  const float *grain_weight; /* [n_sizes] grainWeight x grainAbun             */
+  float t_sublime;           /* TdustSublime [K]                               */
+  const float *ndust;        /* [Nc+1] grains per cm^3 (Ndust)                 */
 } mc_emission_tables_t;
 
 mc_status mc_ctx_set_emission_tables(mc_ctx_t *ctx, const mc_emission_tables_t *tables);
 /* Builds every cell's emission CDF from the resident Te, Ne and ionic
  * fractions (needs mc_ctx_set_update_tables for the forbidden lines and the
- * abundances, and a cell state); ms = device time, or NULL. */
+ * abundances, and a cell state); ms = device time, or NULL.  With grains and
+ * grain temperatures: on a gas grid the thermal grain emission joins the
+ * recPDF rows (sumDiffuseDust, emission_mod.f90:1042-1105); on a dust-only
+ * grid the dustPDF rows are built instead (setDustPDF, :1313-1387). */
 mc_status mc_ctx_build_emission(mc_ctx_t *ctx, float *ms);
 /* Downloads the CDF rows [Nc+1][nbins] and totalLines [Nc+1] (either NULL). */
 mc_status mc_ctx_get_emission(mc_ctx_t *ctx, float *rec_rows, float *total_lines);
+/* Downloads the dust-emission CDF rows [Nc+1][nbins] (dust-only grids). */
+mc_status mc_ctx_get_dust_emission(mc_ctx_t *ctx, float *dust_rows);
 /* Parameters (33072 floats: W1[128][80] b1 W2[128][128] b2 W3[48][128] b3). */
 mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
 /* Loss and gradients of one batch (x [m][80], normalised targets t [m][48];

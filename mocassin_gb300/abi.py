@@ -76,7 +76,8 @@ class McEmissionTables(C.Structure):
                 ("nlim_heii", C.c_int32), ("nu_gamma_hi", _fp), ("nu_gamma_hei", _fp), ("nu_gamma_heii", _fp),
                 ("lg_hi", _fp), ("lg_hei", _fp), ("lg_heii", _fp), ("y_ay", _fp), ("hi_rec", _fp),
                 ("heii_rec", _fp), ("heii_lyman", _fp), ("hei_rec", _fp), ("gaunt_dd", _dp), ("n_heavy", C.c_int32),
-                ("heavy", _ip), ("xs_outer", _fp)]
+                ("heavy", _ip), ("xs_outer", _fp), ("n_sizes", C.c_int32), ("xs_abs", _fp), ("grain_weight", _fp),
+                ("t_sublime", C.c_float), ("ndust", _fp)]
 
 
 def emission_tables_struct(t):
@@ -99,6 +100,10 @@ def emission_tables_struct(t):
                          lg_heii=f("lg_heii"), y_ay=f("y_ay"), hi_rec=f("hi_rec"), heii_rec=f("heii_rec"),
                          heii_lyman=f("heii_lyman"), hei_rec=f("hei_rec"), gaunt_dd=dd.ctypes.data_as(_dp),
                          n_heavy=len(hv), heavy=hv.ctypes.data_as(_ip), xs_outer=f("xs_outer"))
+    if t.get("xs_abs") is not None:
+        s.n_sizes = len(t["grain_weight"])
+        s.xs_abs, s.grain_weight, s.ndust = f("xs_abs"), f("grain_weight"), f("ndust")
+        s.t_sublime = float(t["t_sublime"])
     s._keep = keep
     return s
 
@@ -169,7 +174,10 @@ class Marshalled:
         g.sca_opac = _ptr(f(neb.sca_opac), C.c_float)
         g.rec_pdf = _ptr(f(neb.rec_pdf), C.c_float)
         g.total_lines = _ptr(f(neb.total_lines), C.c_float)
-        g.dust_pdf = _ptr(None, C.c_float)
+        # a dust-only grid (no lgGas) re-emits from its dustPDF rows, which the
+        # nebula carries in rec_pdf
+        dust_only = not (neb.flags & (1 << 1))
+        g.dust_pdf = _ptr(f(neb.rec_pdf) if dust_only else None, C.c_float)
         g.nu_array = _ptr(f(neb.nu), C.c_float)
         g.g_sca = _ptr(f(neb.g_sca), C.c_float)
         for i in range(3):

@@ -51,20 +51,49 @@ __global__ void __launch_bounds__(128) emission_forb_kernel(const __grid_constan
 
 __device__ __forceinline__ float pow10f(float x) { return exp10f(x); }
 
+// getFlux(energy, T, 'blackbody') (continuum_mod.f90:359-394): the Planck
+// function over h, with the Wien and Rayleigh-Jeans branches
+__device__ __forceinline__ float planck_over_h(float nu, float T) {
+  const float hp = 6.6262e-27f, constant = 0.5250229f / hp;
+  const float u = kHcRydK * nu / T;
+  if (u > 86.f) return constant * nu * nu * nu * expf(-u);
+  const float den = expf(u) - 1.f;
+  if (den <= 0.f) return 3.32154e-6f * nu * nu * T / hp;
+  return constant * nu * nu * nu / den;
+}
+
 __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_constant__ EmiArgs E) {
   extern __shared__ float s_row[];  // [nb]
   __shared__ float s_lg[3][kEmiMaxLim], s_afit[3][kEmiMaxLim / 2], s_gc[2][8], s_w[kEmiMaxHeavy];
   __shared__ float s_scan[kEmiThreads / 32];
   __shared__ float s_par[16];
+  __shared__ float s_td[kEmiMaxSizes];
   const int nb = E.nb, t = threadIdx.x;
   const int chunk = (nb + kEmiThreads - 1) / kEmiThreads;
   for (int c = 1 + blockIdx.x; c <= E.nc; c += gridDim.x) {
-    const double *Xc = E.X + (size_t)c * kNE * kNX;
-    const float Te = (float)E.te[c];
-    const float Ne = fmaxf((float)E.ne[c], 1e-5f);
+    const double *Xc = E.gas ? E.X + (size_t)c * kNE * kNX : nullptr;
+    const float Te = E.gas ? (float)E.te[c] : 1e4f;
+    const float Ne = E.gas ? fmaxf((float)E.ne[c], 1e-5f) : 1.f;
     const float sq = sqrtf(Te), l10 = log10f(Te), t4 = Te * 1e-4f, kT = kHcRydK / Te;
+    const bool dust = E.nsizes > 0 && E.tdust != nullptr;
+    if (dust && t < E.nsizes) s_td[t] = E.tdust[(size_t)(1 + t) * (E.nc + 1) + c];
+    if (!E.gas) {
+      // dust-only grid: setDustPDF (emission_mod.f90:1313-1387)
+      __syncthreads();
+      for (int b = t; b < nb; b += kEmiThreads) {
+        const float nu = E.nu[b];
+        float sd = 0.f;
+        for (int ai = 0; ai < E.nsizes; ++ai) {
+          const float T = s_td[ai];
+          if (T > 0.f && T < E.t_sub)
+            sd += E.xs_abs[(size_t)ai * nb + b] * planck_over_h(nu, T) * E.widflx[b] * E.gw[ai];
+        }
+        s_row[b] = sd;
+      }
+    }
     // ---- per-cell coefficients ----
-    if (t < E.nlim[0] + E.nlim[1] + E.nlim[2]) {
+    if (!E.gas) {
+    } else if (t < E.nlim[0] + E.nlim[1] + E.nlim[2]) {
       int sidx = 0, i = t;
       while (i >= E.nlim[sidx]) { i -= E.nlim[sidx]; ++sidx; }
       const float *lg = E.lg[sidx];
@@ -147,7 +176,7 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
       }
     }
     __syncthreads();
-    if (t < (E.nlim[0] + E.nlim[1] + E.nlim[2]) / 2) {
+    if (E.gas && t < (E.nlim[0] + E.nlim[1] + E.nlim[2]) / 2) {
       int sidx = 0, p = t;
       while (p >= E.nlim[sidx] / 2) { p -= E.nlim[sidx] / 2; ++sidx; }
       const int iup = E.edge[sidx][2 * p + 1], ilow = E.edge[sidx][2 * p];
@@ -155,14 +184,19 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
     }
     __syncthreads();
     // ---- one thread per bin ----
-    const float xH2 = (float)Xc[2], xHe2 = (float)Xc[kNX + 2], xHe3 = (float)Xc[kNX + 3];
-    const float fH = E.ab[0] * xH2 * Ne, fHeI = E.ab[1] * xHe2 * Ne, fHeII = E.ab[1] * xHe3 * Ne;
+    // the thermal grain emission of a gas grid (sumDiffuseDust, :1042-1105)
+    const float dfac = dust && E.gas ? 6.6262e-27f * 4.f * 3.141592654f * 1e25f * 3.2898423e15f * E.ndust[c] / (float)E.hden[c]
+                            : 0.f;
+    const float xH2 = E.gas ? (float)Xc[2] : 0.f, xHe2 = E.gas ? (float)Xc[kNX + 2] : 0.f;
+    const float xHe3 = E.gas ? (float)Xc[kNX + 3] : 0.f;
+    const float abH = E.gas ? E.ab[0] : 0.f, abHe = E.gas ? E.ab[1] : 0.f;
+    const float fH = abH * xH2 * Ne, fHeI = abHe * xHe2 * Ne, fHeII = abHe * xHe3 * Ne;
     const float xlrkt = 5.1983649f - fminf(fmaxf(l10, 2.5f), 8.f);
     const float con = 0.72727273f * xlrkt + 0.90909091f;
     float gam2[2];
     for (int z = 0; z < 2; ++z) gam2[z] = pow10f(0.66666667f * (2.f * (z ? 0.30103f : 0.f) + xlrkt) * 1.5f);
     const float cm = E.milne_c / (Te * sq);
-    for (int b = t; b < nb; b += kEmiThreads) {
+    for (int b = t; E.gas && b < nb; b += kEmiThreads) {
       const float nu = E.nu[b];
       const float nu3 = nu * nu * nu;
       float g[3];
@@ -219,7 +253,16 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
       if (b == E.j2) sHeI += s_par[1];
       for (int i = 0; i < 4; ++i)
         if (b == E.ly_bin[i]) sHeII += s_par[2 + i];
-      s_row[b] = w * eHI + sHeI + sHeII;
+      float sd = 0.f;
+      if (dust) {
+        for (int ai = 0; ai < E.nsizes; ++ai) {
+          const float T = s_td[ai];
+          if (T < E.t_sub && T > 0.f)
+            sd += E.xs_abs[(size_t)ai * nb + b] * planck_over_h(nu, T) * E.widflx[b] * E.gw[ai];
+        }
+        sd *= dfac;
+      }
+      s_row[b] = w * eHI + sHeI + sHeII + sd;
     }
     __syncthreads();
     // ---- cumulative row: sequential within a chunk, scanned across chunks ----
@@ -257,13 +300,13 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
     __syncthreads();
     const float total = s_row[nb - 1];
     const bool ok = total > 0.f && total < INFINITY;
-    float *out = E.rec_cdf + (size_t)c * nb;
+    float *out = (E.gas ? E.rec_cdf : E.dust_cdf) + (size_t)c * nb;
     for (int b = t; b < nb; b += kEmiThreads) {
       float v = ok ? s_row[b] / total : 1.f;
-      if (b == nb - 1 || v > 0.999998f) v = 1.f;
+      if (b == nb - 1 || (E.gas && v > 0.999998f)) v = 1.f;
       out[b] = v;
     }
-    if (t == 0) {
+    if (E.gas && t == 0) {
       const float lines = s_par[0], all = (ok ? total : 0.f) + lines;
       E.total_lines[c] = all > 0.f ? lines / all : 0.f;
     }
@@ -274,7 +317,7 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
 }  // namespace
 
 cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int num_sms, cudaStream_t s) {
-  if (E.nb > kEmiMaxBins || E.nheavy > kEmiMaxHeavy || E.nlim[0] > kEmiMaxLim || E.nlim[1] > kEmiMaxLim ||
+  if (E.nb > kEmiMaxBins || E.nheavy > kEmiMaxHeavy || E.nsizes > kEmiMaxSizes || E.nlim[0] > kEmiMaxLim || E.nlim[1] > kEmiMaxLim ||
       E.nlim[2] > kEmiMaxLim || E.nlim[0] + E.nlim[1] + E.nlim[2] > 64)
     return cudaErrorInvalidValue;
   if (a.ncel > 0) {

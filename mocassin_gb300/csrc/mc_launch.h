@@ -168,8 +168,15 @@ struct EmiArgs {
   float hi_rec_sum, heii_rec_sum;
   const float *hei_rec;           // [34][3][4] HeI line fits (first coefficient x 1e25)
   float milne_c;                  // 4 pi h c Ryd (h^2 / 2 pi m k)^1.5 Ryd^2 1e40
+  // grains (nsizes 0: none); tdust [nsizes+1][nc+1] (row 0 the mixture), null before the first
+  int nsizes, gas;
+  const float *xs_abs, *gw, *widflx, *ndust, *tdust;   // [nsizes][nb], [nsizes], [nb], [nc+1]
+  const double *hden;
+  float t_sub;
   float *rec_cdf, *total_lines;   // out: [nc+1][nb] rows, [nc+1]
+  float *dust_cdf;                // out on a dust-only grid: [nc+1][nb]
 };
+constexpr int kEmiMaxSizes = 16;
 cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int num_sms, cudaStream_t s);
 
 // Sets the text returned by mc_last_error() on the calling thread.

@@ -130,6 +130,10 @@ struct mc_ctx {
   double m_near_res = 0.3;  // warm start: residual / heating below which a prediction is bracketed
   // diffuse-emission CDF: derived tables (one buffer) and forbidden-line totals
   DBuf e_tab, e_forb;
+  DBuf d_tdust;      // grain temperatures of the last mc_ctx_dust_temperatures [nsizes+1][nc+1]
+  DBuf o_fix_den, o_fix_xs;  // opacity rows that do not follow the cell state (grains)
+  int o_nfix = 0;
+  int d_nsizes = 0;
   mcg::EmiArgs emi{};
   bool e_ready = false;
   bool u_ready = false, s_ready = false;
@@ -982,12 +986,15 @@ extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const
     w[(size_t)i * nout] = 1.f;
     for (int k = 0; k < nsizes; ++k) w[(size_t)i * nout + 1 + k] = w_abs[(size_t)i * nsizes + k];
   }
-  DBuf dw, dm, de, dg, dt, err;
+  DBuf dw, dm, de, dg, err;
+  DBuf &dt = c->d_tdust;
+  if (dt.p && dt.bytes != (size_t)nout * nc1 * sizeof(float)) { cudaFree(dt.p); dt.p = nullptr; dt.bytes = 0; }
   MC_CUDA(dw.alloc(w.size() * sizeof(float)));
   MC_CUDA(dm.alloc((size_t)nout * nc1 * sizeof(float)));
   MC_CUDA(de.alloc((size_t)nsizes * ntemps * sizeof(float)));
   MC_CUDA(dg.alloc((size_t)nsizes * sizeof(float)));
-  MC_CUDA(dt.alloc((size_t)nout * nc1 * sizeof(float)));
+  if (!dt.p) MC_CUDA(dt.alloc((size_t)nout * nc1 * sizeof(float)));
+  c->d_nsizes = nsizes;
   MC_CUDA(err.alloc(sizeof(int)));
   cudaStream_t s = c->stream;
   MC_CUDA(cudaMemcpyAsync(dw.p, w.data(), dw.bytes, cudaMemcpyHostToDevice, s));
@@ -1833,6 +1840,17 @@ extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_t
   I.insert(I.end(), hhi.begin(), hhi.end());
   const size_t o_hg = putf(hg.data(), nh), o_hnu = putf(hnu.data(), nh);
   const size_t o_xso = putf(t->xs_outer, (size_t)nh * nb);
+  const int ns = t->n_sizes;
+  if (ns < 0 || ns > mcg::kEmiMaxSizes || (ns > 0 && (!t->xs_abs || !t->grain_weight || !t->ndust)))
+    return set_error(MC_ERR_ARG, "emission tables: 0..%d grain sizes with xs_abs, grain_weight, ndust",
+                     mcg::kEmiMaxSizes);
+  size_t o_xa = 0, o_gw = 0, o_nd = 0;
+  const size_t o_wf = putf(t->wid_flx, nb);
+  if (ns > 0) {
+    o_xa = putf(t->xs_abs, (size_t)ns * nb);
+    o_gw = putf(t->grain_weight, ns);
+    o_nd = putf(t->ndust, (size_t)c->nc + 1);
+  }
   const size_t o_hei = putf(t->hei_rec, 34 * 3 * 4);
   float hi_sum = 0.f, heii_sum = 0.f;
   for (int iup = 3; iup <= 15; ++iup)
@@ -1880,6 +1898,12 @@ extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_t
   E.hi_rec_sum = hi_sum;
   E.heii_rec_sum = heii_sum;
   E.hei_rec = fb + o_hei;
+  E.nsizes = ns;
+  E.widflx = fb + o_wf;
+  E.xs_abs = ns ? fb + o_xa : nullptr;
+  E.gw = ns ? fb + o_gw : nullptr;
+  E.ndust = ns ? fb + o_nd : nullptr;
+  E.t_sub = t->t_sublime;
   // fourPi hcRyd constant 1e20 1e20 of fb_ff (:429-527), formed in FP64 (1e40 is not an FP32 number)
   E.milne_c = (float)((double)(4.f * 3.141592654f) * 2.1799153e-11 * (double)4.9874105e-6f * 1e40);
   c->e_ready = true;
@@ -1889,20 +1913,31 @@ extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_t
 extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
   if (!c) return set_error(MC_ERR_ARG, "ctx is required");
   if (!c->e_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_emission_tables has not been called");
-  if (!c->u_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_update_tables has not been called");
-  if (!c->s_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_cell_state has not been called");
   const int nc1 = c->nc + 1, nb = c->nb;
+  const bool gas = (c->flags & MC_FLAG_GAS) != 0;
+  if (gas && !c->u_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_update_tables has not been called");
+  if (gas && !c->s_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_cell_state has not been called");
+  if (!gas && c->emi.nsizes == 0) return set_error(MC_ERR_ARG, "a dust-only grid needs grains in the emission tables");
+  if (c->emi.nsizes > 0 && c->d_tdust.p && c->d_nsizes != c->emi.nsizes)
+    return set_error(MC_ERR_ARG, "grain temperatures of %d sizes, emission tables of %d", c->d_nsizes, c->emi.nsizes);
   cudaStream_t s = c->stream;
   mc_status st;
   if ((st = put_buf(c->e_forb, nullptr, (size_t)std::max(c->u_ncel, 1) * nc1 * sizeof(float), s))) return st;
-  if (!c->rec_cdf.p) {
+  if (!gas && !c->dust_cdf.p) {
+    MC_CUDA(c->dust_cdf.alloc((size_t)nc1 * nb * sizeof(float)));
+    std::vector<float> one(nb, 1.f);
+    MC_CUDA(cudaMemcpyAsync(c->dust_cdf.p, one.data(), nb * sizeof(float), cudaMemcpyHostToDevice, s));
+    MC_CUDA(cudaStreamSynchronize(s));
+    c->g.dust_cdf = c->dust_cdf.as<float>();
+  }
+  if (gas && !c->rec_cdf.p) {
     MC_CUDA(c->rec_cdf.alloc((size_t)nc1 * nb * sizeof(float)));
     std::vector<float> one(nb, 1.f);  // row 0 (outside the nebula) is never sampled
     MC_CUDA(cudaMemcpyAsync(c->rec_cdf.p, one.data(), nb * sizeof(float), cudaMemcpyHostToDevice, s));
     MC_CUDA(cudaStreamSynchronize(s));
     c->g.rec_cdf = c->rec_cdf.as<float>();
   }
-  if (!c->tlines.p) {
+  if (gas && !c->tlines.p) {
     MC_CUDA(c->tlines.alloc((size_t)nc1 * sizeof(float)));
     MC_CUDA(cudaMemsetAsync(c->tlines.p, 0, (size_t)nc1 * sizeof(float), s));
     c->g.total_lines = c->tlines.as<float>();
@@ -1917,6 +1952,11 @@ extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
   E.ab = c->f_ab.as<float>();
   E.rec_cdf = c->rec_cdf.as<float>();
   E.total_lines = c->tlines.as<float>();
+  E.gas = gas ? 1 : 0;
+  E.tdust = E.nsizes > 0 ? c->d_tdust.as<float>() : nullptr;
+  E.hden = c->u_hden.as<double>();
+  E.dust_cdf = c->dust_cdf.as<float>();
+  if (!gas) a.ncel = 0;  // no forbidden lines without gas
   MC_CUDA(cudaEventRecord(c->ev0, s));
   cudaError_t e = mcg::launch_emission(a, E, c->e_forb.as<float>(), c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "emission launch failed: %s", cudaGetErrorString(e));
@@ -1937,6 +1977,15 @@ extern "C" mc_status mc_ctx_get_emission(mc_ctx_t *c, float *rec_rows, float *to
     if (!c->tlines.p) return set_error(MC_ERR_ARG, "no totalLines on the device");
     MC_CUDA(cudaMemcpyAsync(total_lines, c->tlines.p, nc1 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   }
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_get_dust_emission(mc_ctx_t *c, float *dust_rows) {
+  if (!c || !dust_rows) return set_error(MC_ERR_ARG, "ctx and dust_rows are required");
+  if (!c->dust_cdf.p) return set_error(MC_ERR_ARG, "no dust-emission CDF on the device");
+  MC_CUDA(cudaMemcpyAsync(dust_rows, c->dust_cdf.p, ((size_t)c->nc + 1) * c->nb * sizeof(float),
+                          cudaMemcpyDeviceToHost, c->stream));
   MC_CUDA(cudaStreamSynchronize(c->stream));
   return MC_OK;
 }
@@ -1965,11 +2014,25 @@ extern "C" mc_status mc_ctx_get_opacity(mc_ctx_t *c, float *out) {
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *c, int32_t nrows, const float *den, const float *xs) {
+  if (!c || nrows < 0 || nrows > 16 || (nrows > 0 && (!den || !xs)))
+    return set_error(MC_ERR_ARG, "ctx, 0..16 rows, den and xs are required");
+  const size_t nc1 = (size_t)c->nc + 1;
+  mc_status st;
+  if (nrows > 0 && ((st = put_buf(c->o_fix_den, den, nrows * nc1 * sizeof(float), c->stream)) ||
+                    (st = put_buf(c->o_fix_xs, xs, (size_t)nrows * c->nb * sizeof(float), c->stream))))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  c->o_nfix = nrows;
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, const int32_t *species,
                                               const float *xs, int32_t method, double *kernel_ms) {
   if (!c || !species || !xs) return set_error(MC_ERR_ARG, "ctx, species and xs are required");
   if (!c->u_ready || !c->s_ready) return set_error(MC_ERR_ARG, "cell state or tables missing");
-  if (nspecies < 1 || nspecies > 64) return set_error(MC_ERR_ARG, "nspecies must be 1..64 (got %d)", nspecies);
+  if (nspecies < 1 || nspecies + c->o_nfix > 64)
+    return set_error(MC_ERR_ARG, "nspecies must be 1..%d (got %d)", 64 - c->o_nfix, nspecies);
   if (method != MC_OPAC_FP32 && method != MC_OPAC_BF16X3) return set_error(MC_ERR_ARG, "unknown opacity method");
   std::vector<int32_t> se(nspecies), ss(nspecies);
   for (int k = 0; k < nspecies; ++k) {
@@ -1980,12 +2043,22 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
   const int nc1 = c->nc + 1, nb = c->nb;
   cudaStream_t s = c->stream;
   mc_status st;
+  const int nrows = nspecies + c->o_nfix;
   if ((st = put_buf(c->s_spe, se.data(), nspecies * sizeof(int32_t), s)) ||
       (st = put_buf(c->s_sps, ss.data(), nspecies * sizeof(int32_t), s)) ||
-      (st = put_buf(c->s_xs, xs, (size_t)nspecies * nb * sizeof(float), s)) ||
-      (st = put_buf(c->s_den, nullptr, (size_t)nspecies * nc1 * sizeof(float), s)) ||
+      (st = put_buf(c->s_xs, nullptr, (size_t)nrows * nb * sizeof(float), s)) ||
+      (st = put_buf(c->s_den, nullptr, (size_t)nrows * nc1 * sizeof(float), s)) ||
       (st = put_buf(c->s_err, nullptr, sizeof(int), s)))
     return st;
+  MC_CUDA(cudaMemcpyAsync(c->s_xs.p, xs, (size_t)nspecies * nb * sizeof(float), cudaMemcpyHostToDevice, s));
+  if (c->o_nfix > 0) {
+    // the fixed rows follow the species: their densities and cross-sections
+    MC_CUDA(cudaMemcpyAsync(c->s_xs.as<float>() + (size_t)nspecies * nb, c->o_fix_xs.p,
+                            (size_t)c->o_nfix * nb * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    MC_CUDA(cudaMemcpyAsync(c->s_den.as<float>() + (size_t)nspecies * nc1, c->o_fix_den.p,
+                            (size_t)c->o_nfix * nc1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  }
+  MC_CUDA(cudaStreamSynchronize(s));  // xs is the caller's (pageable) array
   MC_CUDA(cudaMemsetAsync(c->s_err.p, 0, sizeof(int), s));
   cudaEvent_t e0, e1;
   MC_CUDA(cudaEventCreate(&e0));
@@ -1994,7 +2067,7 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
   cudaError_t e = mcg::launch_species(c->nc, nspecies, c->s_spe.as<int>(), c->s_sps.as<int>(), c->s_X.as<double>(),
                                       c->u_ab.as<double>(), c->u_hden.as<double>(), c->s_den.as<float>(), c->num_sms, s);
   if (e == cudaSuccess)
-    e = mcg::launch_opacity(method, nc1, nspecies, nb, c->s_den.as<float>(), c->s_xs.as<float>(), nullptr,
+    e = mcg::launch_opacity(method, nc1, nrows, nb, c->s_den.as<float>(), c->s_xs.as<float>(), nullptr,
                             c->opacity.as<float>(), c->s_err.as<int>(), c->num_sms, s);
   if (e == cudaSuccess && !c->identity)
     e = mcg::launch_wave_expand(c->opacity.as<float>(), c->opac_m.as<float>(), c->lin2cell.as<int32_t>(), c->ncell3,

@@ -16,7 +16,9 @@ import os
 
 import numpy as np
 
-from . import nebula
+from . import dust, nebula
+
+T_SUBLIME = 1400.0  # sublimation temperature of the synthetic silicate-like grains [K]
 
 _T = None
 
@@ -39,4 +41,9 @@ def tables(neb):
     ix = {ion: k for k, ion in enumerate(ions)}
     t["wid_flx"] = nebula.wid_flx(neb.nu)
     t["xs_h"], t["xs_hei"], t["xs_heii"] = neb.xs[ix[(1, 1)]], neb.xs[ix[(2, 1)]], neb.xs[ix[(2, 2)]]
+    if neb.flags & nebula.FLAG_DUST:
+        # the grains of nebula._dust_kappa: one species, grainAbun 1
+        xs_abs, w, _ = dust.grains(neb.nu)
+        t["xs_abs"], t["grain_weight"], t["t_sublime"] = xs_abs, w, T_SUBLIME
+        t["ndust"] = neb.ndust
     return t

@@ -15,10 +15,12 @@ Each iteration runs, on the grid resident in HBM,
   5. the re-emission CDFs of the next transport (recPDF rows and totalLines,
      emissionDriver / setDiffusePDF, emission_mod.f90:32-1311, on the GPU),
      built from the initial state before the first transport too, as the
-     reference builds them at the top of every iteration.  ``emission``
-     "auto" does this for a gas-only grid; a grid with dust keeps the input
-     CDFs (the dust emission of setDiffusePDF / setDustPDF is not on this
-     path).
+     reference builds them at the top of every iteration.
+On a grid with grains the grain temperatures (getDustT) follow the update,
+the grains' opacity (Ndust x (abs + sca) per grain, the dust add of
+iteration_mod.f90:166-227) is added to every opacity rebuild, and their
+thermal emission joins the recPDF rows.  The grains keep their opacity above
+the sublimation temperature (the reference drops it there).
 
 ``form`` picks the transport ("graph": the frequency-sorted persistent march
 with its rounds in one CUDA graph; "wave": the same with host-driven rounds;
@@ -57,8 +59,14 @@ class LambdaIteration:
         self.ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
         te, ne, X = balance.initial_state(neb)
         self.ctx.set_cell_state(te, ne, X)
+        self.dust = None
+        if neb.flags & nebula.FLAG_DUST:
+            from . import dust
+            xs_abs, gw, _ = dust.grains(neb.nu)
+            self.dust = (dust.absorption_weights(xs_abs), dust.emission_table(xs_abs, neb.nu), gw)
+            self.ctx.set_fixed_opacity(neb.ndust, neb.dust_kappa)
         if emission == "auto":
-            emission = not (neb.flags & nebula.FLAG_DUST)
+            emission = True
         self.emission = bool(emission)
         if self.emission:
             self.ctx.set_emission_tables()
@@ -93,6 +101,8 @@ class LambdaIteration:
                 loss, train_ms = self.ctx.surrogate_train(self.sur["finetune_steps"], self.sur["batch"],
                                                           0.3 * self.sur["lr"], self.sur["seed"])
         t2b = time.perf_counter()
+        if self.dust is not None:
+            self.ctx.dust_temperatures(*self.dust, self.scale)
         op_ms = self.ctx.opacity_from_state(self.species, self.neb.xs, method=self.opacity_method)
         em_ms = self.ctx.build_emission() if self.emission else 0.0
         t3 = time.perf_counter()

@@ -68,6 +68,8 @@ def library():
         lib.mc_ctx_build_emission.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
         lib.mc_ctx_get_emission.restype = C.c_int
         lib.mc_ctx_get_emission.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.mc_ctx_get_dust_emission.restype = C.c_int
+        lib.mc_ctx_get_dust_emission.argtypes = [C.c_void_p, C.c_void_p]
         lib.mc_ctx_set_cell_state.restype = C.c_int
         lib.mc_ctx_set_cell_state.argtypes = [C.c_void_p, dp, dp, dp]
         lib.mc_ctx_get_cell_state.restype = C.c_int
@@ -77,6 +79,8 @@ def library():
                                             C.POINTER(abi.McUpdateStats)]
         lib.mc_ctx_opacity_from_state.restype = C.c_int
         lib.mc_ctx_opacity_from_state.argtypes = [C.c_void_p, C.c_int32, ip, fp, C.c_int32, dp]
+        lib.mc_ctx_set_fixed_opacity.restype = C.c_int
+        lib.mc_ctx_set_fixed_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp]
         u64 = C.c_uint64
         lib.mc_ctx_surrogate_init.restype = C.c_int
         lib.mc_ctx_surrogate_fallback.restype = C.c_int
@@ -290,6 +294,12 @@ class TransportContext:
         _check(self.lib.mc_ctx_get_emission(self.handle, rows.ctypes.data, tl.ctypes.data))
         return rows, tl
 
+    def get_dust_emission(self):
+        """The dustPDF rows (Nc+1, nbins) of a dust-only grid on the device."""
+        rows = np.empty((self.neb.ncells + 1, self.neb.nbins), dtype=np.float32)
+        _check(self.lib.mc_ctx_get_dust_emission(self.handle, rows.ctypes.data))
+        return rows
+
     def set_cell_state(self, te, ne, X):
         te = np.ascontiguousarray(te, dtype=np.float64)
         ne = np.ascontiguousarray(ne, dtype=np.float64)
@@ -382,6 +392,13 @@ class TransportContext:
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
         _check(self.lib.mc_ctx_get_opacity(self.handle, _fptr(out)))
         return out
+
+    def set_fixed_opacity(self, den, xs):
+        """Opacity rows that do not follow the cell state (den [rows][Nc+1],
+        xs [rows][nbins]), appended to every opacity_from_state."""
+        d = np.ascontiguousarray(np.atleast_2d(den), dtype=np.float32)
+        x = np.ascontiguousarray(np.atleast_2d(xs), dtype=np.float32)
+        _check(self.lib.mc_ctx_set_fixed_opacity(self.handle, len(d), _fptr(d), _fptr(x)))
 
     def opacity_from_state(self, species, xs, method="bf16x3"):
         sp = np.ascontiguousarray(species, dtype=np.int32)

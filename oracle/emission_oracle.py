@@ -113,10 +113,56 @@ def two_photon_ay(y):
     return 202.0 * (y * (1 - y) * (1 - q ** 0.8) + 0.88 * ((y * (1 - y)) ** 1.53) * q ** 0.8)
 
 
-def diffuse_pdf(te, ne, X, abund, forb, T=None, nu=None, xs=None, ions=None):
+def planck_over_h(nu, t):
+    """getFlux(energy, T, 'blackbody') (continuum_mod.f90:359-394), FP64,
+    for a frequency vector at one temperature."""
+    constant = 0.5250229 / HPLANCK
+    u = HCRYD_K * nu / t
+    out = np.empty_like(u)
+    big = u > 86.0
+    out[big] = constant * nu[big] ** 3 * np.exp(-u[big])
+    den = np.expm1(u[~big])
+    rj = den <= 0
+    out[~big] = np.where(rj, 3.32154e-6 * nu[~big] ** 2 * t / HPLANCK, constant * nu[~big] ** 3 / np.where(rj, 1, den))
+    return out
+
+
+def grain_emission(tdust, xs_abs, gw, t_sub, nu, positive):
+    """sum over size bins of xSecAbs B(nu, Tdust) widFlx grainWeight grainAbun
+    [n][nbins] (sumDiffuseDust, emission_mod.f90:1042-1105; setDustPDF
+    :1329-1367 also requires Tdust > 0)."""
+    nu64 = nu.astype(np.float64)
+    wid = nebula.wid_flx(nu).astype(np.float64)
+    out = np.zeros((len(tdust), len(nu)))
+    for c in range(len(tdust)):
+        for a in range(xs_abs.shape[0]):
+            t = float(tdust[c][a])
+            if t < t_sub and (t > 0 or not positive):
+                if t <= 0:
+                    continue  # the Planck function of 0 K is 0
+                out[c] += xs_abs[a].astype(np.float64) * planck_over_h(nu64, t) * wid * gw[a]
+    return out
+
+
+def dust_pdf(tdust, xs_abs, gw, t_sub, nu=None):
+    """dustPDF rows [n][nbins] of a dust-only grid (setDustPDF, :1313-1387)."""
+    nu = nebula.atomic_table()["nu"] if nu is None else nu
+    s = grain_emission(tdust, xs_abs, gw, t_sub, nu, True)
+    cdf = np.cumsum(s, axis=1)
+    last = cdf[:, -1].copy()
+    ok = last > 0
+    cdf[ok] = cdf[ok] / last[ok, None]
+    cdf[~ok] = 1.0
+    cdf[:, -1] = 1.0
+    return cdf
+
+
+def diffuse_pdf(te, ne, X, abund, forb, T=None, nu=None, xs=None, ions=None, dust=None):
     """recPDF rows [n][nbins] (cumulative, normalised) and totalLines [n] of
     n cells: te, ne [n], X [n][7][8] (elements H He C N O Ne S, stage 1..7),
-    abund [7], forb [n][ncel] from update_runner.forbidden_lines."""
+    abund [7], forb [n][ncel] from update_runner.forbidden_lines.  dust: None
+    or a dict with tdust [n][nsizes], xs_abs [nsizes][nbins], gw [nsizes],
+    t_sub and ndust_over_hden [n] for the thermal grain emission."""
     T = tables() if T is None else T
     at = nebula.atomic_table()
     nu = at["nu"] if nu is None else nu
@@ -260,7 +306,12 @@ def diffuse_pdf(te, ne, X, abund, forb, T=None, nu=None, xs=None, ions=None):
     for i in range(4):
         val = lya if i == 3 else lyd[i] * lya
         sHeII[:, locate(nu, lynu[i]) - 1] += val
-    normalize = sHI.sum(1) + sHeI.sum(1) + sHeII.sum(1)
+    sDust = np.zeros_like(sHI)
+    if dust is not None:
+        const = HPLANCK * 4.0 * PI * 1e25 * CRYD   # :1097-1100
+        sDust = grain_emission(dust["tdust"], dust["xs_abs"], dust["gw"], dust["t_sub"], nu, False) * \
+            (const * np.asarray(dust["ndust_over_hden"], dtype=np.float64))[:, None]
+    normalize = sHI.sum(1) + sHeI.sum(1) + sHeII.sum(1) + sDust.sum(1)
 
     # recombination lines (RecLinesEmission :744-832) and normRec (:1122-1139)
     hbeta = 10 ** (-0.870 * log10te + 3.57) * ne * xH2 * abH
@@ -291,7 +342,7 @@ def diffuse_pdf(te, ne, X, abund, forb, T=None, nu=None, xs=None, ions=None):
     total = norm_rec + norm_for
 
     # the CDF (:1177-1212) and the line fraction (:1302-1304)
-    s = sHI + sHeI + sHeII
+    s = sHI + sHeI + sHeII + sDust
     cdf = np.cumsum(s, axis=1)
     last = cdf[:, -1].copy()
     ok = last > 0

@@ -167,3 +167,87 @@ def test_lambda_iteration_rebuilds_the_emission_cdfs(gpu_lib):
     assert np.abs(rows[c] - cdf).max() <= 2e-5
     np.testing.assert_allclose(tl[c], otl, rtol=1e-4, atol=1e-7)
     assert not np.array_equal(tl, tl0)
+
+
+def _dusty(n=21, packets=300_000, gas=True):
+    import dataclasses
+    neb = nebula.build(dataclasses.replace(nebula.dusty81(packets), name="dusty%d" % n, n=n))
+    if not gas:
+        neb = dataclasses.replace(neb, flags=neb.flags & ~nebula.FLAG_GAS)
+    return neb
+
+
+def _grain_temperatures(ctx, neb):
+    from mocassin_gb300 import dust
+    xs_abs, w, _ = dust.grains(neb.nu)
+    td, _ = ctx.dust_temperatures(dust.absorption_weights(xs_abs), dust.emission_table(xs_abs, neb.nu), w, 1e-9)
+    return td
+
+
+@pytest.mark.gpu
+def test_gpu_emission_with_grains_matches_oracle(gpu_lib):
+    """A gas grid with grains: the thermal grain emission at the grain
+    temperatures the GPU left joins the recPDF rows (sumDiffuseDust)."""
+    from mocassin_gb300 import dust, transport
+    neb = _dusty()
+    ctx = transport.TransportContext(neb)
+    ctx.run(seed=4, precision="fp32", zero_first=True)
+    td = _grain_temperatures(ctx, neb)
+    ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+    te, ne, X = balance.initial_state(neb)
+    ctx.set_cell_state(te, ne, X)
+    ctx.set_emission_tables()
+    ctx.build_emission()
+    rows, tl = ctx.get_emission()
+    ctx.close()
+    hit = np.nonzero(td[1] > 0)[0]
+    assert len(hit) > 100
+    c = np.sort(np.random.default_rng(2).choice(hit[hit > 0], 200, replace=False))
+    xs_abs, w, _ = dust.grains(neb.nu)
+    d = {"tdust": td[1:, c].T.astype(np.float64), "xs_abs": xs_abs, "gw": w, "t_sub": emission.T_SUBLIME,
+         "ndust_over_hden": neb.ndust[c].astype(np.float64) / neb.hden[c].astype(np.float64)}
+    forb = update_runner.forbidden_lines(balance.tables(), balance.abundances(), te[c], ne[c], X[c])
+    cdf, otl = EO.diffuse_pdf(te[c], ne[c], X[c], balance.abundances(), forb, dust=d)
+    cdf0, _ = EO.diffuse_pdf(te[c], ne[c], X[c], balance.abundances(), forb)
+    assert np.abs(cdf - cdf0).max() > 1e-3  # the grains change the rows
+    assert np.abs(rows[c] - cdf).max() <= 2e-5
+    np.testing.assert_allclose(tl[c], otl, rtol=1e-4, atol=1e-7)
+
+
+@pytest.mark.gpu
+def test_gpu_dust_only_grid_builds_dust_pdf(gpu_lib):
+    """A dust-only grid: the dustPDF rows of setDustPDF from the grain
+    temperatures alone (no cell state, no update tables)."""
+    from mocassin_gb300 import dust, transport
+    neb = _dusty(gas=False)
+    ctx = transport.TransportContext(neb)
+    ctx.run(seed=4, precision="fp32", zero_first=True)
+    td = _grain_temperatures(ctx, neb)
+    ctx.set_emission_tables()
+    ctx.build_emission()
+    rows = ctx.get_dust_emission()
+    ctx.close()
+    xs_abs, w, _ = dust.grains(neb.nu)
+    c = np.arange(1, neb.ncells + 1, 23)
+    cdf = EO.dust_pdf(td[1:, c].T.astype(np.float64), xs_abs, w, emission.T_SUBLIME)
+    assert np.abs(rows[c] - cdf).max() <= 2e-5
+    assert np.all(np.diff(rows[1:], axis=1) >= 0) and np.all(rows[1:, -1] == 1.0)
+
+
+@pytest.mark.gpu
+def test_lambda_iteration_on_a_dusty_grid(gpu_lib):
+    """The Lambda iteration of a gas grid with grains keeps the grain opacity
+    in every rebuild, follows the grain temperatures and builds the CDFs with
+    their thermal emission."""
+    from mocassin_gb300 import iterate, transport
+    neb = _dusty(n=21, packets=300_000)
+    li = iterate.LambdaIteration(neb, form="graph", update="fp32")
+    _, hist = li.run(seed=5, max_iterations=2, min_convergence=101.0)
+    op = li.ctx.get_opacity()
+    rows, tl = li.ctx.get_emission()
+    li.close()
+    # opacity = gas contraction + Ndust x kappa_d: at the lowest frequencies the grains dominate
+    kd = neb.ndust[1:].astype(np.float64) * neb.dust_kappa[0]
+    np.testing.assert_allclose(op[0, 1:], kd, rtol=2e-3)
+    assert np.all(np.diff(rows[1:], axis=1) >= 0) and np.all(rows[1:, -1] == 1.0)
+    assert len(hist) == 2 and all(h["emission_ms"] > 0 for h in hist)
