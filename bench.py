@@ -391,9 +391,10 @@ def main():
         t = pin(neb.sca_opac)
         m.grid.sca_opac = C.cast(t.data_ptr(), C.POINTER(C.c_float))
         h2d += t.numel() * 4
-    js = torch.zeros((neb.nbins, neb.ncells + 1), dtype=torch.float64).pin_memory()
-    es = torch.zeros((neb.nbins + 1, neb.ncells + 1), dtype=torch.float64).pin_memory()
-    d2h = (js.numel() + es.numel()) * 8
+    # the grid's own 4-byte estimator arrays (mc_transport_run_f32): FP64 sums on the device, rounded once
+    js = torch.zeros((neb.nbins, neb.ncells + 1), dtype=torch.float32).pin_memory()
+    es = torch.zeros((neb.nbins + 1, neb.ncells + 1), dtype=torch.float32).pin_memory()
+    d2h = (js.numel() + es.numel()) * 4
     # the estimators start each iteration at zero (MC_RUN_ZERO_FIRST: not uploaded)
     e2e_t, e2e_c = 0.0, 0
     for k in range(args.e2e_steps + 1):
@@ -404,9 +405,9 @@ def main():
         st = abi.McStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rc = lib.mc_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts),
-                                  C.cast(js.data_ptr(), C.POINTER(C.c_double)), None,
-                                  C.cast(es.data_ptr(), C.POINTER(C.c_double)), C.byref(st))
+        rc = lib.mc_transport_run_f32(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts),
+                                      C.cast(js.data_ptr(), C.POINTER(C.c_float)), None,
+                                      C.cast(es.data_ptr(), C.POINTER(C.c_float)), C.byref(st))
         dt = time.perf_counter() - t0
         if rc != 0:
             raise transport.TransportError(rc, lib.mc_last_error().decode())
@@ -414,9 +415,10 @@ def main():
             e2e_t += dt
             e2e_c += st.crossings
     e2e = {"value": e2e_c / e2e_t if e2e_t > 0 else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-           "call": "mc_transport_run (host pinned buffers: grid upload, CDF re-layout, transport, estimator "
-                   "download; the estimators start at zero (MC_RUN_ZERO_FIRST); device buffers kept between calls "
-                   "of the same grid shape)"}
+           "call": "mc_transport_run_f32 (host pinned buffers: grid upload, CDF re-layout, transport, estimator "
+                   "download into the grid's own FP32 Jste and escapedPackets, FP64 sums rounded once on the device; "
+                   "the estimators start at zero (MC_RUN_ZERO_FIRST); device buffers kept between calls of the same "
+                   "grid shape)"}
 
     peak, peak_kind = measured_peak()
     # dominant kernel: the march (its own CUDA events on the library stream)

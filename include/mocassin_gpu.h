@@ -183,6 +183,16 @@ mc_status mc_transport_run(const mc_grid_t *grid, const mc_source_t *src,
                            double *jste, double *jdif, double *escaped,
                            mc_stats_t *stats);
 
+/* The same with the estimators in the grid's own 4-byte arrays
+ * (grid%Jste, grid%Jdif, grid%escapedPackets are `real` in common_mod.f90:
+ * 276-279), so the Fortran passes them without a conversion pass: the sums
+ * are still formed in FP64 on the device and rounded to FP32 once, on the
+ * device, before the copy back (half the bytes of mc_transport_run). */
+mc_status mc_transport_run_f32(const mc_grid_t *grid, const mc_source_t *src,
+                               int32_t nsrc, const mc_run_opts_t *opts,
+                               float *jste, float *jdif, float *escaped,
+                               mc_stats_t *stats);
+
 /* mc_transport_run keeps the device buffers of the last grid shape for the
  * next call (a Lambda iteration calls it with the same grid every time);
  * this frees them.  No counterpart in the reference (it allocates nothing

@@ -113,6 +113,12 @@ struct mc_ctx {
   DBuf xa, ya, za, active, opacity, sca, rec_raw, rec_cdf, dust_raw, dust_cdf, tlines, nu, gsca;
   DBuf dx32, dy32, dz32, dx64, dy64, dz64;
   DBuf jste, jdif, esc;
+  DBuf stage_j, stage_d, stage_e;  // FP32 staging of the drop-in call's estimators
+  // the drop-in call uploads and re-lays out recPDF on a side stream while
+  // round 0 (stellar packets only) runs; round 1 waits for ev_cdf
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_side0 = nullptr, ev_cdf = nullptr;
+  bool cdf_pending = false;
   DBuf view;        // viewing-angle table (n_angle > 0)
   int n_angle = 0;
   // cell update: atomic tables, per-cell state and scratch
@@ -252,7 +258,7 @@ mc_status view_table(const mc_grid_t *g, mcg::DevGrid &d, std::vector<uint8_t> &
   return MC_OK;
 }
 
-mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first) {
+mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t cdf_stream = nullptr) {
   const int nc1 = g->ncells + 1, nb = g->nbins;
   const size_t plane = (size_t)nc1 * nb * sizeof(float);
   cudaStream_t s = c->stream;
@@ -281,9 +287,15 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first) {
   if (g->total_lines && (st = put(c->tlines, g->total_lines, (size_t)nc1 * sizeof(float)))) return st;
   if (g->g_sca && (st = put(c->gsca, g->g_sca, (size_t)nb * sizeof(float)))) return st;
   if (g->rec_pdf) {
-    if ((st = put(c->rec_raw, g->rec_pdf, plane))) return st;
+    const cudaStream_t cs = cdf_stream ? cdf_stream : s;
+    if (first || !c->rec_raw.p) {
+      if ((st = upload(c->rec_raw, g->rec_pdf, plane, cs))) return st;
+    } else {
+      cudaError_t e = cudaMemcpyAsync(c->rec_raw.p, g->rec_pdf, plane, cudaMemcpyHostToDevice, cs);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
+    }
     if (!c->rec_cdf.p) MC_CUDA(c->rec_cdf.alloc(plane));
-    MC_CUDA(mcg::launch_cdf_transpose(c->rec_raw.as<float>(), c->rec_cdf.as<float>(), nc1, nb, s));
+    MC_CUDA(mcg::launch_cdf_transpose(c->rec_raw.as<float>(), c->rec_cdf.as<float>(), nc1, nb, cs));
   }
   if (g->dust_pdf) {
     if ((st = put(c->dust_raw, g->dust_pdf, plane))) return st;
@@ -628,19 +640,17 @@ mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSourc
   const bool f64 = precision == MC_PREC_FP64;
   cudaStream_t s = c->stream;
   MC_CUDA(cudaMemsetAsync(L.w.round_ctr, 0, sizeof(int), s));
-  cudaGraph_t graph = nullptr;
+  // two graphs: round 0 (stellar packets only), then the round control and a
+  // WHILE node over the re-emission rounds; a pending recPDF upload of the
+  // drop-in call is waited for between them
+  cudaGraph_t g0 = nullptr, graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   auto fail = [&](cudaError_t e, const char *what) {
+    if (g0) cudaGraphDestroy(g0);
     if (graph) cudaGraphDestroy(graph);
     return set_error(MC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
   };
-  cudaError_t e = cudaGraphCreate(&graph, 0);
-  if (e != cudaSuccess) return fail(e, "graph creation failed");
-  cudaGraphConditionalHandle handle;
-  e = cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault);
-  if (e != cudaSuccess) return fail(e, "conditional handle creation failed");
-  // round 0, then the condition for round 1
-  e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail(e, "capture failed");
   auto round0 = [&]() -> cudaError_t {
     cudaError_t r = cudaMemsetAsync(c->bins.p, 0, (size_t)c->nb * 2 * sizeof(unsigned int), s);
@@ -648,34 +658,39 @@ mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSourc
     if (r == cudaSuccess) r = mcg::launch_wave_sort(L, (unsigned int)S.total);
     if (r == cudaSuccess) r = f64 ? mcg::launch_wave_emit_fp64(L, 0) : mcg::launch_wave_emit_fp32(L, 0);
     if (r == cudaSuccess) r = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
-    if (r == cudaSuccess) r = mcg::launch_wave_round_control(L, handle);
     return r;
   };
   cudaError_t ce = round0();
-  cudaGraph_t captured = nullptr;
-  e = cudaStreamEndCapture(s, &captured);
+  e = cudaStreamEndCapture(s, &g0);
   if (ce != cudaSuccess) return fail(ce, "round 0 capture failed");
   if (e != cudaSuccess) return fail(e, "round 0 capture failed");
-  // the WHILE node after round 0
+  e = cudaGraphCreate(&graph, 0);
+  if (e != cudaSuccess) return fail(e, "graph creation failed");
+  cudaGraphConditionalHandle handle;
+  e = cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "conditional handle creation failed");
+  // the condition for round 1, from round 0's absorbed count
+  e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "capture failed");
+  ce = mcg::launch_wave_round_control(L, handle);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(s, &captured);
+  if (ce != cudaSuccess) return fail(ce, "round control capture failed");
+  if (e != cudaSuccess) return fail(e, "round control capture failed");
   cudaGraphNode_t last = nullptr;
   size_t nsink = 0;
   e = cudaGraphGetNodes(graph, nullptr, &nsink);
   std::vector<cudaGraphNode_t> nodes(nsink);
   if (e == cudaSuccess && nsink) e = cudaGraphGetNodes(graph, nodes.data(), &nsink);
-  if (e != cudaSuccess) return fail(e, "graph inspection failed");
-  // the round-control kernel is the one node nothing depends on
-  for (cudaGraphNode_t n : nodes) {
-    size_t nd = 0;
-    cudaGraphNodeGetDependentNodes(n, nullptr, nullptr, &nd);
-    if (nd == 0) last = n;
-  }
+  if (e != cudaSuccess || nsink != 1) return fail(e != cudaSuccess ? e : cudaErrorUnknown, "graph inspection failed");
+  last = nodes[0];
   cudaGraphNodeParams cp{};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = handle;
   cp.conditional.type = cudaGraphCondTypeWhile;
   cp.conditional.size = 1;
   cudaGraphNode_t cond = nullptr;
-  e = cudaGraphAddNode(&cond, graph, last ? &last : nullptr, nullptr, last ? 1 : 0, &cp);
+  e = cudaGraphAddNode(&cond, graph, &last, nullptr, 1, &cp);
   if (e != cudaSuccess) return fail(e, "conditional node failed");
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
@@ -696,6 +711,17 @@ mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSourc
   e = cudaStreamEndCapture(s, &cbody);
   if (ce != cudaSuccess) return fail(ce, "round capture failed");
   if (e != cudaSuccess) return fail(e, "round capture failed");
+  cudaGraphExec_t exec0 = nullptr;
+  e = cudaGraphInstantiate(&exec0, g0, 0);
+  if (e != cudaSuccess) return fail(e, "graph instantiation failed");
+  e = cudaGraphLaunch(exec0, s);
+  cudaGraphExecDestroy(exec0);
+  if (e != cudaSuccess) return fail(e, "graph launch failed");
+  if (c->cdf_pending) {
+    e = cudaStreamWaitEvent(s, c->ev_cdf, 0);
+    c->cdf_pending = false;
+    if (e != cudaSuccess) return fail(e, "event wait failed");
+  }
   e = cudaGraphInstantiate(&exec, graph, 0);
   if (e != cudaSuccess) return fail(e, "graph instantiation failed");
   e = cudaGraphLaunch(exec, s);
@@ -711,6 +737,7 @@ mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSourc
   int rounds = 0;
   MC_CUDA(cudaMemcpyAsync(&rounds, L.w.round_ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
+  cudaGraphDestroy(g0);
   cudaGraphDestroy(graph);
   *rounds_out = rounds;
   return MC_OK;
@@ -799,6 +826,12 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
   MC_CUDA(cudaMemcpyAsync(c->counters.p, &h, sizeof h, cudaMemcpyHostToDevice, c->stream));
   const bool plain = o->run_flags & MC_RUN_FORM_PLAIN;
   float wave_ms = 0.f;
+  // the graph form waits for a pending recPDF upload between round 0 and
+  // round 1; the other forms before they start
+  if (c->cdf_pending && !(S.total > 0 && !plain && (o->run_flags & MC_RUN_GRAPH))) {
+    MC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_cdf, 0));
+    c->cdf_pending = false;
+  }
   if (S.total > 0) {
     if (plain) {
       MC_CUDA(cudaEventRecord(c->evm0, c->stream));
@@ -880,6 +913,10 @@ void mc_ctx_destroy(mc_ctx_t *c) {
   if (c->evm0) cudaEventDestroy(c->evm0);
   if (c->evm1) cudaEventDestroy(c->evm1);
   if (c->wave_exec) cudaGraphExecDestroy(c->wave_exec);
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->ev_side0) cudaEventDestroy(c->ev_side0);
+  if (c->ev_cdf) cudaEventDestroy(c->ev_cdf);
+  if (c->side) cudaStreamDestroy(c->side);
   cudaStream_t s = c->stream;
   delete c;  // frees the device buffers
   if (s) cudaStreamDestroy(s);
@@ -2085,9 +2122,22 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
   return MC_OK;
 }
 
-mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
-                           double *jste, double *jdif, double *escaped, mc_stats_t *stats) {
+namespace {
+
+__global__ void widen_kernel(const float *__restrict__ in, double *__restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+__global__ void narrow_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// the drop-in call with FP64 (f32 = false) or FP32 host estimators
+mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                             void *jste, void *jdif, void *escaped, bool f32, mc_stats_t *stats) {
   if (!jste) return set_error(MC_ERR_ARG, "jste is NULL");
+  if (!o) return set_error(MC_ERR_ARG, "opts is NULL");
   if (g && (g->flags & MC_FLAG_DEBUG) && !jdif) return set_error(MC_ERR_ARG, "debug grid needs jdif");
   mc_status st = check_grid(g);
   if (st) return st;
@@ -2097,7 +2147,22 @@ mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t n
   cudaGetDevice(&dev);
   bool reuse = c && c->device == dev && c->nx == g->nx && c->ny == g->ny && c->nz == g->nz && c->nc == g->ncells &&
                c->nb == g->nbins && c->flags == g->flags && c->n_angle == g->n_angle;
-  if (reuse && (refresh_geometry(c, g) != MC_OK || upload_arrays(c, g, false) != MC_OK)) reuse = false;
+  if (reuse) {
+    if (!c->side && (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+                     cudaEventCreateWithFlags(&c->ev_side0, cudaEventDisableTiming) != cudaSuccess ||
+                     cudaEventCreateWithFlags(&c->ev_cdf, cudaEventDisableTiming) != cudaSuccess))
+      return set_error(MC_ERR_CUDA, "side stream creation failed");
+    // recPDF on the side stream, after whatever the context's stream still runs
+    MC_CUDA(cudaEventRecord(c->ev_side0, c->stream));
+    MC_CUDA(cudaStreamWaitEvent(c->side, c->ev_side0, 0));
+    if (refresh_geometry(c, g) != MC_OK || upload_arrays(c, g, false, c->side) != MC_OK) {
+      cudaStreamSynchronize(c->side);
+      reuse = false;
+    } else {
+      MC_CUDA(cudaEventRecord(c->ev_cdf, c->side));
+      c->cdf_pending = true;
+    }
+  }
   if (!reuse) {
     if (c) mc_ctx_destroy(c);
     g_cached = nullptr;
@@ -2109,19 +2174,54 @@ mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t n
   // come back (no host-side pass over the arrays).  With MC_RUN_ZERO_FIRST
   // the caller states that its arrays hold zeros (the Fortran driver zeroes
   // them before each iteration, iteration_mod.f90:458-472): the device
-  // copies are cleared instead of uploaded.
+  // copies are cleared instead of uploaded.  FP32 arrays go through a staging
+  // buffer per array and a widening / narrowing pass on the device.
   const bool zero = o->run_flags & MC_RUN_ZERO_FIRST;
-  struct Item { double *h; DBuf *d; } items[3] = {{jste, &c->jste}, {jdif, &c->jdif}, {escaped, &c->esc}};
+  cudaStream_t s = c->stream;
+  struct Item { void *h; DBuf *d; DBuf *stage; } items[3] = {
+      {jste, &c->jste, &c->stage_j}, {jdif, &c->jdif, &c->stage_d}, {escaped, &c->esc, &c->stage_e}};
   for (auto &it : items) {
     if (!it.d->p) continue;
-    if (it.h && !zero) MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, c->stream));
-    else MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, c->stream));
+    const size_t n = it.d->bytes / sizeof(double);
+    if (f32 && it.h && (st = put_buf(*it.stage, nullptr, n * sizeof(float), s))) return st;
+    if (!it.h || zero) {
+      MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, s));
+    } else if (!f32) {
+      MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, s));
+    } else {
+      MC_CUDA(cudaMemcpyAsync(it.stage->p, it.h, n * sizeof(float), cudaMemcpyHostToDevice, s));
+      widen_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.stage->as<float>(), it.d->as<double>(), n);
+      MC_CUDA(cudaGetLastError());
+    }
   }
   mc_run_opts_t o2 = *o;
   o2.run_flags &= ~MC_RUN_ZERO_FIRST;
   st = mc_ctx_run(c, src, nsrc, &o2, stats);
-  if (st == MC_OK) st = mc_ctx_download(c, jste, jdif, escaped, 0);
-  return st;
+  if (st != MC_OK) return st;
+  if (!f32) return mc_ctx_download(c, (double *)jste, (double *)jdif, (double *)escaped, 0);
+  // narrow each array and start its copy back; the next array's narrowing
+  // overlaps the previous copy
+  for (auto &it : items) {
+    if (!it.h || !it.d->p) continue;
+    const size_t n = it.d->bytes / sizeof(double);
+    narrow_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.d->as<double>(), it.stage->as<float>(), n);
+    MC_CUDA(cudaGetLastError());
+    MC_CUDA(cudaMemcpyAsync(it.h, it.stage->p, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+  }
+  MC_CUDA(cudaStreamSynchronize(s));
+  return MC_OK;
+}
+
+}  // namespace
+
+mc_status mc_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                           double *jste, double *jdif, double *escaped, mc_stats_t *stats) {
+  return transport_run_impl(g, src, nsrc, o, jste, jdif, escaped, false, stats);
+}
+
+mc_status mc_transport_run_f32(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
+                               float *jste, float *jdif, float *escaped, mc_stats_t *stats) {
+  return transport_run_impl(g, src, nsrc, o, jste, jdif, escaped, true, stats);
 }
 
 mc_status mc_transport_release(void) {

@@ -43,6 +43,9 @@ def library():
         lib.mc_transport_run.restype = C.c_int
         lib.mc_transport_run.argtypes = [C.POINTER(abi.McGrid), C.POINTER(abi.McSource), C.c_int32,
                                          C.POINTER(abi.McRunOpts), dp, dp, dp, C.POINTER(abi.McStats)]
+        lib.mc_transport_run_f32.restype = C.c_int
+        lib.mc_transport_run_f32.argtypes = [C.POINTER(abi.McGrid), C.POINTER(abi.McSource), C.c_int32,
+                                             C.POINTER(abi.McRunOpts), fp, fp, fp, C.POINTER(abi.McStats)]
         lib.mc_ctx_create.restype = C.c_int
         lib.mc_ctx_create.argtypes = [C.POINTER(abi.McGrid), C.POINTER(C.c_void_p)]
         lib.mc_ctx_update.restype = C.c_int
@@ -127,12 +130,17 @@ def _dptr(a):
 
 
 def _check_shapes(neb, jste, jdif, escaped):
+    """The estimators are all float64 (mc_transport_run) or all float32
+    (mc_transport_run_f32, the grid's own arrays)."""
     nj = (neb.nbins, neb.ncells + 1)
+    dt = jste.dtype if jste is not None else np.dtype(np.float64)
+    if dt not in (np.float64, np.float32):
+        raise ValueError("the estimators must be float64 or float32")
     for name, a, shape in (("jste", jste, nj), ("jdif", jdif, nj), ("escaped", escaped, abi.escaped_shape(neb))):
         if a is None:
             continue
-        if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
-            raise ValueError("%s must be a C-contiguous float64 array of shape %s" % (name, shape))
+        if a.shape != shape or a.dtype != dt or not a.flags.c_contiguous:
+            raise ValueError("%s must be a C-contiguous %s array of shape %s" % (name, dt, shape))
 
 
 def _flags(form, zero_first=False):
@@ -170,8 +178,13 @@ def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp
     if jdif is None and (neb.flags & abi_flag_debug()):
         jdif = jd0
     st = abi.McStats()
-    _check(lib.mc_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), _dptr(jste), _dptr(jdif),
-                                _dptr(escaped), C.byref(st)))
+    if jste.dtype == np.float32:
+        # the grid's own 4-byte arrays (mc_transport_run_f32)
+        _check(lib.mc_transport_run_f32(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), _fptr(jste), _fptr(jdif),
+                                        _fptr(escaped), C.byref(st)))
+    else:
+        _check(lib.mc_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), _dptr(jste), _dptr(jdif),
+                                    _dptr(escaped), C.byref(st)))
     return jste, jdif, escaped, st.as_dict()
 
 

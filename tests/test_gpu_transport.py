@@ -193,3 +193,23 @@ def test_drop_in_zero_first_overwrites(gpu_lib):
     es[:] = 2.0
     got = transport.energy_packet_driver(neb, precision="fp64", seed=41, jste=js, escaped=es, zero_first=True)
     assert helpers.rel_err(got[0], ref[0]) < 1e-12 and helpers.rel_err(got[2], ref[2]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_drop_in_fp32_estimators_are_the_fp64_sums_rounded(gpu_lib):
+    """mc_transport_run_f32 writes the grid's own 4-byte arrays: the FP64
+    device sums rounded once (so within one FP32 rounding of the FP64 call's
+    results), and it accumulates into their current values."""
+    neb = nebula.build(CASES[2])
+    ref = transport.energy_packet_driver(neb, precision="fp64", seed=41)
+    js = np.zeros_like(ref[0], dtype=np.float32)
+    es = np.zeros_like(ref[2], dtype=np.float32)
+    got = transport.energy_packet_driver(neb, precision="fp64", seed=41, jste=js, escaped=es, zero_first=True)
+    for a, b in ((got[0], ref[0]), (got[2], ref[2])):
+        assert a.dtype == np.float32
+        np.testing.assert_allclose(a, b.astype(np.float32), rtol=2.5e-7, atol=0)
+    js2 = np.full_like(js, 0.5)
+    es2 = np.full_like(es, 0.25)
+    acc = transport.energy_packet_driver(neb, precision="fp64", seed=41, jste=js2, escaped=es2)
+    np.testing.assert_allclose(acc[0], (ref[0] + 0.5).astype(np.float32), rtol=2.5e-7, atol=0)
+    np.testing.assert_allclose(acc[2], (ref[2] + 0.25).astype(np.float32), rtol=2.5e-7, atol=0)
