@@ -181,14 +181,25 @@ def converged_model(neb, args):
     update, opacity and emission-CDF rebuild) until 95 % of the cells have
     |dX(H0)/X(H0)| <= 5 % (the reference's minConvergence / XHILimit), for
     the chosen form (persistent wave march in a CUDA graph, FP32 cell
-    update), the same with the learned warm start after two iterations, and
-    the plain form (one thread per history, FP64 cell update), from the same
-    initial state."""
-    from mocassin_gb300 import iterate
+    update), the same with the learned warm start, and the plain form (one
+    thread per history, FP64 cell update), from the same initial state.  The
+    warm start's network is trained before the first update on the batch's
+    FP64 cell states (``--surrogate-rows``; its dataset and training times
+    are reported apart: one network serves every model), or, with
+    ``--surrogate-rows 0``, on the model's own first two iterations."""
+    from mocassin_gb300 import iterate, nebula
     out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
            "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
+    rows = None
+    if args.surrogate_rows > 0:
+        x, t, info = iterate.training_rows(nebula.batch64(), max_rows=args.surrogate_rows)
+        rows = (x, t)
+        out["surrogate_dataset"] = info
     for name, (form, upd, sur) in LAMBDA_FORMS.items():
+        if sur is not None and rows is not None:
+            sur = {"rows": rows, "train_after": None, "steps": 2000, "batch": 4096, "lr": 2e-3}
         li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
+        pre = li.pretrain
         wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
         li.close()
         last = hist[-1]
@@ -198,7 +209,10 @@ def converged_model(neb, args):
                      "dte_lt_1pc_pct": last["dte_lt_1pc_pct"],
                      "transport_s": sum(h["transport_s"] for h in hist), "update_s": sum(h["update_s"] for h in hist),
                      "opacity_s": sum(h["opacity_s"] for h in hist),
-                     "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist]))}
+                     "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist])),
+                     "warm_fallback_pct": float(np.mean([h["warm_fallback_pct"] for h in hist]))}
+        if pre is not None:
+            out[name]["pretrain"] = pre
     out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
     out["speedup_chosen_surrogate_vs_plain"] = out["plain"]["wall_s"] / out["chosen_surrogate"]["wall_s"]
     return out
@@ -245,6 +259,8 @@ def main():
     ap.add_argument("--batch-models", type=int, default=16,
                     help="batched serving: models of the 64-model batch to serve (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4)
+    ap.add_argument("--surrogate-rows", type=int, default=1_000_000,
+                    help="batch cell states (FP64 update) the warm start is trained on; 0: the model's own")
     ap.add_argument("--lambda-only", default="", choices=["", "chosen", "chosen_surrogate", "plain"],
                     help="run only the Lambda iteration of one form and print its record (profiling)")
     args = ap.parse_args()

@@ -355,18 +355,19 @@ mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32
                                     int32_t method, double *kernel_ms);
 
 /* ---- the learned warm start of the cell update ----------------------------
- * A small MLP (80 -> 128 -> 128 -> 48, ReLU; BF16 operands, FP32
+ * An MLP (80 -> 256 -> 256 -> 256 -> 48, ReLU; BF16 operands, FP32
  * accumulation and Adam, all on the GPU) from the Jste sums of a cell (log10
  * of sum Jste, of the 33 photoionisation and 33 heating sums, of Hden) to
  * log10 Te and log10 of the 40 ionic fractions.  Trained on cell states the
  * update produced (collect after mc_ctx_update_cells), it warm-starts the
  * update: mc_ctx_update_cells_warm writes the prediction into the state and
  * runs the same solve from there.  At the first T step the solve accepts
- * the prediction when the thermal residual is below 1 % of the heating;
- * below 30 % it brackets the balance from the prediction with steps of 3 %,
- * 6 %, 12 %, then the reference's 20 %, before its secant; otherwise the
- * cell falls back to the plain solve from the state before the prediction
- * (20 % steps, the full 25 T steps; counted in warm_fallback).  Every result
+ * the prediction when the thermal residual is below 1 % of the heating (or
+ * the stricter accept_res of mc_ctx_surrogate_rule); below 30 % (near_res)
+ * it brackets the balance from the prediction with steps of 3 %, 6 %, 12 %,
+ * then the reference's 20 %, before its secant; otherwise the cell falls
+ * back to the plain solve from the state before the prediction (20 % steps,
+ * the full 25 T steps; counted in warm_fallback).  Every result
  * meets the reference's 1 % residual test.  No counterpart in the reference
  * (updateCell starts from the previous iteration's state with 20 % steps). */
 mc_status mc_ctx_surrogate_init(mc_ctx_t *ctx, uint64_t seed, int64_t capacity);
@@ -375,10 +376,13 @@ mc_status mc_ctx_surrogate_train(mc_ctx_t *ctx, int32_t steps, int32_t batch, fl
                                  double *train_ms);
 mc_status mc_ctx_update_cells_warm(mc_ctx_t *ctx, const float *w, double scale, double xhi_limit, int32_t precision,
                                    mc_update_stats_t *stats);
-/* The warm start's fallback threshold: a prediction whose residual is at
- * least near_res x the heating (>= 0.01; default 0.3) goes back to the
- * plain solve. */
-mc_status mc_ctx_surrogate_fallback(mc_ctx_t *ctx, double near_res);
+/* The warm start's rule at the first T step, in units of the heating: a
+ * prediction whose thermal residual is below accept_res (0 < accept_res <=
+ * 0.01, the reference's own test; default 0.01) is accepted; below near_res
+ * (>= accept_res; default 0.3) it is bracketed from the prediction; from
+ * near_res up the cell goes back to the plain solve.  accept_res = near_res
+ * = 1e-3 is "accept below 1e-3, otherwise the plain solve". */
+mc_status mc_ctx_surrogate_rule(mc_ctx_t *ctx, double accept_res, double near_res);
 
 /* ---- diffuse-emission CDF on the GPU ---------------------------------------
  * emissionDriver + setDiffusePDF (emission_mod.f90:32-1311) for a gas grid:
@@ -432,7 +436,14 @@ mc_status mc_ctx_build_emission(mc_ctx_t *ctx, float *ms);
 mc_status mc_ctx_get_emission(mc_ctx_t *ctx, float *rec_rows, float *total_lines);
 /* Downloads the dust-emission CDF rows [Nc+1][nbins] (dust-only grids). */
 mc_status mc_ctx_get_dust_emission(mc_ctx_t *ctx, float *dust_rows);
-/* Parameters (33072 floats: W1[128][80] b1 W2[128][128] b2 W3[48][128] b3). */
+/* The collected training rows (features [n][80], targets [n][48], as
+ * collect forms them, not normalised): rows gives their count and, with x
+ * and t, copies them out; load appends rows (up to the capacity), e.g. the
+ * cell states of other models' updates, so one network learns from many. */
+mc_status mc_ctx_surrogate_rows(mc_ctx_t *ctx, int64_t *n, float *x, float *t);
+mc_status mc_ctx_surrogate_load(mc_ctx_t *ctx, int64_t n, const float *x, const float *t);
+/* Parameters (164656 floats: W1[256][80] b1 W2[256][256] b2 W3[256][256] b3
+ * W4[48][256] b4). */
 mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
 /* Loss and gradients of one batch (x [m][80], normalised targets t [m][48];
  * the first 41 columns count), and the outputs y [m][48]. */

@@ -465,6 +465,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       coolInt = __shfl_sync(0xffffffffu, coolInt, 0);
       const Real thResidual = heatInt - coolInt;
       bool again = false;
+      const bool first_warm = warm;
       if (warm) {
         warm = false;
         // a prediction far from balance: the cold solve from the state
@@ -482,7 +483,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
           continue;
         }
       }
-      if (fabs(thResidual) >= (Real)0.01 * heatInt) {
+      if (fabs(thResidual) >= (first_warm ? (Real)a.accept_res : (Real)0.01) * heatInt) {
         if (nIterT < 25) {
           bool open = false;
           if (thResidual < (Real)0) {

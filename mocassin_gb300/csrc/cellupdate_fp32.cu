@@ -203,7 +203,8 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
     float resHigh = w.sec[2 * nc1 + c], resLow = w.sec[3 * nc1 + c], fstep = w.sec[4 * nc1 + c];
     int nIterT = ++w.nit[c];
     bool again = false, noTe = false;
-    if (a.x_prev && nIterT == 1 && !(w.flags[c] & 4) && fabsf(res) >= (float)a.near_res * heat) {
+    const bool first_warm = a.x_prev && nIterT == 1 && !(w.flags[c] & 4);
+    if (first_warm && fabsf(res) >= (float)a.near_res * heat) {
       // a prediction far from balance: the cold solve from the state before
       // the prediction, with the full T-step allowance (one extra T step)
       const double *Xp = a.x_prev + (size_t)c * kX;
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
       w.act[cur ^ 1][atomicAdd(&w.count[cur ^ 1], 1)] = c;
       continue;
     }
-    if (fabsf(res) >= 0.01f * heat) {
+    if (fabsf(res) >= (first_warm ? (float)a.accept_res : 0.01f) * heat) {
       if (nIterT < 25) {
         bool open = false;
         if (res < 0.f) {

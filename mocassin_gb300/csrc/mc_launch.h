@@ -85,11 +85,12 @@ struct UpdArgs {
   double xhi;
   int mat_rows, mat_stride;  // FP32 form: matrix row length (max levels) and odd per-lane stride
   // warm start: the state before the prediction (null: cold).  At the first
-  // T step a prediction whose thermal residual is below 1 % of the heating is
-  // accepted; below near_res it is bracketed with small steps; otherwise the
-  // cell restarts the cold solve from this state (the plain solve as fallback).
+  // T step a prediction whose thermal residual is below accept_res (<= the
+  // reference's 1 %) of the heating is accepted; below near_res it is
+  // bracketed with small steps; otherwise the cell restarts the cold solve
+  // from this state (the plain solve as fallback).
   const double *te_prev, *ne_prev, *x_prev;  // x_prev [nc+1][7][8]
-  double near_res;
+  double accept_res, near_res;
   double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
   int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
 };
@@ -106,15 +107,13 @@ cudaError_t launch_species(int nc, int nsp, const int *sp_e, const int *sp_s, co
 void spline_natural(const double *x, const double *y, int n, double *y2);
 
 // ---- the learned warm start (mlp.cu) ----
-constexpr int kMlpIn = 80, kMlpHid = 128, kMlpOut = 48, kMlpTargets = 41;
+constexpr int kMlpIn = 80, kMlpHid = 256, kMlpOut = 48, kMlpTargets = 41;
 constexpr int kMlpW1 = 0, kMlpB1 = kMlpW1 + kMlpHid * kMlpIn, kMlpW2 = kMlpB1 + kMlpHid,
-              kMlpB2 = kMlpW2 + kMlpHid * kMlpHid, kMlpW3 = kMlpB2 + kMlpHid, kMlpB3 = kMlpW3 + kMlpOut * kMlpHid,
-              kMlpParams = kMlpB3 + kMlpOut;
-size_t mlp_dense_smem(int nin, int nout);
-cudaError_t launch_mlp_dense(int M, int nin, int nout, const float *in, int ldin, const float *mask, const float *W,
-                             bool transposed, const float *bias, int act, bool round_in, float *out, int ldout,
-                             cudaStream_t s);
-cudaError_t launch_mlp_wgrad(int M, int nin, int nout, const float *dz, const float *mask, const float *in, float *dW,
+              kMlpB2 = kMlpW2 + kMlpHid * kMlpHid, kMlpW3 = kMlpB2 + kMlpHid, kMlpB3 = kMlpW3 + kMlpHid * kMlpHid,
+              kMlpW4 = kMlpB3 + kMlpHid, kMlpB4 = kMlpW4 + kMlpOut * kMlpHid, kMlpParams = kMlpB4 + kMlpOut;
+cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const float *mask, bool round_a,
+                            const float *w, bool wt, const float *bias, int act, float *c, int ldc, cudaStream_t s);
+cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
                              float *db, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_loss(int M, int nt, int ld, const float *y, const float *tn, float *dy, double *loss,
                             cudaStream_t s);

@@ -129,11 +129,12 @@ struct mc_ctx {
   int u_bal_z[7] = {}, u_bal_first[7] = {};
   // learned warm start: parameters, Adam state, training buffer, work arrays
   DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss, m_dstep;
-  DBuf m_xb, m_tb, m_a1, m_a2, m_y, m_dy, m_d2, m_d1, m_xi, m_h1, m_h2, m_yi, m_te_prev, m_ne_prev, m_x_prev;
+  DBuf m_xb, m_tb, m_a1, m_a2, m_a3, m_y, m_dy, m_d3, m_d2, m_d1, m_xi, m_h1, m_h2, m_h3, m_yi, m_te_prev, m_ne_prev, m_x_prev;
   long long m_cap = 0, m_n = 0;
   int m_step = 0, m_B = 0;
   bool m_ready = false, m_norm = false;
   double m_near_res = 0.3;  // warm start: residual / heating below which a prediction is bracketed
+  double m_accept_res = 0.01;  // ... and below which it is accepted
   // diffuse-emission CDF: derived tables (one buffer) and forbidden-line totals
   DBuf e_tab, e_forb;
   DBuf d_tdust;      // grain temperatures of the last mc_ctx_dust_temperatures [nsizes+1][nc+1]
@@ -1375,6 +1376,7 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   a.ne_prev = warm ? c->m_ne_prev.as<double>() : nullptr;
   a.x_prev = warm ? c->m_x_prev.as<double>() : nullptr;
   a.near_res = c->m_near_res;
+  a.accept_res = c->m_accept_res;
   // a predicted Te is near the balance: bracket it with small steps first
   a.step0 = warm ? 1.03 : 1.2;
   a.step_grow = warm ? 1 : 0;
@@ -1475,18 +1477,21 @@ mc_status ensure(DBuf &b, size_t bytes) {
   return MC_OK;
 }
 
-// forward pass of M rows: x [M][80] -> a1, a2 [M][128] -> y [M][48]
-mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, float *y) {
+// forward pass of M rows: x [M][80] -> a1, a2, a3 [M][256] -> y [M][48]
+mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, float *a3, float *y) {
   const float *W = c->m_w.as<float>();
   cudaStream_t s = c->stream;
-  cudaError_t e = mcg::launch_mlp_dense(M, kMlpIn, kMlpHid, x, kMlpIn, nullptr, W + mcg::kMlpW1, false,
-                                        W + mcg::kMlpB1, 1, true, a1, kMlpHid, s);
+  cudaError_t e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpIn, x, kMlpIn, nullptr, true, W + mcg::kMlpW1, true,
+                                       W + mcg::kMlpB1, 1, a1, kMlpHid, s);
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpHid, a1, kMlpHid, nullptr, W + mcg::kMlpW2, false, W + mcg::kMlpB2, 1,
-                              true, a2, kMlpHid, s);
+    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, a1, kMlpHid, nullptr, true, W + mcg::kMlpW2, true, W + mcg::kMlpB2,
+                             1, a2, kMlpHid, s);
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpOut, a2, kMlpHid, nullptr, W + mcg::kMlpW3, false, W + mcg::kMlpB3, 0,
-                              true, y, kMlpOut, s);
+    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, a2, kMlpHid, nullptr, true, W + mcg::kMlpW3, true, W + mcg::kMlpB3,
+                             1, a3, kMlpHid, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_gemm(M, kMlpOut, kMlpHid, a3, kMlpHid, nullptr, true, W + mcg::kMlpW4, true, W + mcg::kMlpB4,
+                             0, y, kMlpOut, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp forward failed: %s", cudaGetErrorString(e));
   return MC_OK;
 }
@@ -1495,32 +1500,41 @@ mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, 
 mc_status mlp_backward(mc_ctx_t *c, int M, const float *x, const float *t) {
   cudaStream_t s = c->stream;
   mc_status st;
-  if ((st = ensure(c->m_a1, (size_t)M * kMlpHid * 4)) || (st = ensure(c->m_a2, (size_t)M * kMlpHid * 4)) ||
-      (st = ensure(c->m_y, (size_t)M * kMlpOut * 4)) || (st = ensure(c->m_dy, (size_t)M * kMlpOut * 4)) ||
-      (st = ensure(c->m_d2, (size_t)M * kMlpHid * 4)) || (st = ensure(c->m_d1, (size_t)M * kMlpHid * 4)))
+  const size_t h = (size_t)M * kMlpHid * 4, o = (size_t)M * kMlpOut * 4;
+  if ((st = ensure(c->m_a1, h)) || (st = ensure(c->m_a2, h)) || (st = ensure(c->m_a3, h)) ||
+      (st = ensure(c->m_y, o)) || (st = ensure(c->m_dy, o)) || (st = ensure(c->m_d3, h)) ||
+      (st = ensure(c->m_d2, h)) || (st = ensure(c->m_d1, h)))
     return st;
-  float *a1 = c->m_a1.as<float>(), *a2 = c->m_a2.as<float>(), *y = c->m_y.as<float>(), *dy = c->m_dy.as<float>();
-  float *d2 = c->m_d2.as<float>(), *d1 = c->m_d1.as<float>();
-  if ((st = mlp_forward(c, M, x, a1, a2, y))) return st;
+  float *a1 = c->m_a1.as<float>(), *a2 = c->m_a2.as<float>(), *a3 = c->m_a3.as<float>();
+  float *y = c->m_y.as<float>(), *dy = c->m_dy.as<float>();
+  float *d3 = c->m_d3.as<float>(), *d2 = c->m_d2.as<float>(), *d1 = c->m_d1.as<float>();
+  if ((st = mlp_forward(c, M, x, a1, a2, a3, y))) return st;
   const float *W = c->m_w.as<float>();
   float *G = c->m_g.as<float>();
   MC_CUDA(cudaMemsetAsync(G, 0, kMlpParams * sizeof(float), s));
+  const int sm = c->num_sms;
   cudaError_t e = mcg::launch_mlp_loss(M, mcg::kMlpTargets, kMlpOut, y, t, dy, c->m_loss.as<double>(), s);
-  // layer 3 (linear): dW3 = dY^T a2, dA2 = dY W3
+  // layer 4 (linear): dW4 = dY^T a3, dA3 = dY W4
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpOut, dy, nullptr, a2, G + mcg::kMlpW3, G + mcg::kMlpB3, c->num_sms, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpOut, kMlpHid, dy, nullptr, a3, G + mcg::kMlpW4, G + mcg::kMlpB4, sm, s);
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_dense(M, kMlpOut, kMlpHid, dy, kMlpOut, nullptr, W + mcg::kMlpW3, true, nullptr, 0, false, d2,
-                              kMlpHid, s);
+    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpOut, dy, kMlpOut, nullptr, false, W + mcg::kMlpW4, false, nullptr, 0, d3,
+                             kMlpHid, s);
+  // layer 3 (ReLU): dZ3 = dA3 (a3 > 0)
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d3, a3, a2, G + mcg::kMlpW3, G + mcg::kMlpB3, sm, s);
+  if (e == cudaSuccess)
+    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, d3, kMlpHid, a3, false, W + mcg::kMlpW3, false, nullptr, 0, d2,
+                             kMlpHid, s);
   // layer 2 (ReLU): dZ2 = dA2 (a2 > 0)
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d2, a2, a1, G + mcg::kMlpW2, G + mcg::kMlpB2, c->num_sms, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d2, a2, a1, G + mcg::kMlpW2, G + mcg::kMlpB2, sm, s);
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_dense(M, kMlpHid, kMlpHid, d2, kMlpHid, a2, W + mcg::kMlpW2, true, nullptr, 0, false, d1,
-                              kMlpHid, s);
+    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, d2, kMlpHid, a2, false, W + mcg::kMlpW2, false, nullptr, 0, d1,
+                             kMlpHid, s);
   // layer 1 (ReLU): dZ1 = dA1 (a1 > 0)
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpIn, kMlpHid, d1, a1, x, G + mcg::kMlpW1, G + mcg::kMlpB1, c->num_sms, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpIn, d1, a1, x, G + mcg::kMlpW1, G + mcg::kMlpB1, sm, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp backward failed: %s", cudaGetErrorString(e));
   return MC_OK;
 }
@@ -1530,7 +1544,8 @@ mc_status surrogate_predict_state(mc_ctx_t *c) {
   cudaStream_t s = c->stream;
   mc_status st;
   if ((st = ensure(c->m_xi, (size_t)nc1 * kMlpIn * 4)) || (st = ensure(c->m_h1, (size_t)nc1 * kMlpHid * 4)) ||
-      (st = ensure(c->m_h2, (size_t)nc1 * kMlpHid * 4)) || (st = ensure(c->m_yi, (size_t)nc1 * kMlpOut * 4)) ||
+      (st = ensure(c->m_h2, (size_t)nc1 * kMlpHid * 4)) || (st = ensure(c->m_h3, (size_t)nc1 * kMlpHid * 4)) ||
+      (st = ensure(c->m_yi, (size_t)nc1 * kMlpOut * 4)) ||
       (st = ensure(c->m_te_prev, (size_t)nc1 * 8)) || (st = ensure(c->m_ne_prev, (size_t)nc1 * 8)) ||
       (st = ensure(c->m_x_prev, (size_t)nc1 * 56 * 8)))
     return st;
@@ -1538,7 +1553,8 @@ mc_status surrogate_predict_state(mc_ctx_t *c) {
                                                  c->m_fmean.as<float>(), c->m_fstd.as<float>(), c->m_xi.as<float>(),
                                                  c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "features failed: %s", cudaGetErrorString(e));
-  if ((st = mlp_forward(c, nc1, c->m_xi.as<float>(), c->m_h1.as<float>(), c->m_h2.as<float>(), c->m_yi.as<float>())))
+  if ((st = mlp_forward(c, nc1, c->m_xi.as<float>(), c->m_h1.as<float>(), c->m_h2.as<float>(), c->m_h3.as<float>(),
+                        c->m_yi.as<float>())))
     return st;
   e = mcg::launch_mlp_apply(c->nc, c->s_mom.as<float>(), c->m_yi.as<float>(), c->m_tmean.as<float>(),
                             c->m_tstd.as<float>(), c->s_te.as<double>(), c->s_ne.as<double>(), c->s_X.as<double>(),
@@ -1581,8 +1597,10 @@ mc_status surrogate_normalise(mc_ctx_t *c) {
 
 }  // namespace
 
-extern "C" mc_status mc_ctx_surrogate_fallback(mc_ctx_t *c, double near_res) {
-  if (!c || !(near_res >= 0.01)) return set_error(MC_ERR_ARG, "ctx and near_res >= 0.01 are required");
+extern "C" mc_status mc_ctx_surrogate_rule(mc_ctx_t *c, double accept_res, double near_res) {
+  if (!c || !(accept_res > 0. && accept_res <= 0.01) || !(near_res >= accept_res))
+    return set_error(MC_ERR_ARG, "ctx, 0 < accept_res <= 0.01 and near_res >= accept_res are required");
+  c->m_accept_res = accept_res;
   c->m_near_res = near_res;
   return MC_OK;
 }
@@ -1603,7 +1621,8 @@ extern "C" mc_status mc_ctx_surrogate_init(mc_ctx_t *c, uint64_t seed, int64_t c
   };
   fill(mcg::kMlpW1, kMlpHid, 68);
   fill(mcg::kMlpW2, kMlpHid, kMlpHid);
-  fill(mcg::kMlpW3, kMlpOut, kMlpHid);
+  fill(mcg::kMlpW3, kMlpHid, kMlpHid);
+  fill(mcg::kMlpW4, kMlpOut, kMlpHid);
   for (int o = 0; o < kMlpHid; ++o)
     for (int i = 68; i < kMlpIn; ++i) w[mcg::kMlpW1 + o * kMlpIn + i] = 0.f;
   mc_status st;
@@ -1707,6 +1726,33 @@ extern "C" mc_status mc_ctx_surrogate_train(mc_ctx_t *c, int32_t steps, int32_t 
   cudaEventDestroy(e1);
   if (loss) *loss = steps > 0 ? last / ((double)batch * mcg::kMlpTargets) : 0.;
   if (train_ms) *train_ms = ms;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_rows(mc_ctx_t *c, int64_t *n, float *x, float *t) {
+  if (!c || !c->m_ready || !n) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
+  const long long rows = std::min(c->m_n, c->m_cap);
+  *n = rows;
+  if (x) MC_CUDA(cudaMemcpyAsync(x, c->m_xs.p, (size_t)rows * kMlpIn * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (t) MC_CUDA(cudaMemcpyAsync(t, c->m_ts.p, (size_t)rows * kMlpOut * 4, cudaMemcpyDeviceToHost, c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_load(mc_ctx_t *c, int64_t n, const float *x, const float *t) {
+  if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
+  if (n < 0 || (n > 0 && (!x || !t))) return set_error(MC_ERR_ARG, "n >= 0 rows with x and t required");
+  const long long have = std::min(c->m_n, c->m_cap), take = std::min((long long)n, c->m_cap - have);
+  if (take > 0) {
+    MC_CUDA(cudaMemcpyAsync(c->m_xs.as<float>() + (size_t)have * kMlpIn, x, (size_t)take * kMlpIn * 4,
+                            cudaMemcpyHostToDevice, c->stream));
+    MC_CUDA(cudaMemcpyAsync(c->m_ts.as<float>() + (size_t)have * kMlpOut, t, (size_t)take * kMlpOut * 4,
+                            cudaMemcpyHostToDevice, c->stream));
+  }
+  const unsigned long long total = (unsigned long long)(have + std::max(take, 0ll));
+  MC_CUDA(cudaMemcpyAsync(c->m_count.p, &total, 8, cudaMemcpyHostToDevice, c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  c->m_n = (long long)total;
   return MC_OK;
 }
 

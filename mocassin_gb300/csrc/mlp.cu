@@ -1,22 +1,24 @@
-// mlp.cu -- the learned warm start of the cell update: a small MLP from the
-// Jste sums of a cell (log10 of the 33 photoionisation and 33 heating sums,
-// of sum Jste and of Hden) to log10 Te and log10 of the 40 ionic fractions,
+// mlp.cu -- the learned warm start of the cell update: an MLP from the Jste
+// sums of a cell (log10 of the 33 photoionisation and 33 heating sums, of
+// sum Jste and of Hden) to log10 Te and log10 of the 40 ionic fractions,
 // trained on the GPU on cell states that the cell update produced.
 //
-// Network 80 -> 128 (ReLU) -> 128 (ReLU) -> 48 (padded sizes; 68 features,
-// 41 targets).  Arithmetic: each layer rounds its inputs and its weights to
-// BF16 and accumulates in FP32 (the operand precision of a BF16 tensor-core
-// product), weights kept in FP32 for Adam.  The layers run on CUDA cores:
-// the whole network is ~66 kFLOP per cell (15 GFLOP for a 61^3 grid, well
-// under a millisecond), nothing next to the cell update it warm-starts.
+// Network: four layers, 80 -> 256 (ReLU) -> 256 (ReLU) -> 256 (ReLU) -> 48
+// (padded sizes; 68 features, 41 targets).  Arithmetic: each layer rounds its
+// operands to BF16 and accumulates in FP32 (the operand precision of a BF16
+// tensor-core product), weights kept in FP32 for Adam.  The layers run on
+// CUDA cores as tiled GEMMs: ~330 kFLOP per cell forward, a few ms for a
+// 101^3 grid.
 //
 // Kernels
-//   mlp_dense_kernel   out[m][o] = act(b[o] + sum_i bf16(in[m][i]) bf16(S[i][o]))
-//                      for 128 rows per block; S is the layer's weight matrix
-//                      staged in shared memory in (input, output) order, so
-//                      the same kernel gives the forward pass (S = W^T) and
-//                      the data gradient (S = W, inputs dZ, ReLU' fused)
-//   mlp_wgrad_kernel   dW[o][i] += sum_m dZ[m][o] bf16(in[m][i]), db[o] += sum dZ
+//   mlp_gemm_kernel    C[m][n] = act(b[n] + sum_k A(m,k) B(k,n)) in 64 x 64
+//                      tiles, 16-deep K steps through shared memory, 4 x 4
+//                      outputs per thread; B is a layer's weights read as
+//                      W^T (forward) or W (data gradient, the ReLU mask of
+//                      the layer output fused on A)
+//   mlp_wgrad_kernel   dW[n][k] += sum_m dZ(m,n) bf16(X(m,k)) in 64 x 64 tiles,
+//                      the rows split over blocks (FP32 atomics); the bias
+//                      gradient in mlp_bgrad_kernel
 //   mlp_loss_kernel    dY = 2 (Y - T) / (B 41) on the 41 targets, sum of squares
 //   mlp_adam_kernel    Adam (beta 0.9 / 0.999, eps 1e-8) on the FP32 weights
 //   features / apply   the per-cell features from the moments, and the
@@ -24,6 +26,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -36,96 +39,143 @@ namespace {
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-constexpr int kRows = 128;
+constexpr int kTM = 64, kTN = 64, kTK = 16;  // GEMM tile: rows, columns, depth
 
-// act: 0 linear, 1 ReLU.  mask (data gradient): inputs are multiplied by
-// (mask[m][i] > 0), the ReLU derivative of the layer output they belong to.
-// Block (x, y): rows 128 x .. 128 x + 127, outputs 16 y .. 16 y + 15.
-constexpr int kOC = 16;
-__global__ void __launch_bounds__(kRows) mlp_dense_kernel(int M, int nin, int nout, const float *in, int ldin,
-                                                          const float *mask, const float *W, bool transposed,
-                                                          const float *bias, int act, bool round_in, float *out,
-                                                          int ldout) {
-  extern __shared__ float sh[];
-  float *S = sh;                        // [nin][kOC]
-  float *X = sh + (size_t)nin * kOC;    // [nin][kRows]
-  const int t = threadIdx.x, m = blockIdx.x * kRows + t, o0 = blockIdx.y * kOC;
-  // weights: forward S[i][o] = W[o][i] (W is [nout][nin]); data gradient
-  // S[i][o] = W[i][o] (W is [nin][nout] = the forward layer's [out][in])
-  for (int q = t; q < nin * kOC; q += kRows) {
-    const int i = q / kOC, o = o0 + q % kOC;
-    S[q] = bf16r(transposed ? W[(size_t)i * nout + o] : W[(size_t)o * nin + i]);
-  }
-  for (int i = 0; i < nin; ++i) {
-    float v = 0.f;
-    if (m < M) {
-      v = in[(size_t)m * ldin + i];
-      if (mask && !(mask[(size_t)m * ldin + i] > 0.f)) v = 0.f;
-      if (round_in) v = bf16r(v);
+// C[m][n] = act(bias[n] + sum_k A(m,k) B(k,n)), A(m,k) = a[m*lda + k] (zero
+// where mask[m*lda + k] <= 0, BF16-rounded if round_a), B(k,n) = bf16 of
+// w[n*K + k] (wt: a layer's [N][K] weights, the forward pass) or w[k*N + n]
+// (the data gradient through a layer of [K][N] weights).  256 threads.
+__global__ void __launch_bounds__(256) mlp_gemm_kernel(int M, int N, int K, const float *a, int lda,
+                                                       const float *mask, bool round_a, const float *w, bool wt,
+                                                       const float *bias, int act, float *c, int ldc) {
+  __shared__ float As[kTK][kTM + 4], Bs[kTK][kTN + 4];
+  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * kTN;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += kTK) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int q = t + 256 * e;
+      {  // A: 64 rows x 16 k, k fastest
+        const int r = q / kTK, k = q % kTK, m = m0 + r, kk = k0 + k;
+        float v = 0.f;
+        if (m < M && kk < K) {
+          v = a[(size_t)m * lda + kk];
+          if (mask && !(mask[(size_t)m * lda + kk] > 0.f)) v = 0.f;
+          if (round_a) v = bf16r(v);
+        }
+        As[k][r] = v;
+      }
+      if (wt) {  // B(k,n) = w[n][k]: k fastest
+        const int n = q / kTK, k = q % kTK, nn = n0 + n, kk = k0 + k;
+        Bs[k][n] = nn < N && kk < K ? bf16r(w[(size_t)nn * K + kk]) : 0.f;
+      } else {   // B(k,n) = w[k][n]: n fastest
+        const int k = q / kTN, n = q % kTN, nn = n0 + n, kk = k0 + k;
+        Bs[k][n] = nn < N && kk < K ? bf16r(w[(size_t)kk * N + nn]) : 0.f;
+      }
     }
-    X[i * kRows + t] = v;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kTK; ++k) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[k][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[k][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += av[i] * bv[j];
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  if (m >= M) return;
-  float acc[kOC];
 #pragma unroll
-  for (int j = 0; j < kOC; ++j) acc[j] = bias ? bias[o0 + j] : 0.f;
-  for (int i = 0; i < nin; ++i) {
-    const float x = X[i * kRows + t];
-    const float *sr = S + (size_t)i * kOC;
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty * 4 + i;
+    if (m >= M) continue;
 #pragma unroll
-    for (int j = 0; j < kOC; ++j) acc[j] += x * sr[j];
-  }
-#pragma unroll
-  for (int j = 0; j < kOC; ++j) {
-    float v = acc[j];
-    if (act == 1) v = v > 0.f ? v : 0.f;
-    out[(size_t)m * ldout + o0 + j] = v;
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tx * 4 + j;
+      if (n >= N) continue;
+      float v = acc[i][j] + (bias ? bias[n] : 0.f);
+      if (act == 1) v = v > 0.f ? v : 0.f;
+      c[(size_t)m * ldc + n] = v;
+    }
   }
 }
 
-// dW[o][i] += sum_m dZ[m][o] * bf16(in[m][i]); db[o] += sum_m dZ[m][o]
-__global__ void __launch_bounds__(256) mlp_wgrad_kernel(int M, int nin, int nout, const float *dz, const float *mask,
-                                                        const float *in, float *dW, float *db) {
-  constexpr int R = 32;
-  extern __shared__ float sh[];
-  float *Z = sh;                    // [R][nout]
-  float *X = sh + R * nout;         // [R][nin]
-  const int t = threadIdx.x;
-  const int npair = nin * nout;
-  const int per = (npair + 255) / 256;  // <= 64
-  float acc[64];
-  for (int p = 0; p < 64; ++p) acc[p] = 0.f;
-  float bacc = 0.f;
-  for (int r0 = blockIdx.x * R; r0 < M; r0 += gridDim.x * R) {
+// dW[n][k] += sum_m dZ(m,n) bf16(X(m,k)), dZ(m,n) = dz[m*N + n] (zero where
+// mask[m*N + n] <= 0); tiles of 64 n x 64 k, rows split over blockIdx.z
+__global__ void __launch_bounds__(256) mlp_wgrad_kernel(int M, int N, int K, const float *dz, const float *mask,
+                                                        const float *x, float *dW, int rows_per_split) {
+  __shared__ float Zs[kTK][kTN + 4], Xs[kTK][kTN + 4];
+  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+  const int n0 = blockIdx.x * kTN, k0 = blockIdx.y * kTN;
+  const int mb = blockIdx.z * rows_per_split, me = min(M, mb + rows_per_split);
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int r0 = mb; r0 < me; r0 += kTK) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int q = t + 256 * e;
+      const int r = q / kTN, col = q % kTN, m = r0 + r;
+      float zv = 0.f, xv = 0.f;
+      if (m < me) {
+        const int n = n0 + col, k = k0 + col;
+        if (n < N) {
+          zv = dz[(size_t)m * N + n];
+          if (mask && !(mask[(size_t)m * N + n] > 0.f)) zv = 0.f;
+        }
+        if (k < K) xv = bf16r(x[(size_t)m * K + k]);
+      }
+      Zs[r][col] = zv;
+      Xs[r][col] = xv;
+    }
     __syncthreads();
-    for (int q = t; q < R * nout; q += 256) {
-      const int r = q / nout, o = q % nout;
-      float v = r0 + r < M ? dz[(size_t)(r0 + r) * nout + o] : 0.f;
-      if (mask && r0 + r < M && !(mask[(size_t)(r0 + r) * nout + o] > 0.f)) v = 0.f;
-      Z[q] = v;
-    }
-    for (int q = t; q < R * nin; q += 256) {
-      const int r = q / nin, i = q % nin;
-      X[q] = r0 + r < M ? bf16r(in[(size_t)(r0 + r) * nin + i]) : 0.f;
+#pragma unroll
+    for (int r = 0; r < kTK; ++r) {
+      float zv[4], xv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) zv[i] = Zs[r][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) xv[j] = Xs[r][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += zv[i] * xv[j];
     }
     __syncthreads();
-    for (int p = 0; p < per; ++p) {
-      const int q = p * 256 + t;
-      if (q >= npair) break;
-      const int o = q / nin, i = q % nin;
-      float a = acc[p];
-      for (int r = 0; r < R; ++r) a += Z[r * nout + o] * X[r * nin + i];
-      acc[p] = a;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int n = n0 + ty * 4 + i;
+    if (n >= N) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = k0 + tx * 4 + j;
+      if (k < K) atomicAdd(&dW[(size_t)n * K + k], acc[i][j]);
     }
-    if (t < nout)
-      for (int r = 0; r < R; ++r) bacc += Z[r * nout + t];
   }
-  for (int p = 0; p < per; ++p) {
-    const int q = p * 256 + t;
-    if (q < npair) atomicAdd(&dW[q], acc[p]);
-  }
-  if (t < nout) atomicAdd(&db[t], bacc);
+}
+
+// db[n] += sum_m dZ(m,n)
+__global__ void mlp_bgrad_kernel(int M, int N, const float *dz, const float *mask, float *db) {
+  const int n = blockIdx.x * 32 + (threadIdx.x & 31);
+  float acc = 0.f;
+  if (n < N)
+    for (int m = blockIdx.y * 8 + (threadIdx.x >> 5); m < M; m += gridDim.y * 8) {
+      float v = dz[(size_t)m * N + n];
+      if (mask && !(mask[(size_t)m * N + n] > 0.f)) v = 0.f;
+      acc += v;
+    }
+  if (n < N) atomicAdd(&db[n], acc);
 }
 
 // dY[m][o] = 2 (Y - Tn) / (M * nt) for o < nt; loss += sum (Y - Tn)^2
@@ -282,29 +332,27 @@ __global__ void mlp_apply_kernel(int nc, const float *mom, const float *y, const
 
 }  // namespace
 
-size_t mlp_dense_smem(int nin, int nout) {
-  (void)nout;
-  return ((size_t)nin * kOC + (size_t)nin * kRows) * sizeof(float);
-}
-
-cudaError_t launch_mlp_dense(int M, int nin, int nout, const float *in, int ldin, const float *mask, const float *W,
-                             bool transposed, const float *bias, int act, bool round_in, float *out, int ldout,
-                             cudaStream_t s) {
-  if (nout % 16 != 0 || nin > kMlpHid) return cudaErrorInvalidValue;
-  const size_t sh = mlp_dense_smem(nin, nout);  // within the limit mlp_prepare set
-  mlp_dense_kernel<<<dim3((M + kRows - 1) / kRows, nout / kOC), kRows, sh, s>>>(M, nin, nout, in, ldin, mask, W,
-                                                                                transposed, bias, act, round_in, out,
-                                                                                ldout);
+cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const float *mask, bool round_a,
+                            const float *w, bool wt, const float *bias, int act, float *c, int ldc, cudaStream_t s) {
+  if (M < 1 || N < 1 || K < 1) return cudaErrorInvalidValue;
+  mlp_gemm_kernel<<<dim3((M + kTM - 1) / kTM, (N + kTN - 1) / kTN), 256, 0, s>>>(M, N, K, a, lda, mask, round_a, w,
+                                                                                wt, bias, act, c, ldc);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_wgrad(int M, int nin, int nout, const float *dz, const float *mask, const float *in, float *dW,
+cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
                              float *db, int num_sms, cudaStream_t s) {
-  if (nin * nout > 64 * 256 || nout > 256) return cudaErrorInvalidValue;
-  const size_t sh = (size_t)32 * (nin + nout) * sizeof(float);
-  int blocks = (M + 31) / 32;
-  if (blocks > num_sms * 2) blocks = num_sms * 2;
-  mlp_wgrad_kernel<<<blocks, 256, sh, s>>>(M, nin, nout, dz, mask, in, dW, db);
+  if (M < 1 || N < 1 || K < 1) return cudaErrorInvalidValue;
+  const int tiles = ((N + kTN - 1) / kTN) * ((K + kTN - 1) / kTN);
+  // enough row splits to fill the SMs twice, at least 64 rows each
+  int splits = std::max(1, std::min((M + 63) / 64, (2 * num_sms + tiles - 1) / tiles));
+  const int per = ((M + splits - 1) / splits + kTK - 1) / kTK * kTK;
+  splits = (M + per - 1) / per;
+  mlp_wgrad_kernel<<<dim3((N + kTN - 1) / kTN, (K + kTN - 1) / kTN, splits), 256, 0, s>>>(M, N, K, dz, mask, x, dW,
+                                                                                          per);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !db) return e;
+  mlp_bgrad_kernel<<<dim3((N + 31) / 32, std::max(1, std::min(64, (M + 255) / 256))), 256, 0, s>>>(M, N, dz, mask, db);
   return cudaGetLastError();
 }
 
@@ -332,10 +380,7 @@ cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dste
   return cudaGetLastError();
 }
 
-cudaError_t mlp_prepare() {
-  return cudaFuncSetAttribute(mlp_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)mlp_dense_smem(kMlpHid, kMlpHid));
-}
+cudaError_t mlp_prepare() { return cudaSuccess; }
 
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s) {
   mlp_stats_kernel<<<dim3(64, cols), 256, 0, s>>>(n, cols, a, sum, sq);

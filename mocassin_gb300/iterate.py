@@ -48,8 +48,12 @@ class LambdaIteration:
                  emission="auto"):
         """surrogate: None (updates start from the previous state, as the
         reference's) or a dict with train_after (cold iterations whose cell
-        states train the MLP first), steps, batch, lr, finetune_steps (after
-        every later iteration), capacity (training rows kept)."""
+        states train the MLP first; None: never), steps, batch, lr,
+        finetune_steps (after every later iteration), capacity (training rows
+        kept), rows (an (x, t) pair of training rows from other models, e.g.
+        training_rows(); the network is trained on them before the first
+        update and warm-starts every update), rule ((accept_res, near_res) of
+        mc_ctx_surrogate_rule)."""
         self.neb = neb
         self.form = form
         self.update = update
@@ -77,10 +81,21 @@ class LambdaIteration:
         self.history = []
         self.sur = None
         self.trained = False
+        self.pretrain = None
         if surrogate is not None:
             self.sur = dict({"train_after": 2, "steps": 500, "batch": 4096, "lr": 3e-3, "finetune_steps": 0,
-                             "capacity": 1_000_000, "seed": 1}, **surrogate)
-            self.ctx.surrogate_init(seed=self.sur["seed"], capacity=self.sur["capacity"])
+                             "capacity": 1_000_000, "seed": 1, "rows": None, "rule": None}, **surrogate)
+            rows = self.sur["rows"]
+            cap = max(self.sur["capacity"], (len(rows[0]) if rows is not None else 0) + neb.ncells + 1)
+            self.ctx.surrogate_init(seed=self.sur["seed"], capacity=cap)
+            if self.sur["rule"] is not None:
+                self.ctx.surrogate_rule(*self.sur["rule"])
+            if rows is not None:
+                self.ctx.surrogate_load(*rows)
+                loss, ms = self.ctx.surrogate_train(self.sur["steps"], self.sur["batch"], self.sur["lr"],
+                                                    self.sur["seed"])
+                self.trained = True
+                self.pretrain = {"rows": int(len(rows[0])), "loss": loss, "train_ms": ms}
 
     def step(self, seed, n_packets=None):
         t0 = time.perf_counter()
@@ -91,9 +106,10 @@ class LambdaIteration:
         up = self.ctx.update_cells(self.w, self.scale, xhi_limit=self.xhi, precision=self.update, warm=warm)
         t2 = time.perf_counter()
         train_ms, loss = 0.0, None
-        if self.sur is not None:
+        if self.sur is not None and (self.sur["rows"] is None or self.sur["finetune_steps"] > 0):
             self.ctx.surrogate_collect()
-            if not self.trained and len(self.history) + 1 >= self.sur["train_after"]:
+            if (not self.trained and self.sur["train_after"] is not None
+                    and len(self.history) + 1 >= self.sur["train_after"]):
                 loss, train_ms = self.ctx.surrogate_train(self.sur["steps"], self.sur["batch"], self.sur["lr"],
                                                           self.sur["seed"])
                 self.trained = True
@@ -150,3 +166,37 @@ class LambdaIteration:
 
     def close(self):
         self.ctx.close()
+
+
+def training_rows(specs, max_rows=1_000_000, iterations=2, update="fp64", form="graph", seed=1):
+    """Training rows for the warm start from other models: the cell states
+    that the plain update (FP64 by default) produced in the first
+    ``iterations`` Lambda iterations of each model of ``specs`` in turn (e.g.
+    the 64-model batch), until ``max_rows`` rows (a seeded subsample of the
+    last model's rows fills the count).  Returns (x, t, info)."""
+    t0 = time.perf_counter()
+    xs, ts, used, upd_s = [], [], [], 0.0
+    n = 0
+    rng = np.random.default_rng(seed)
+    for spec in specs:
+        neb = nebula.build(spec)
+        li = LambdaIteration(neb, form=form, update=update,
+                             surrogate={"train_after": None, "capacity": (neb.ncells + 1) * iterations})
+        for it in range(iterations):
+            upd_s += li.step(seed=seed + 101 * it)["update_s"]
+        x, t = li.ctx.surrogate_rows()
+        li.close()
+        if n + len(x) > max_rows:
+            keep = np.sort(rng.choice(len(x), max_rows - n, replace=False))
+            x, t = x[keep], t[keep]
+        xs.append(x)
+        ts.append(t)
+        n += len(x)
+        used.append(spec.name)
+        if n >= max_rows:
+            break
+    x = np.concatenate(xs) if xs else np.zeros((0, 80), np.float32)
+    t = np.concatenate(ts) if ts else np.zeros((0, 48), np.float32)
+    return x, t, {"models": used, "rows": int(n), "iterations_per_model": iterations, "update": update,
+                  "update_s": upd_s, "wall_s": time.perf_counter() - t0}
+

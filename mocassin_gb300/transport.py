@@ -86,8 +86,12 @@ def library():
         lib.mc_ctx_set_fixed_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp]
         u64 = C.c_uint64
         lib.mc_ctx_surrogate_init.restype = C.c_int
-        lib.mc_ctx_surrogate_fallback.restype = C.c_int
-        lib.mc_ctx_surrogate_fallback.argtypes = [C.c_void_p, C.c_double]
+        lib.mc_ctx_surrogate_rows.restype = C.c_int
+        lib.mc_ctx_surrogate_rows.argtypes = [C.c_void_p, C.POINTER(C.c_int64), fp, fp]
+        lib.mc_ctx_surrogate_load.restype = C.c_int
+        lib.mc_ctx_surrogate_load.argtypes = [C.c_void_p, C.c_int64, fp, fp]
+        lib.mc_ctx_surrogate_rule.restype = C.c_int
+        lib.mc_ctx_surrogate_rule.argtypes = [C.c_void_p, C.c_double, C.c_double]
         lib.mc_ctx_surrogate_init.argtypes = [C.c_void_p, u64, C.c_int64]
         lib.mc_ctx_surrogate_collect.restype = C.c_int
         lib.mc_ctx_surrogate_collect.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
@@ -343,15 +347,33 @@ class TransportContext:
         return st.as_dict()
 
     # ---- the learned warm start ----
-    N_PARAMS = 33072
+    N_PARAMS = 164656
 
     def surrogate_init(self, seed=1, capacity=2_000_000):
         _check(self.lib.mc_ctx_surrogate_init(self.handle, int(seed), int(capacity)))
 
-    def surrogate_fallback(self, near_res):
-        """Residual / heating at the prediction from which a warm start falls
-        back to the plain solve (mc_ctx_surrogate_fallback)."""
-        _check(self.lib.mc_ctx_surrogate_fallback(self.handle, float(near_res)))
+    def surrogate_rows(self):
+        """The collected training rows: features (n, 80), targets (n, 48)."""
+        n = C.c_int64()
+        _check(self.lib.mc_ctx_surrogate_rows(self.handle, C.byref(n), None, None))
+        x = np.empty((n.value, 80), dtype=np.float32)
+        t = np.empty((n.value, 48), dtype=np.float32)
+        _check(self.lib.mc_ctx_surrogate_rows(self.handle, C.byref(n), _fptr(x), _fptr(t)))
+        return x, t
+
+    def surrogate_load(self, x, t):
+        """Appends training rows (e.g. other models' cell states)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        if x.shape[1:] != (80,) or t.shape != (len(x), 48):
+            raise ValueError("x (n, 80) and t (n, 48)")
+        _check(self.lib.mc_ctx_surrogate_load(self.handle, len(x), _fptr(x), _fptr(t)))
+
+    def surrogate_rule(self, accept_res=0.01, near_res=0.3):
+        """The warm start's rule (mc_ctx_surrogate_rule): accept a prediction
+        whose residual / heating is below accept_res, bracket it below
+        near_res, else fall back to the plain solve."""
+        _check(self.lib.mc_ctx_surrogate_rule(self.handle, float(accept_res), float(near_res)))
 
     def surrogate_collect(self):
         n = C.c_int64()

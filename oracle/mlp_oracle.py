@@ -1,16 +1,20 @@
 """CPU oracle of the warm-start MLP (test infrastructure): forward pass,
 mean-squared loss and gradients in FP64 with the GPU's BF16 rounding of
-layer inputs and weights (round to nearest even), for checking the GPU's
-own training kernels.  Layout of the parameters as mc_ctx_surrogate_params."""
+layer operands (round to nearest even), for checking the GPU's own training
+kernels.  Four layers 80 -> 256 -> 256 -> 256 -> 48 with ReLU on the hidden
+ones; layout of the parameters as mc_ctx_surrogate_params."""
 import numpy as np
 
-NI, NH, NO, NT = 80, 128, 48, 41
-OFF = {"W1": (0, (NH, NI)), "b1": (NH * NI, (NH,))}
-OFF["W2"] = (OFF["b1"][0] + NH, (NH, NH))
-OFF["b2"] = (OFF["W2"][0] + NH * NH, (NH,))
-OFF["W3"] = (OFF["b2"][0] + NH, (NO, NH))
-OFF["b3"] = (OFF["W3"][0] + NO * NH, (NO,))
-NPARAM = OFF["b3"][0] + NO
+NI, NH, NO, NT = 80, 256, 48, 41
+SIZES = (NI, NH, NH, NH, NO)
+OFF = {}
+_o = 0
+for _l in range(4):
+    OFF["W%d" % (_l + 1)] = (_o, (SIZES[_l + 1], SIZES[_l]))
+    _o += SIZES[_l + 1] * SIZES[_l]
+    OFF["b%d" % (_l + 1)] = (_o, (SIZES[_l + 1],))
+    _o += SIZES[_l + 1]
+NPARAM = _o
 
 
 def unpack(p):
@@ -31,27 +35,41 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def _r(rounding):
+    return bf16 if rounding else (lambda a: np.asarray(a, dtype=np.float64))
+
+
 def forward(p, x, rounding=True):
+    """Activations of the three hidden layers and the output."""
     P = unpack(p)
-    r = bf16 if rounding else (lambda a: np.asarray(a, dtype=np.float64))
-    a1 = np.maximum(r(x) @ r(P["W1"]).T + P["b1"], 0.0)
-    a2 = np.maximum(r(a1) @ r(P["W2"]).T + P["b2"], 0.0)
-    y = r(a2) @ r(P["W3"]).T + P["b3"]
-    return a1, a2, y
+    r = _r(rounding)
+    acts = []
+    h = np.asarray(x, dtype=np.float64)
+    for l in range(1, 5):
+        z = r(h) @ r(P["W%d" % l]).T + P["b%d" % l]
+        h = np.maximum(z, 0.0) if l < 4 else z
+        acts.append(h)
+    return acts[:3], acts[3]
 
 
 def loss_and_grads(p, x, t, rounding=True):
+    """Loss over the first NT outputs, gradients of every parameter, output.
+    Rounding as the GPU's kernels: the forward pass rounds both operands;
+    the data gradient rounds the weights, the weight gradient the layer
+    inputs."""
     P = unpack(p)
-    bf16_ = bf16 if rounding else (lambda a: np.asarray(a, dtype=np.float64))
+    r = _r(rounding)
     m = x.shape[0]
-    a1, a2, y = forward(p, x, rounding)
+    hidden, y = forward(p, x, rounding)
+    ins = [np.asarray(x, dtype=np.float64)] + hidden
     d = np.zeros_like(y)
     d[:, :NT] = y[:, :NT] - t[:, :NT]
     loss = float((d ** 2).sum() / (m * NT))
-    dy = 2.0 * d / (m * NT)
-    g = {"W3": dy.T @ bf16_(a2), "b3": dy.sum(0)}
-    dz2 = (dy @ bf16_(P["W3"])) * (a2 > 0)
-    g["W2"], g["b2"] = dz2.T @ bf16_(a1), dz2.sum(0)
-    dz1 = (dz2 @ bf16_(P["W2"])) * (a1 > 0)
-    g["W1"], g["b1"] = dz1.T @ bf16_(x), dz1.sum(0)
+    dz = 2.0 * d / (m * NT)
+    g = {}
+    for l in range(4, 0, -1):
+        g["W%d" % l] = dz.T @ r(ins[l - 1])
+        g["b%d" % l] = dz.sum(0)
+        if l > 1:
+            dz = (dz @ r(P["W%d" % l])) * (ins[l - 1] > 0)
     return loss, g, y
