@@ -247,7 +247,7 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="override the grid size n (odd for full grids)")
     ap.add_argument("--ref-packets", type=int, default=200000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--form", default="graph", choices=["graph", "wave", "plain"],
                     help="graph: the chosen form with its rounds in one CUDA graph; wave: the same with host-driven "
                          "rounds; plain: one thread per history")
