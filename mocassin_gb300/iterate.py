@@ -152,6 +152,7 @@ class LambdaIteration:
         from . import gridio
         te, ne, X, conv, niter, flags = self.ctx.get_cell_state()
         gridio.write_grid(path, self.neb, te, ne, X, conv=conv, black=(flags != 0).astype(np.int32))
+        gridio.write_parameters(path, gridio.model_parameters(self.neb, xhi_limit=self.xhi))
 
     def restart_from(self, path):
         """Sets the cell state from grid files (resetGrid), e.g. for a warm restart."""

@@ -75,3 +75,24 @@ def test_gpu_warm_restart_from_snapshot(gpu_lib, tmp_path):
     np.testing.assert_allclose(sb[0][c], sa[0][c], rtol=1e-7)
     np.testing.assert_allclose(sb[2][c], sa[2][c], rtol=1e-7, atol=1e-30)
     np.testing.assert_allclose(ob, oa, rtol=1e-5, atol=1e-30)
+
+
+def test_model_parameters_round_trip(tmp_path):
+    """grid3.out / photoSource.out in writeGrid's record order, read back as
+    resetGrid reads them; the viewing angles come back shifted by one, as in
+    the reference (written 0..nAngleBins, read into 1..nAngleBins)."""
+    import dataclasses
+    spec = dataclasses.replace(nebula.small_cases()[0], views=((0.5, 1.0), (1.2, -1.0)))
+    neb = nebula.build(spec)
+    p = gridio.model_parameters(neb, xhi_limit=0.02, max_iterate=12, min_convergence=90.0)
+    gridio.write_parameters(str(tmp_path), p)
+    q = gridio.read_parameters(str(tmp_path))
+    for k in ("nGrids", "lgSymmetricXYZ", "nbins", "maxIterateMC", "lgDust", "lgGas", "nAngleBins", "nstages",
+              "lgMultistars", "abundanceFile", "dustSpeciesFile", "nSizes", "lgEcho", "lgNosource"):
+        assert q[k] == p[k], k
+    for k in ("nuMax", "nuMin", "XHIlimit", "minConvergence", "R_in"):
+        assert abs(q[k] - p[k]) <= 1e-7 * max(abs(p[k]), 1.0), k
+    assert q["nbins"] == neb.nbins and q["XHIlimit"] == pytest.approx(0.02)
+    assert q["viewPointTheta"][1:] == pytest.approx(p["viewPointTheta"][:2])
+    src = open(tmp_path / "photoSource.out").read().split("\n")
+    assert int(src[0].split()[0]) == len(spec.stars)
