@@ -6,6 +6,7 @@
 // returned as mc_status with a message for mc_last_error(); nothing here
 // aborts the process (the reference's "print*; stop" sites become codes).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -43,6 +44,14 @@ mc_status set_error(mc_status code, const char *fmt, ...) {
   } while (0)
 
 // Device buffer owned by a context.
+// NVTX range over a C-ABI call, for timeline tools (nsys, ncu's NVTX filter)
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 struct DBuf {
   void *p = nullptr;
   size_t bytes = 0;
@@ -794,6 +803,7 @@ mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S,
 
 mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
                      mc_stats_t *stats) {
+  NvtxRange nvtx_range("mc transport");
   if (!c || !src || !o) return set_error(MC_ERR_ARG, "ctx/src/opts is NULL");
   if (o->precision != MC_PREC_FP32 && o->precision != MC_PREC_FP64)
     return set_error(MC_ERR_ARG, "precision must be MC_PREC_FP32 or MC_PREC_FP64");
@@ -984,6 +994,7 @@ extern "C" mc_status mc_opacity_build(int32_t ncells, int32_t nspecies, int32_t 
 
 extern "C" mc_status mc_ctx_jste_moments(mc_ctx_t *c, int32_t nout, const float *w, double scale, float *out,
                                           double *kernel_ms) {
+  NvtxRange nvtx_range("mc Jste moments");
   if (!c || !w || !out) return set_error(MC_ERR_ARG, "ctx, w and out are required");
   if (nout < 1 || nout > 128) return set_error(MC_ERR_ARG, "nout must be 1..128 (got %d)", nout);
   const int nc1 = c->nc + 1, nb = c->nb;
@@ -1013,6 +1024,7 @@ extern "C" mc_status mc_ctx_jste_moments(mc_ctx_t *c, int32_t nout, const float 
 extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const float *w_abs,
                                               const float *em_table, int32_t ntemps, const float *grain_weight,
                                               double scale, float *tdust, double *kernel_ms) {
+  NvtxRange nvtx_range("mc grain temperatures");
   if (!c || !w_abs || !em_table || !grain_weight || !tdust)
     return set_error(MC_ERR_ARG, "ctx, w_abs, em_table, grain_weight and tdust are required");
   if (nsizes < 1 || nsizes > 127) return set_error(MC_ERR_ARG, "nsizes must be 1..127 (got %d)", nsizes);
@@ -1342,6 +1354,7 @@ static void fill_update_tables(mc_ctx_t *c, mcg::UpdArgs &a) {
 
 static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, double xhi_limit, int32_t precision,
                                    bool warm, mc_update_stats_t *stats) {
+  NvtxRange nvtx_range("mc cell update");
   if (!c || !w) return set_error(MC_ERR_ARG, "ctx and w are required");
   if (warm && !(c->m_ready && c->m_norm)) return set_error(MC_ERR_ARG, "the surrogate is not trained");
   if (precision != MC_PREC_FP32 && precision != MC_PREC_FP64) return set_error(MC_ERR_ARG, "unknown precision");
@@ -1668,6 +1681,7 @@ extern "C" mc_status mc_ctx_surrogate_collect(mc_ctx_t *c, int64_t *rows) {
 
 extern "C" mc_status mc_ctx_surrogate_train(mc_ctx_t *c, int32_t steps, int32_t batch, float lr, uint64_t seed,
                                            double *loss, double *train_ms) {
+  NvtxRange nvtx_range("mc surrogate training");
   if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
   if (steps < 0 || batch < 1) return set_error(MC_ERR_ARG, "steps >= 0 and batch >= 1 required");
   mc_status st;
@@ -1994,6 +2008,7 @@ extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_t
 }
 
 extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
+  NvtxRange nvtx_range("mc emission CDFs");
   if (!c) return set_error(MC_ERR_ARG, "ctx is required");
   if (!c->e_ready) return set_error(MC_ERR_ARG, "mc_ctx_set_emission_tables has not been called");
   const int nc1 = c->nc + 1, nb = c->nb;
@@ -2112,6 +2127,7 @@ extern "C" mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *c, int32_t nrows, const 
 
 extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, const int32_t *species,
                                               const float *xs, int32_t method, double *kernel_ms) {
+  NvtxRange nvtx_range("mc opacity");
   if (!c || !species || !xs) return set_error(MC_ERR_ARG, "ctx, species and xs are required");
   if (!c->u_ready || !c->s_ready) return set_error(MC_ERR_ARG, "cell state or tables missing");
   if (nspecies < 1 || nspecies + c->o_nfix > 64)
@@ -2182,6 +2198,7 @@ __global__ void narrow_kernel(const double *__restrict__ in, float *__restrict__
 // the drop-in call with FP64 (f32 = false) or FP32 host estimators
 mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
                              void *jste, void *jdif, void *escaped, bool f32, mc_stats_t *stats) {
+  NvtxRange nvtx_range("mc drop-in transport");
   if (!jste) return set_error(MC_ERR_ARG, "jste is NULL");
   if (!o) return set_error(MC_ERR_ARG, "opts is NULL");
   if (g && (g->flags & MC_FLAG_DEBUG) && !jdif) return set_error(MC_ERR_ARG, "debug grid needs jdif");

@@ -154,6 +154,30 @@ class LambdaIteration:
         gridio.write_grid(path, self.neb, te, ne, X, conv=conv, black=(flags != 0).astype(np.int32))
         gridio.write_parameters(path, gridio.model_parameters(self.neb, xhi_limit=self.xhi))
 
+    def write_summary(self, path):
+        """output/summary.out of the iterations so far, with the reference's
+        per-iteration lines (iterateMC, iteration_mod.f90:1003-1065): converged,
+        no-hit, no-ion-balance and no-Te-balance percentages of the grid, the
+        total converged percentage and the packets used."""
+        import os
+        os.makedirs(path, exist_ok=True)
+        nc = max(self.neb.ncells, 1)
+        npk = int(sum(self.neb.n_packets))
+        with open(os.path.join(path, "summary.out"), "w") as fh:
+            for h in self.history:
+                it = h["iteration"]
+                pre = " ! iterateMC: [Summary] Iteration %12d ; " % it
+                hit = max(h["hit"], 1)
+                fh.write(pre + "%12d%% converged cells in grid %12d\n" % (int(h["converged_pct"]), 1))
+                fh.write(pre + "%12d%% no hit cells in grid %12d\n" % (int(100.0 * (nc - h["hit"]) / nc), 1))
+                fh.write(pre + "%12d%% Ion balance not reached in grid %12d\n"
+                         % (int(100.0 * h["no_ion_balance"] / hit), 1))
+                fh.write(pre + "%12d%% Te balance not reached in grid %12d\n"
+                         % (int(100.0 * h["no_te_balance"] / hit), 1))
+                fh.write(pre + "Total:  %16.8E%% converged cells over all grids\n" % h["converged_pct"])
+                fh.write(pre + "%12d  energy packets used\n" % npk)
+                fh.write("\n")
+
     def restart_from(self, path):
         """Sets the cell state from grid files (resetGrid), e.g. for a warm restart."""
         from . import gridio

@@ -96,3 +96,21 @@ def test_model_parameters_round_trip(tmp_path):
     assert q["viewPointTheta"][1:] == pytest.approx(p["viewPointTheta"][:2])
     src = open(tmp_path / "photoSource.out").read().split("\n")
     assert int(src[0].split()[0]) == len(spec.stars)
+
+
+def test_summary_lines_follow_the_reference(tmp_path):
+    """summary.out carries iterateMC's per-iteration lines (converged, no
+    hit, no ion balance, no Te balance, total, packets)."""
+    from mocassin_gb300 import iterate
+    li = iterate.LambdaIteration.__new__(iterate.LambdaIteration)  # the history alone, no GPU context
+    li.neb = nebula.build(nebula.small_cases()[0])
+    li.history = [{"iteration": 1, "converged_pct": 12.5, "hit": li.neb.ncells // 2, "no_ion_balance": 3,
+                   "no_te_balance": li.neb.ncells // 4}]
+    li.write_summary(str(tmp_path))
+    lines = [l for l in open(tmp_path / "summary.out").read().split("\n") if l]
+    assert len(lines) == 6 and all("[Summary] Iteration" in l for l in lines)
+    words = [" ".join(l.split()) for l in lines]
+    assert "; 12% converged cells in grid 1" in words[0]
+    assert "; 50% no hit cells in grid 1" in words[1]
+    assert "; 50% Te balance not reached in grid 1" in words[3]
+    assert "energy packets used" in words[5]
