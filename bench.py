@@ -195,12 +195,14 @@ def converged_model(neb, args):
         x, t, info = iterate.training_rows(nebula.batch64(), max_rows=args.surrogate_rows)
         rows = (x, t)
         out["surrogate_dataset"] = info
+    states = {}
     for name, (form, upd, sur) in LAMBDA_FORMS.items():
         if sur is not None and rows is not None:
             sur = {"rows": rows, "train_after": None, "steps": 2000, "batch": 4096, "lr": 2e-3}
         li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
         pre = li.pretrain
         wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
+        states[name] = li.ctx.get_cell_state()
         li.close()
         last = hist[-1]
         out[name] = {"transport": form, "update": upd, "surrogate": sur is not None, "wall_s": wall,
@@ -213,6 +215,21 @@ def converged_model(neb, args):
                      "warm_fallback_pct": float(np.mean([h["warm_fallback_pct"] for h in hist]))}
         if pre is not None:
             out[name]["pretrain"] = pre
+    # the converged states against the plain FP64 form's (same draws, same initial state): Te and
+    # the ionic fractions above 1e-3 of every cell the last update reached and balanced in Te in
+    # both forms (where the update gives up on Te balance, noTeBal, its Te means nothing)
+    te_p, _, x_p = states["plain"][:3]
+    for name in ("chosen", "chosen_surrogate"):
+        te, _, x = states[name][:3]
+        reached = (states["plain"][4] > 0) & ((states["plain"][5] & 1) == 0) & ((states[name][5] & 1) == 0)
+        dte = np.abs(te[reached] / te_p[reached] - 1)
+        big = (x_p[reached] > 1e-3)
+        dx = np.abs(x[reached][big] / x_p[reached][big] - 1)
+        out[name]["vs_plain"] = {"te_rel_median": float(np.median(dte)), "te_rel_p95": float(np.quantile(dte, 0.95)),
+                                 "ion_frac_rel_median": float(np.median(dx)),
+                                 "ion_frac_rel_p95": float(np.quantile(dx, 0.95)),
+                                 "ion_frac_within_2pct": float(np.mean(dx <= 0.02)),
+                                 "cells": int(reached.sum())}
     out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
     out["speedup_chosen_surrogate_vs_plain"] = out["plain"]["wall_s"] / out["chosen_surrogate"]["wall_s"]
     return out
