@@ -201,11 +201,14 @@ __device__ Real cel_cooling(const UpdArgs &a, int k, Real Te, Real Ne, Real up) 
 // top_levels = 10 gives thermBalance's cooling (transitions among levels
 // 1..10).  With fscale > 0 each line is scaled by fscale and only lines above
 // 1e-35 count: setDiffusePDF's normFor over forbiddenLines (all levels,
-// emission_mod.f90:1151-1172).
+// emission_mod.f90:1151-1172).  With emis non-null the same populations also
+// give that emission sum (over all levels, scaled by escale) in *emis.
 template <typename Real>
 __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real up, Real *M, int L,
-                                 int top_levels = 10, Real fscale = (Real)0.) {
+                                 int top_levels = 10, Real fscale = (Real)0., Real *emis = nullptr,
+                                 Real escale = (Real)0.) {
   const UpdTabs<Real> &T = tabs<Real>(a);
+  if (emis) *emis = (Real)0.;
   if (up != up) return (Real)0.;
   const UpdCelT<Real> &c = T.cel[k];
   const int n = c.nlev, nt = c.nt;
@@ -295,6 +298,16 @@ __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real
         if (!(fscale > (Real)0.)) cool += line;
         else if (line * fscale > (Real)1e-35) cool += line * fscale;
       }
+  if (emis) {
+    Real em = (Real)0.;
+    for (int i = 1; i <= n - 1; ++i)
+      for (int j = i + 1; j <= n; ++j)
+        if (A[j * kNL + i] != (Real)0.) {
+          const Real line = (Real)A[j * kNL + i] * ((Real)e[j] - (Real)e[i]) * (y[j] * inv) * escale;
+          if (line > (Real)1e-35) em += line;
+        }
+    *emis = em;
+  }
   return cool;
 }
 
@@ -518,6 +531,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
     if (lane == 0) {
       a.te[c] = (double)Te;
       a.ne[c] = (double)Ne;
+      if (a.forb_ok) a.forb_ok[c] = 0;  // this form keeps no line totals
       a.conv[c] = fabs((sX[w][0][1] - XOldHI) / XOldHI) <= (Real)a.xhi ? 1 : 0;
       a.niter[c] = nIterT;
       a.flags[c] = (noTe ? 1 : 0) | (ionConv ? 0 : 2) | (cold ? 4 : 0);

@@ -154,8 +154,11 @@ __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ W
     const float xi = XS(w, C.e * kNX + C.ion, c);
     const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
     float x[kNL * kNL];
-    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows);
+    float emis = 0.f;
+    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f, a.forb_out ? &emis : nullptr,
+                                               T.ab[C.e] * xi * 1.9865e9f);
     w.cool[(size_t)k * (a.nc + 1) + c] = cool * T.ab[C.e] * xi * 1.9865e-16f;
+    if (a.forb_out) a.forb_out[(size_t)k * (a.nc + 1) + c] = emis;
   }
 }
 
@@ -262,6 +265,9 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
       for (int s = 1; s < kNX; ++s) Xc[e * kNX + s] = (double)XS(w, e * kNX + s, c);
     a.te[c] = (double)Te;
     a.ne[c] = (double)Ne;
+    // the last T step's line totals belong to this state unless Te was moved
+    // after them (no balance) or the emission would clamp Ne
+    if (a.forb_ok) a.forb_ok[c] = (!noTe && Ne >= 1e-5f) ? 1 : 0;
     const double xh = (double)xH1;
     a.conv[c] = fabs((xh - x0) / x0) <= a.xhi ? 1 : 0;
     a.niter[c] = nIterT;

@@ -30,13 +30,24 @@ constexpr float kHcRydK = 157893.94f;
 constexpr float kFourPi = 4.f * 3.141592654f;
 constexpr int kEmiThreads = 128;
 
-__global__ void __launch_bounds__(128) emission_forb_kernel(const __grid_constant__ UpdArgs a, float *forb) {
+// the cells whose line totals do not belong to their state (ok[c] == 0)
+__global__ void emission_stale_kernel(int nc, const int *ok, int *list, int *count) {
+  for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x)
+    if (!ok[c]) list[atomicAdd(count, 1)] = c;
+}
+__global__ void emission_fresh_kernel(const int *list, const int *count, int *ok) {
+  const int n = *count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) ok[list[i]] = 1;
+}
+
+__global__ void __launch_bounds__(128) emission_forb_kernel(const __grid_constant__ UpdArgs a, float *forb,
+                                                            const int *list, const int *count) {
   const UpdTabs<float> &T = a.f;
-  const int nc = a.nc;
-  const long long total = (long long)nc * a.ncel;
+  const int nc = a.nc, n = *count;
+  const long long total = (long long)n * a.ncel;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(q / nc), c = 1 + (int)(q % nc);
+    const int k = (int)(q / n), c = list[q % n];
     const UpdCelT<float> &C = T.cel[k];
     const float Te = (float)a.te[c];
     const float Ne = fmaxf((float)a.ne[c], 1e-5f);
@@ -316,14 +327,19 @@ __global__ void __launch_bounds__(kEmiThreads) emission_cdf_kernel(const __grid_
 
 }  // namespace
 
-cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int num_sms, cudaStream_t s) {
+cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int *ok, int *list, int *count,
+                            int num_sms, cudaStream_t s) {
   if (E.nb > kEmiMaxBins || E.nheavy > kEmiMaxHeavy || E.nsizes > kEmiMaxSizes || E.nlim[0] > kEmiMaxLim || E.nlim[1] > kEmiMaxLim ||
       E.nlim[2] > kEmiMaxLim || E.nlim[0] + E.nlim[1] + E.nlim[2] > 64)
     return cudaErrorInvalidValue;
   if (a.ncel > 0) {
+    // only the cells whose totals the update did not leave
     cudaError_t e = cudaFuncSetAttribute(emission_forb_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
-    emission_forb_kernel<<<num_sms * cel_blocks_per_sm(), 128, 0, s>>>(a, forb);
+    emission_stale_kernel<<<num_sms * 4, 256, 0, s>>>(a.nc, ok, list, count);
+    emission_forb_kernel<<<num_sms * 32, 128, 0, s>>>(a, forb, list, count);
+    emission_fresh_kernel<<<num_sms * 4, 256, 0, s>>>(list, count, ok);
   }
   emission_cdf_kernel<<<num_sms * 12, kEmiThreads, (size_t)E.nb * sizeof(float), s>>>(E);
   return cudaGetLastError();

@@ -91,6 +91,11 @@ struct UpdArgs {
   // from this state (the plain solve as fallback).
   const double *te_prev, *ne_prev, *x_prev;  // x_prev [nc+1][7][8]
   double accept_res, near_res;
+  // the emission's forbidden-line totals, from the populations of each
+  // cell's last T step (null: not kept): forb_out [ncel][nc+1], and per cell
+  // forb_ok = 1 when they belong to the state the update left
+  float *forb_out;
+  int *forb_ok;
   double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
   int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
 };
@@ -176,7 +181,10 @@ struct EmiArgs {
   float *dust_cdf;                // out on a dust-only grid: [nc+1][nb]
 };
 constexpr int kEmiMaxSizes = 16;
-cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int num_sms, cudaStream_t s);
+// forb / ok: the line totals and their per-cell validity (the cells with ok 0
+// are recomputed, through list [nc+1] and count, then marked valid)
+cudaError_t launch_emission(const UpdArgs &a, const EmiArgs &E, float *forb, int *ok, int *list, int *count,
+                            int num_sms, cudaStream_t s);
 
 // Sets the text returned by mc_last_error() on the calling thread.
 void set_last_error_text(const char *msg);

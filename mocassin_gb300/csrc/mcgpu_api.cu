@@ -146,6 +146,7 @@ struct mc_ctx {
   double m_accept_res = 0.01;  // ... and below which it is accepted
   // diffuse-emission CDF: derived tables (one buffer) and forbidden-line totals
   DBuf e_tab, e_forb;
+  DBuf e_ok, e_list, e_cnt;  // per cell: the line totals in e_forb belong to the state (1); stale-cell list
   DBuf d_tdust;      // grain temperatures of the last mc_ctx_dust_temperatures [nsizes+1][nc+1]
   DBuf o_fix_den, o_fix_xs;  // opacity rows that do not follow the cell state (grains)
   int o_nfix = 0;
@@ -1283,6 +1284,7 @@ extern "C" mc_status mc_ctx_set_update_tables(mc_ctx_t *c, const mc_update_table
     return st;
   MC_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
   c->u_ncel = ncel;
+  if (c->e_ok.p) MC_CUDA(cudaMemsetAsync(c->e_ok.p, 0, c->e_ok.bytes, s));  // other line ions
   c->u_maxlev = 1;
   for (int k = 0; k < ncel; ++k) c->u_maxlev = std::max(c->u_maxlev, (int)t->cel_nlev[k]);
   c->u_ndirec = t->ndirec;
@@ -1304,6 +1306,7 @@ extern "C" mc_status mc_ctx_set_cell_state(mc_ctx_t *c, const double *te, const 
   MC_CUDA(cudaMemsetAsync(c->s_conv.p, 0, c->s_conv.bytes, s));
   MC_CUDA(cudaMemsetAsync(c->s_niter.p, 0, c->s_niter.bytes, s));
   MC_CUDA(cudaMemsetAsync(c->s_flags.p, 0, c->s_flags.bytes, s));
+  if (c->e_ok.p) MC_CUDA(cudaMemsetAsync(c->e_ok.p, 0, c->e_ok.bytes, s));  // line totals of another state
   MC_CUDA(cudaStreamSynchronize(s));
   c->s_ready = true;
   return MC_OK;
@@ -1351,6 +1354,8 @@ static void fill_update_tables(mc_ctx_t *c, mcg::UpdArgs &a) {
   a.mat_rows = c->u_maxlev;
   a.mat_stride = (c->u_maxlev * c->u_maxlev) | 1;
 }
+
+static mc_status ensure_line_totals(mc_ctx_t *c);
 
 static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, double xhi_limit, int32_t precision,
                                    bool warm, mc_update_stats_t *stats) {
@@ -1402,6 +1407,14 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   a.xhi = xhi_limit;
   a.mat_rows = c->u_maxlev;
   a.mat_stride = (c->u_maxlev * c->u_maxlev) | 1;
+  // with emission tables the FP32 form keeps each cell's last line totals for
+  // the next emission build; the FP64 form marks the cells it updated stale
+  if (c->e_ready && c->u_ncel > 0) {
+    mc_status es = ensure_line_totals(c);
+    if (es) return es;
+    a.forb_out = precision == MC_PREC_FP32 ? c->e_forb.as<float>() : nullptr;
+    a.forb_ok = c->e_ok.as<int>();
+  }
   if (precision == MC_PREC_FP32) {
     const size_t need = mcg::cell_update_fp32_scratch(c->nc, c->u_ncel);
     mc_status ss = c->s_wave.bytes == need ? MC_OK : put_buf(c->s_wave, nullptr, need, s);
@@ -1838,6 +1851,21 @@ float hydro2phot_shape(float nu, int z) {
 
 }  // namespace
 
+// the line-total buffers of the emission build; e_ok starts at 0 (stale)
+static mc_status ensure_line_totals(mc_ctx_t *c) {
+  const size_t nc1 = (size_t)c->nc + 1;
+  mc_status st;
+  if ((st = put_buf(c->e_forb, nullptr, (size_t)std::max(c->u_ncel, 1) * nc1 * sizeof(float), c->stream)))
+    return st;
+  if (!c->e_ok.p) {
+    MC_CUDA(c->e_ok.alloc(nc1 * sizeof(int)));
+    MC_CUDA(cudaMemsetAsync(c->e_ok.p, 0, nc1 * sizeof(int), c->stream));
+  }
+  if (!c->e_list.p) MC_CUDA(c->e_list.alloc(nc1 * sizeof(int)));
+  if (!c->e_cnt.p) MC_CUDA(c->e_cnt.alloc(sizeof(int)));
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_set_emission_tables(mc_ctx_t *c, const mc_emission_tables_t *t) {
   if (!c || !t) return set_error(MC_ERR_ARG, "ctx and tables are required");
   const int nb = c->nb;
@@ -2020,7 +2048,7 @@ extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
     return set_error(MC_ERR_ARG, "grain temperatures of %d sizes, emission tables of %d", c->d_nsizes, c->emi.nsizes);
   cudaStream_t s = c->stream;
   mc_status st;
-  if ((st = put_buf(c->e_forb, nullptr, (size_t)std::max(c->u_ncel, 1) * nc1 * sizeof(float), s))) return st;
+  if ((st = ensure_line_totals(c))) return st;
   if (!gas && !c->dust_cdf.p) {
     MC_CUDA(c->dust_cdf.alloc((size_t)nc1 * nb * sizeof(float)));
     std::vector<float> one(nb, 1.f);
@@ -2056,7 +2084,8 @@ extern "C" mc_status mc_ctx_build_emission(mc_ctx_t *c, float *ms) {
   E.dust_cdf = c->dust_cdf.as<float>();
   if (!gas) a.ncel = 0;  // no forbidden lines without gas
   MC_CUDA(cudaEventRecord(c->ev0, s));
-  cudaError_t e = mcg::launch_emission(a, E, c->e_forb.as<float>(), c->num_sms, s);
+  cudaError_t e = mcg::launch_emission(a, E, c->e_forb.as<float>(), c->e_ok.as<int>(), c->e_list.as<int>(),
+                                       c->e_cnt.as<int>(), c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "emission launch failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(c->ev1, s));
   MC_CUDA(cudaEventSynchronize(c->ev1));

@@ -251,3 +251,33 @@ def test_lambda_iteration_on_a_dusty_grid(gpu_lib):
     np.testing.assert_allclose(op[0, 1:], kd, rtol=2e-3)
     assert np.all(np.diff(rows[1:], axis=1) >= 0) and np.all(rows[1:, -1] == 1.0)
     assert len(hist) == 2 and all(h["emission_ms"] > 0 for h in hist)
+
+
+@pytest.mark.gpu
+def test_line_totals_kept_by_the_update_are_the_recomputed_ones(gpu_lib):
+    """After an FP32 update the emission build takes the forbidden-line totals
+    of each cell's last T step instead of solving the level populations again;
+    the rows and line fractions are bit-identical to a build that recomputes
+    every cell (after the same state is set again)."""
+    import dataclasses
+    from mocassin_gb300 import transport
+    neb = nebula.build(dataclasses.replace(nebula.clumpy61(400_000), name="clumpy21", n=21))
+    ctx = transport.TransportContext(neb)
+    ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+    te, ne, X = balance.initial_state(neb)
+    ctx.set_cell_state(te, ne, X)
+    ctx.set_emission_tables()
+    ions = [tuple(int(v) for v in r) for r in nebula.atomic_table()["ions"]]
+    w = balance.moment_weights(neb.xs, neb.nu, ions)
+    ctx.build_emission()
+    ctx.run(seed=8, precision="fp32", zero_first=True)
+    ctx.update_cells(w, 1e-9, precision="fp32")
+    ctx.build_emission()
+    rows1, tl1 = ctx.get_emission()
+    s = ctx.get_cell_state()
+    ctx.set_cell_state(s[0], s[1], s[2])
+    ctx.build_emission()
+    rows2, tl2 = ctx.get_emission()
+    ctx.close()
+    np.testing.assert_array_equal(tl1, tl2)
+    np.testing.assert_array_equal(rows1, rows2)
