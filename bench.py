@@ -9,14 +9,22 @@ ending in a full crossing or an interaction (source/photon_mod.f90:1517,
 
   value   crossings / device time of the step, grid resident in HBM (the
           estimators are zeroed inside the step, as iterateMC does)
-  e2e     the same metric through the drop-in call mc_transport_run with HOST
-          (pinned) buffers: grid upload, transport, estimator download
+  e2e     the same metric through the drop-in call mc_transport_run_f32 with
+          HOST (pinned) buffers: grid upload, transport, download of the
+          estimators into the grid's own FP32 arrays
   roofline  16 algorithmic bytes per crossing (4 B opacity + 4 B active +
           8 B FP64 Jste) over the transport kernel's CUDA-event time, against
           the measured HBM copy bandwidth
   cpu_baseline  the FP32 oracle (a C++ restatement of the reference's Fortran
           path, FP32 sums like the reference's `real` Jste) on the host cores,
           on a bounded sample of the same workload
+  converged_model  wall time to a converged model (Lambda iterations of
+          transport, cell update, opacity and emission CDFs) of the chosen
+          form, of the chosen form with the learned warm start (trained on the
+          batch's FP64 cell states), and of the plain form (FP64 update), with
+          the converged states compared against the plain form's
+  batched_models  the request loop over the first --batch-models of the
+          64-model batch: wall, p50 / p99 latency per Lambda iteration
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
