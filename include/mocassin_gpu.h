@@ -363,7 +363,7 @@ mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32
  * update: mc_ctx_update_cells_warm writes the prediction into the state and
  * runs the same solve from there.  At the first T step the solve accepts
  * the prediction when the thermal residual is below 1 % of the heating (or
- * the stricter accept_res of mc_ctx_surrogate_rule); below 100 % (near_res)
+ * the stricter accept_res of mc_ctx_surrogate_rule); below 30 % (near_res)
  * it brackets the balance from the prediction with steps of 3 %, 6 %, 12 %,
  * then the reference's 20 %, before its secant; otherwise the cell falls
  * back to the plain solve from the state before the prediction (20 % steps,
@@ -379,7 +379,7 @@ mc_status mc_ctx_update_cells_warm(mc_ctx_t *ctx, const float *w, double scale, 
 /* The warm start's rule at the first T step, in units of the heating: a
  * prediction whose thermal residual is below accept_res (0 < accept_res <=
  * 0.01, the reference's own test; default 0.01) is accepted; below near_res
- * (>= accept_res; default 1.0) it is bracketed from the prediction; from
+ * (>= accept_res; default 0.3) it is bracketed from the prediction; from
  * near_res up the cell goes back to the plain solve.  accept_res = near_res
  * = 1e-3 is "accept below 1e-3, otherwise the plain solve". */
 mc_status mc_ctx_surrogate_rule(mc_ctx_t *ctx, double accept_res, double near_res);

@@ -142,7 +142,7 @@ struct mc_ctx {
   long long m_cap = 0, m_n = 0;
   int m_step = 0, m_B = 0;
   bool m_ready = false, m_norm = false;
-  double m_near_res = 1.0;  // warm start: residual / heating below which a prediction is bracketed
+  double m_near_res = 0.3;  // warm start: residual / heating below which a prediction is bracketed
   double m_accept_res = 0.01;  // ... and below which it is accepted
   // diffuse-emission CDF: derived tables (one buffer) and forbidden-line totals
   DBuf e_tab, e_forb;

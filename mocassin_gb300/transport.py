@@ -369,7 +369,7 @@ class TransportContext:
             raise ValueError("x (n, 80) and t (n, 48)")
         _check(self.lib.mc_ctx_surrogate_load(self.handle, len(x), _fptr(x), _fptr(t)))
 
-    def surrogate_rule(self, accept_res=0.01, near_res=1.0):
+    def surrogate_rule(self, accept_res=0.01, near_res=0.3):
         """The warm start's rule (mc_ctx_surrogate_rule): accept a prediction
         whose residual / heating is below accept_res, bracket it below
         near_res, else fall back to the plain solve."""
