@@ -389,6 +389,11 @@ constexpr int kHot = 2 * kHotHalf + 1;         // cube edge
 constexpr int kHot3 = kHot * kHot * kHot;      // cells per cube
 constexpr int kHotSrc = 2;                     // stars with a cube
 
+// event counts of the fast march: warp-private slots in shared memory (the
+// nine 64-bit per-lane counters of LocalCounts would take 18 registers of the
+// 64 the fast march runs with)
+enum { kCntAbs = 0, kCntSca, kCntEsc, kCntTrap, kCntSilent, kCntSafe, kCntSlots };
+
 template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   const DevGrid &g;
   const DevSources &S;
@@ -397,6 +402,8 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   const Tables<Real> &T;
   DevCounters *cnt;
   LocalCounts &lc;
+  unsigned int *wc;         // Fast: this warp's kCntSlots event counters in shared memory
+  unsigned long long *wcx;  // Fast: this warp's crossing counter in shared memory
 
   // lane state
   R3<Real> r, v, iv;  // position, direction, 1/direction (fast path)
@@ -406,11 +413,31 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   Real absTau, passProb;
   bool stellar, valid;
   bool pend;  // absorbed: the entry for the next round is written after the step
+  int pev;    // Fast: the parked event (EV_* | axis << 2) that stopped the lane's crossings, 0 = none
   RStream<Replay> st;
 
   __device__ Marcher(const DevGrid &g_, const DevSources &S_, const DevReplay &rp_, const WaveGrid &w_,
                      const Tables<Real> &T_, DevCounters *c_, LocalCounts &lc_)
-      : g(g_), S(S_), rp(rp_), w(w_), T(T_), cnt(c_), lc(lc_), valid(false), pend(false) {}
+      : g(g_), S(S_), rp(rp_), w(w_), T(T_), cnt(c_), lc(lc_), wc(nullptr), wcx(nullptr), valid(false), pend(false),
+        pev(0), segI(0) {}
+
+  // one event of kind K (the fast march counts crossings per packet, from segI)
+  template <int K> __device__ __forceinline__ void bump() {
+    if (Fast) {
+      atomicAdd(wc + K, 1u);
+    } else {
+      if (K == kCntAbs) ++lc.absorptions;
+      else if (K == kCntSca) ++lc.scatterings;
+      else if (K == kCntEsc) ++lc.escaped;
+      else if (K == kCntTrap) ++lc.trapped;
+      else if (K == kCntSilent) ++lc.silent;
+      else if (K == kCntSafe) ++lc.safe_hits;
+    }
+  }
+  // the crossings of the lane's last packet (Fast: every crossing is one segI)
+  __device__ __forceinline__ void count_crossings() {
+    if (Fast && segI > 0) { atomicAdd(wcx, (unsigned long long)segI); segI = 0; }
+  }
 
   __device__ __forceinline__ const DevSource &source() const { return S.s[source_of(S, id)]; }
   __device__ __forceinline__ Real rnd() {
@@ -422,7 +449,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     valid = false;
   }
   __device__ __forceinline__ void end_history() {
-    if (runI >= g.recursion_limit) ++lc.trapped;
+    if (runI >= g.recursion_limit) bump<kCntTrap>();
     valid = false;
   }
   __device__ __forceinline__ void escape() {
@@ -432,8 +459,19 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
       view = escape_view<Real>(g, v.x, v.y, v.z, ok);
       if (!ok) { fail(MC_ERR_NAN); return; }
     }
-    add_escape(g, origin, nuP, view, (double)(Real)source().delta_e);
-    ++lc.escaped;
+    const int s0 = source_of(S, id);
+    if (Fast && stellar && nuP == hot_nu && s0 < kHotSrc && origin == esc_org[s0]) {
+      // escapedPackets(star cell, hot_nu, 0): counted in the warp, added as
+      // count x deltaE when the warp's bin changes (every stellar packet of a
+      // bin escapes into the same entry, so the atomics would serialise)
+      atomicAdd(esc_n + s0, 1u);
+      if (view > 0 && g.esc)
+        atomicAdd(g.esc + origin + (long long)(g.nc + 1) * nuP + (long long)(g.nc + 1) * (g.nb + 1) * view,
+                  (double)(Real)S.s[s0].delta_e);
+    } else {
+      add_escape(g, origin, nuP, view, (double)(Real)source().delta_e);
+    }
+    bump<kCntEsc>();
     end_history();
   }
   __device__ __forceinline__ void set_v(R3<Real> d) {
@@ -474,6 +512,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
 
   // a queue entry written by the emission pass
   __device__ __forceinline__ void start(unsigned int q) {
+    count_crossings();
     const uint32_t meta = __ldg(w.q_meta + q);
     nuP = (int)(meta & 0xFFFFu);
     if (nuP == 0) return;  // emission failed (error already raised)
@@ -500,9 +539,9 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
 
   // absorbed: hand the packet to the next round (rerun = 1, :2861-2870)
   __device__ __forceinline__ void absorbed() {
-    ++lc.absorptions;
-    if (segI >= g.safe_limit) { ++lc.safe_hits; end_history(); return; }
-    if (runI >= g.recursion_limit) { ++lc.trapped; valid = false; return; }
+    bump<kCntAbs>();
+    if (segI >= g.safe_limit) { bump<kCntSafe>(); end_history(); return; }
+    if (runI >= g.recursion_limit) { bump<kCntTrap>(); valid = false; return; }
     pend = true;
     valid = false;
   }
@@ -563,7 +602,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   // dust scattering (photon_mod.f90:1718-1798): the packet turns and keeps
   // marching with a fresh passProb
   __device__ void scatter() {
-    ++lc.scatterings;
+    bump<kCntSca>();
     origin = w.identity ? lin_of(g, xP, yP, zP) + 1 : __ldg(w.lin2cell + lin_of(g, xP, yP, zP));
     stellar = false;
     if (g.flags & MC_FLAG_ISOTROPIC) {
@@ -579,7 +618,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     if (isnan(v.x)) { fail(MC_ERR_NAN); return; }
     absTau = (Real)0;
     passProb = -log((Real)1 - rnd());
-    if (segI >= g.safe_limit) { ++lc.safe_hits; end_history(); }
+    if (segI >= g.safe_limit) { bump<kCntSafe>(); end_history(); }
   }
 
   // ---- fast path: 3D-DDA march (Amanatides & Woo 1987) ---------------
@@ -603,6 +642,8 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   // sums (every packet of a frequency bin crosses the cells next to its star,
   // so their atomics would serialise in L2)
   float *hot;          // this warp's slice of shared memory
+  unsigned int *esc_n; // this warp's escape counts of (star kHotSrc, hot_nu)
+  const int *esc_org;  // origin of each of the first kHotSrc stars
   int hot_nu;          // bin held by the accumulator (warp-uniform), 0 = none
   bool hot_ok;         // this packet's deposits may go to the accumulator
 
@@ -640,9 +681,9 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     // a packet sitting on the wall it heads for steps through it first
     // (photon_mod.f90:1268-1290); on the outer wall it leaves silently
     if (fabs(tN0) < tiny || fabs(tN1) < tiny || fabs(tN2) < tiny) {
-      if (fabs(tN0) < tiny) { if (v.x > (Real)0) { if (xP < g.nx) ++xP; else { ++lc.silent; end_history(); return; } } else if (xP > 1) --xP; tN0 = wall_param(0, xP, r0.x, v.x, iv.x); }
-      if (fabs(tN1) < tiny) { if (v.y > (Real)0) { if (yP < g.ny) ++yP; else { ++lc.silent; end_history(); return; } } else if (yP > 1) --yP; tN1 = wall_param(1, yP, r0.y, v.y, iv.y); }
-      if (fabs(tN2) < tiny) { if (v.z > (Real)0) { if (zP < g.nz) ++zP; else { ++lc.silent; end_history(); return; } } else if (zP > 1) --zP; tN2 = wall_param(2, zP, r0.z, v.z, iv.z); }
+      if (fabs(tN0) < tiny) { if (v.x > (Real)0) { if (xP < g.nx) ++xP; else { bump<kCntSilent>(); end_history(); return; } } else if (xP > 1) --xP; tN0 = wall_param(0, xP, r0.x, v.x, iv.x); }
+      if (fabs(tN1) < tiny) { if (v.y > (Real)0) { if (yP < g.ny) ++yP; else { bump<kCntSilent>(); end_history(); return; } } else if (yP > 1) --yP; tN1 = wall_param(1, yP, r0.y, v.y, iv.y); }
+      if (fabs(tN2) < tiny) { if (v.z > (Real)0) { if (zP < g.nz) ++zP; else { bump<kCntSilent>(); end_history(); return; } } else if (zP > 1) --zP; tN2 = wall_param(2, zP, r0.z, v.z, iv.z); }
     }
     load_cell();
   }
@@ -686,7 +727,6 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     const Real dS = tE - tc;
     const Real tau = dS * kap;
     ++segI;
-    ++lc.crossings;
     const bool active = w.identity ? true : (__ldg(w.lin2cell + lin) > 0);
     if ((absTau + tau > passProb) && active) { ea = a; return EV_INTERACT; }
     add_j(dS * de * (idv0 * idv1 * idv2));
@@ -724,10 +764,12 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     const Real ti = tc + dl;
     r = R3<Real>{r0.x + ti * v.x, r0.y + ti * v.y, r0.z + ti * v.z};
     add_j(dl * de * (idv0 * idv1 * idv2));
-    const Real e10 = (Real)1.e10f;
-    const Real rx = r.x / e10, ry = r.y / e10, rz = r.z / e10;
     const Real rout = (Real)g.rout;
-    if (rout > (Real)0 && sqrt(rx * rx + ry * ry + rz * rz) * e10 >= rout) { escape(); return; }
+    if (rout > (Real)0) {
+      const Real e10 = (Real)1.e10f;
+      const Real rx = r.x / e10, ry = r.y / e10, rz = r.z / e10;
+      if (sqrt(rx * rx + ry * ry + rz * rz) * e10 >= rout) { escape(); return; }
+    }
     if (Dust) {
       const Real probSca = (Real)__ldg(w.sca + (long long)(nuP - 1) * w.S + w.off + lin) / kap;
       const Real rr = (Real)1 - rnd();
@@ -745,7 +787,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     const Real va = a == 0 ? v.x : (a == 1 ? v.y : v.z);
     if (va > (Real)0 || !(g.flags & MC_FLAG_SYMMETRIC_XYZ)) { escape(); return; }
     dda_reflect(a);
-    if (valid && segI >= g.safe_limit) { ++lc.safe_hits; end_history(); }
+    if (valid && segI >= g.safe_limit) { bump<kCntSafe>(); end_history(); }
   }
 
   // adds the accumulator into Jste(:, hot_nu) and clears it (whole warp)
@@ -753,6 +795,14 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     __syncwarp();
     if (hot_nu > 0) {
       const int ncube = S.nsrc < kHotSrc ? S.nsrc : kHotSrc;
+      if ((int)lane < ncube) {
+        const unsigned int c = esc_n[lane];
+        if (c) {
+          esc_n[lane] = 0u;
+          if (g.esc)
+            atomicAdd(g.esc + esc_org[lane] + (long long)(g.nc + 1) * hot_nu, (double)c * (double)(Real)S.s[lane].delta_e);
+        }
+      }
       double *row = w.jste + (long long)(hot_nu - 1) * w.S + w.off;
       for (int i = (int)lane; i < ncube * kHot3; i += 32) {
         const float val = hot[i];
@@ -768,16 +818,23 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     __syncwarp();
   }
 
-  // up to k crossings, then the event that stopped them
+  // up to k crossings; the event that stopped them is parked and handled
+  // together with the warp's other parked events (the event code then runs
+  // with many lanes instead of one or two)
   __device__ void advance(int k) {
     int ev = EV_NONE, ea = 0;
     for (int i = 0; i < k; ++i) {
       ev = cross(ea);
       if (ev != EV_NONE) break;
     }
+    pev = ev | (ea << 2);
+  }
+  __device__ void handle_parked() {
+    const int ev = pev & 3, ea = pev >> 2;
+    pev = 0;
     if (ev == EV_INTERACT) interact();
     else if (ev == EV_EDGE) edge(ea);
-    else if (ev == EV_SAFE) { ++lc.safe_hits; end_history(); }
+    else if (ev == EV_SAFE) { bump<kCntSafe>(); end_history(); }
   }
 
   // One pathSegment loop body.  Leaves `valid` false when the packet ended
@@ -794,7 +851,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     Real dSx, dSy, dSz;
     if (!axis_dist(0, r.x, xP, v.x, iv.x, nx, dSx) || !axis_dist(1, r.y, yP, v.y, iv.y, ny, dSy) ||
         !axis_dist(2, r.z, zP, v.z, iv.z, nz, dSz)) {
-      ++lc.silent;
+      bump<kCntSilent>();
       end_history();
       return;
     }
@@ -878,7 +935,7 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
       if (r.y <= Y1 || yP < 1) { if (v.y < (Real)0) flip(1); yP = 1; r.y = Y1; }
       if (r.z <= Z1 || zP < 1) { if (v.z < (Real)0) flip(2); zP = 1; r.z = Z1; }
     }
-    if (segI >= g.safe_limit) { ++lc.safe_hits; end_history(); }
+    if (segI >= g.safe_limit) { bump<kCntSafe>(); end_history(); }
   }
 };
 
@@ -939,6 +996,22 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
   m.hot = hot_all + (threadIdx.x >> 5) * (kHotSrc * kHot3);
   for (int i = threadIdx.x & 31; i < kHotSrc * kHot3; i += 32) m.hot[i] = 0.f;
   m.hot_nu = 0;
+  // the warps' counters follow the accumulators (8-byte aligned): crossings
+  // (64-bit), then the event counts (32-bit: at most one per queue entry)
+  const int nwarps = blockDim.x >> 5;
+  unsigned long long *wcx_all = (unsigned long long *)(hot_all + nwarps * (kHotSrc * kHot3));
+  m.wcx = wcx_all + (threadIdx.x >> 5);
+  m.wc = (unsigned int *)(wcx_all + nwarps) + (threadIdx.x >> 5) * kCntSlots;
+  if ((threadIdx.x & 31) == 0) *m.wcx = 0ull;
+  if ((threadIdx.x & 31) < kCntSlots) m.wc[threadIdx.x & 31] = 0u;
+  // then the warps' escape counts and the stars' origins
+  m.esc_n = (unsigned int *)(wcx_all + nwarps) + nwarps * kCntSlots + (threadIdx.x >> 5) * kHotSrc;
+  int *org = (int *)((unsigned int *)(wcx_all + nwarps) + nwarps * (kCntSlots + kHotSrc)) + (threadIdx.x >> 5) * kHotSrc;
+  if ((threadIdx.x & 31) < kHotSrc) {
+    m.esc_n[threadIdx.x & 31] = 0u;
+    org[threadIdx.x & 31] = (int)(threadIdx.x & 31) < S.nsrc ? origin_of(g, S.s[threadIdx.x & 31]) : -1;
+  }
+  m.esc_org = org;
   __syncwarp();
   const unsigned long long t0 = global_ns();
   const unsigned int lane = threadIdx.x & 31;
@@ -950,7 +1023,29 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
   unsigned long long cbeg = 0, cend = 0;
   bool qdone = qlen == 0;
   unsigned int iter = 0;
+  // warp-aggregated append of the absorbed packets to the next round's list
+  auto append_absorbed = [&]() {
+    const unsigned int pm = __ballot_sync(0xffffffffu, m.pend);
+    if (pm) {
+      const int leader = __ffs(pm) - 1;
+      unsigned int base = 0;
+      if ((int)lane == leader) base = atomicAdd(w.a_count, (unsigned int)__popc(pm));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (m.pend) m.write_absorbed(base + __popc(pm & lt_mask));
+    }
+  };
   while (true) {
+    if (Fast) {
+      // parked events are handled together, once they and the free lanes
+      // number refill_min or no lane is left crossing; the lanes they free
+      // are refilled right after
+      const unsigned int parked = __ballot_sync(0xffffffffu, m.valid && m.pev != 0);
+      const unsigned int idle = parked | __ballot_sync(0xffffffffu, !m.valid);
+      if (parked && (__popc(idle) >= refill_min || idle == 0xffffffffu)) {
+        if (m.valid && m.pev != 0) m.handle_parked();
+        append_absorbed();
+      }
+    }
     const unsigned int need = __ballot_sync(0xffffffffu, !m.valid);
     if (!qdone && (__popc(need) >= refill_min || need == 0xffffffffu)) {
       const unsigned int nneed = __popc(need);
@@ -986,17 +1081,11 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
       if (qdone) break;
       continue;
     }
-    if (m.valid) {
-      if (Fast) m.advance(w.inner_steps);
-      else m.step();
-    }
-    const unsigned int pm = __ballot_sync(0xffffffffu, m.pend);
-    if (pm) {  // warp-aggregated append of the absorbed packets
-      const int leader = __ffs(pm) - 1;
-      unsigned int base = 0;
-      if ((int)lane == leader) base = atomicAdd(w.a_count, (unsigned int)__popc(pm));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (m.pend) m.write_absorbed(base + __popc(pm & lt_mask));
+    if (Fast) {
+      if (m.valid && m.pev == 0) m.advance(w.inner_steps);
+    } else {
+      if (m.valid) m.step();
+      append_absorbed();
     }
     if (((++iter) & 1023u) == 1u) {
       const unsigned long long el = global_ns() - t0;
@@ -1007,12 +1096,22 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
       }
     }
   }
-  if (Fast) m.hot_flush(lane);
+  if (Fast) {
+    m.hot_flush(lane);
+    m.count_crossings();
+    __syncwarp();
+    if (lane == 0) {
+      lc.crossings = *m.wcx; lc.absorptions = m.wc[kCntAbs]; lc.scatterings = m.wc[kCntSca];
+      lc.escaped = m.wc[kCntEsc]; lc.trapped = m.wc[kCntTrap]; lc.silent = m.wc[kCntSilent];
+      lc.safe_hits = m.wc[kCntSafe];
+    }
+  }
   flush_counts(cnt, lc);
 }
 
 template <typename Real> __host__ __device__ inline size_t march_smem_bytes(int nx, int ny, int nz, int warps) {
-  return ((table_bytes<Real>(nx, ny, nz) + 15) & ~(size_t)15) + (size_t)warps * kHotSrc * kHot3 * sizeof(float);
+  return ((table_bytes<Real>(nx, ny, nz) + 15) & ~(size_t)15) + (size_t)warps * kHotSrc * kHot3 * sizeof(float) +
+         (size_t)warps * (sizeof(unsigned long long) + (kCntSlots + 2 * kHotSrc) * sizeof(unsigned int));
 }
 
 }  // namespace mcg
