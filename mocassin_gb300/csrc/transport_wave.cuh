@@ -1019,7 +1019,10 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
   const unsigned int qlen = w.bin_count[0];
   const int refill_min = w.refill_min;
   // the warp's current chunk [cbeg, cend) of the sorted queue
-  constexpr unsigned int kChunk = 64;
+  // (64..512 packets: at least four chunks per warp; a warp's consecutive
+  // chunks lie far apart in the sorted queue, so each starts a new bin and a
+  // flush of the warp's accumulators)
+  const unsigned int kChunk = max(64u, min(512u, qlen / (gridDim.x * (blockDim.x >> 5) * 4u)));
   unsigned long long cbeg = 0, cend = 0;
   bool qdone = qlen == 0;
   unsigned int iter = 0;
