@@ -977,9 +977,10 @@ template <typename Real> __host__ __device__ inline size_t table_bytes(int nx, i
 // The persistent march of one round.  Lanes refill from the sorted queue in
 // batches of at least `refill_min` free lanes (or when the warp is empty).
 // Gas-only fast path: 64 registers (4 blocks of 256 per SM: the latency of
-// the opacity gather and the L2 atomics is hidden by warps); the dust and
-// exact paths keep their registers.
-template <bool Fast, bool Dust> struct MarchOccupancy { static constexpr int kMinBlocks = Fast ? (Dust ? 2 : 4) : 1; };
+// the opacity gather and the L2 atomics is hidden by warps); dust fast path:
+// 80 registers (3 blocks; 4 spill the scattering state); the exact path keeps
+// its registers.
+template <bool Fast, bool Dust> struct MarchOccupancy { static constexpr int kMinBlocks = Fast ? (Dust ? 3 : 4) : 1; };
 
 template <typename Real, bool Fast, bool Dust, bool Replay>
 __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks)) wave_march_kernel(const __grid_constant__ DevGrid g,
