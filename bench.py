@@ -257,7 +257,39 @@ def batched_models(args):
         srv.submit(sp)
     rep = srv.run()
     rep["batch"] = "%d of the 64-model batch (seed 1)" % len(specs)
+    rep["one_launch_transport"] = batch_launch_transport(specs)
     return rep
+
+
+def batch_launch_transport(specs):
+    """One transport iteration of the same models, all resident: each model's
+    own call in turn (mc_ctx_run, host-driven rounds) against one batched call
+    whose rounds run in step with one persistent march launch per round over
+    every model (mc_batch_run).  Same draws, so the same crossings."""
+    from mocassin_gb300 import nebula, transport
+    ctxs = [transport.TransportContext(nebula.build(sp)) for sp in specs]
+    try:
+        seeds = [101 + i for i in range(len(ctxs))]
+
+        def one_by_one():
+            return [c.run(seed=s, zero_first=True) for c, s in zip(ctxs, seeds)]
+
+        def batched():
+            return transport.batch_run(ctxs, seeds=seeds, zero_first=True)
+
+        out = {"models": len(ctxs)}
+        for name, fn in (("one_by_one", one_by_one), ("batched", batched)):
+            fn()  # warm-up (both calls return after their device work)
+            t0 = time.perf_counter()
+            st = fn()
+            wall = time.perf_counter() - t0
+            cross = sum(x["crossings"] for x in st)
+            out[name] = {"wall_ms": wall * 1e3, "crossings": int(cross), "crossings_per_s": cross / wall}
+        out["speedup"] = out["one_by_one"]["wall_ms"] / out["batched"]["wall_ms"]
+        return out
+    finally:
+        for c in ctxs:
+            c.close()
 
 
 def main():

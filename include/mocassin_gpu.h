@@ -221,6 +221,20 @@ mc_status mc_ctx_zero(mc_ctx_t *ctx);
 mc_status mc_ctx_run(mc_ctx_t *ctx, const mc_source_t *src, int32_t nsrc,
                      const mc_run_opts_t *opts, mc_stats_t *stats);
 
+/* One transport iteration of n resident models (contexts of one device,
+ * all gas-only or all dusty): mc_ctx_run of each model, the models' rounds
+ * in step, every round's march one persistent launch over all of them
+ * (blocks take (model, share) tasks from a global counter).  srcs[i] /
+ * nsrcs[i] / opts[i] are model i's arguments of mc_ctx_run; one precision
+ * per batch and Philox draws only (MC_ERR_UNSUPPORTED for replay).  Each
+ * model consumes the draws of its own mc_ctx_run, so its estimators and
+ * counters are those of that call.  stats[i] (may be NULL) is model i's;
+ * march_ms is the batched marches' total.  The reference runs one model
+ * per process; the call replaces energyPacketDriver (photon_mod.f90:26-285)
+ * for many models at once. */
+mc_status mc_batch_run(mc_ctx_t *const *ctxs, int32_t n, const mc_source_t *const *srcs,
+                       const int32_t *nsrcs, const mc_run_opts_t *opts, mc_stats_t *stats);
+
 /* Copies the device estimators into host arrays (adds into them when
  * accumulate != 0, else overwrites).  Any pointer may be NULL. */
 mc_status mc_ctx_download(mc_ctx_t *ctx, double *jste, double *jdif,

@@ -27,6 +27,14 @@ cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round);
 cudaError_t launch_wave_emit_fp64(const WaveLaunch &L, int round);
 cudaError_t launch_wave_march_fp32(const WaveLaunch &L);
 cudaError_t launch_wave_march_fp64(const WaveLaunch &L);
+// batched march over many models' rounds: the resident grid size first (it
+// sets the tasks per pass), then the launch
+cudaError_t launch_wave_march_batch_blocks_fp32(bool dust, size_t smem, int num_sms, int *blocks);
+cudaError_t launch_wave_march_batch_blocks_fp64(bool dust, size_t smem, int num_sms, int *blocks);
+cudaError_t launch_wave_march_batch_fp32(const BatchLaunch &B);
+cudaError_t launch_wave_march_batch_fp64(const BatchLaunch &B);
+size_t march_batch_smem_fp32(int nx, int ny, int nz);
+size_t march_batch_smem_fp64(int nx, int ny, int nz);
 
 // Scan of the per-bin counts and scatter of the round's n entries into the
 // frequency-sorted queue; fold of march-indexed estimators into rows;

@@ -171,6 +171,7 @@ struct mc_ctx {
   int rounds = 0;
   cudaEvent_t evm0 = nullptr, evm1 = nullptr;
   mcg::DevGrid g{};
+  DBuf batch_desc;  // mc_batch_run's model descriptors and task counter (first context of a batch)
 };
 
 namespace {
@@ -888,6 +889,193 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
   if (h.error_code != 0)
     return set_error((mc_status)h.error_code, "device error %d in packet %d", h.error_code, h.error_packet);
   return MC_OK;
+}
+
+mc_status mc_batch_run(mc_ctx_t *const *ctxs, int32_t n, const mc_source_t *const *srcs, const int32_t *nsrcs,
+                       const mc_run_opts_t *opts, mc_stats_t *stats) {
+  NvtxRange nvtx_range("mc batch transport");
+  if (!ctxs || !srcs || !nsrcs || !opts) return set_error(MC_ERR_ARG, "ctxs/srcs/nsrcs/opts is NULL");
+  if (n < 1 || n > 4096) return set_error(MC_ERR_ARG, "1..4096 models per batch");
+  const int prec = opts[0].precision;
+  if (prec != MC_PREC_FP32 && prec != MC_PREC_FP64) return set_error(MC_ERR_ARG, "precision must be MC_PREC_FP32 or MC_PREC_FP64");
+  const bool f64 = prec == MC_PREC_FP64;
+  mc_ctx_t *c0 = ctxs[0];
+  if (!c0) return set_error(MC_ERR_ARG, "ctxs[0] is NULL");
+  struct Model {
+    mc_ctx_t *c;
+    mcg::WaveLaunch L;
+    mcg::DevCounters h;
+    unsigned int n_round;
+    bool live;
+    int rounds;
+  };
+  std::vector<Model> M((size_t)n);
+  const bool dust = c0->flags & MC_FLAG_DUST;
+  for (int i = 0; i < n; ++i) {  // every argument is checked before any model is touched
+    mc_ctx_t *c = ctxs[i];
+    const mc_run_opts_t *o = opts + i;
+    if (!c || !srcs[i]) return set_error(MC_ERR_ARG, "model %d: ctx/src is NULL", i);
+    if (o->precision != prec) return set_error(MC_ERR_ARG, "model %d: one precision per batch", i);
+    if (o->rng != MC_RNG_PHILOX) return set_error(MC_ERR_UNSUPPORTED, "model %d: a batch draws from Philox only", i);
+    if (c->device != c0->device) return set_error(MC_ERR_ARG, "model %d: contexts of one device only", i);
+    if ((bool)(c->flags & MC_FLAG_DUST) != dust) return set_error(MC_ERR_UNSUPPORTED, "model %d: gas and dusty grids in one batch", i);
+    for (int j = 0; j < i; ++j)
+      if (ctxs[j] == c) return set_error(MC_ERR_ARG, "model %d: context given twice", i);
+  }
+  for (int i = 0; i < n; ++i) {
+    mc_ctx_t *c = ctxs[i];
+    const mc_run_opts_t *o = opts + i;
+    mcg::DevSources S{};
+    mc_status st = make_sources(c, srcs[i], nsrcs[i], o, S);
+    if (st) return st;
+    mcg::DevGrid g = c->g;
+    g.recursion_limit = o->recursion_limit > 0 ? o->recursion_limit : 5000;
+    g.safe_limit = o->safe_limit > 0 ? o->safe_limit : 500000;
+    Model &m = M[(size_t)i];
+    m.c = c;
+    m.h = mcg::DevCounters{};
+    m.h.error_packet = -1;
+    m.h.budget_ns = (unsigned long long)kernel_budget_ns();
+    MC_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if (o->run_flags & MC_RUN_ZERO_FIRST) {
+      mc_status z = mc_ctx_zero(c);
+      if (z) return z;
+    }
+    MC_CUDA(cudaMemcpyAsync(c->counters.p, &m.h, sizeof m.h, cudaMemcpyHostToDevice, c->stream));
+    if (c->cdf_pending) {
+      MC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_cdf, 0));
+      c->cdf_pending = false;
+    }
+    st = wave_setup(c, g, S, mcg::DevReplay{nullptr, 0}, m.L);
+    if (st) return st;
+    m.n_round = (unsigned int)S.total;
+    m.live = S.total > 0;
+    m.rounds = 0;
+  }
+  // descriptors of the round's live models, then the task counter
+  const size_t desc_bytes = ((size_t)n * sizeof(mcg::BatchModel) + 15) & ~(size_t)15;
+  if (c0->batch_desc.bytes < desc_bytes + 16) {
+    if (c0->batch_desc.p) { cudaFree(c0->batch_desc.p); c0->batch_desc.p = nullptr; c0->batch_desc.bytes = 0; }
+    MC_CUDA(c0->batch_desc.alloc(desc_bytes + 16));
+  }
+  mcg::BatchModel *d_models = c0->batch_desc.as<mcg::BatchModel>();
+  unsigned int *d_task = (unsigned int *)((char *)c0->batch_desc.p + desc_bytes);
+  std::vector<mcg::BatchModel> hm;
+  float march_ms = 0.f;
+  for (int round = 0;; ++round) {
+    unsigned long long total = 0;
+    size_t smem = 0;
+    hm.clear();
+    for (auto &m : M) {
+      if (!m.live) continue;
+      mc_ctx_t *c = m.c;
+      MC_CUDA(cudaMemsetAsync(c->bins.p, 0, (size_t)c->nb * 2 * sizeof(unsigned int), c->stream));
+      cudaError_t e;
+      if (round == 0) e = f64 ? mcg::launch_wave_sample_stellar_fp64(m.L) : mcg::launch_wave_sample_stellar_fp32(m.L);
+      else e = f64 ? mcg::launch_wave_sample_reemit_fp64(m.L, m.n_round) : mcg::launch_wave_sample_reemit_fp32(m.L, m.n_round);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "sample launch failed: %s", cudaGetErrorString(e));
+      MC_CUDA(mcg::launch_wave_sort(m.L, m.n_round));
+      e = f64 ? mcg::launch_wave_emit_fp64(m.L, round) : mcg::launch_wave_emit_fp32(m.L, round);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "emit launch failed: %s", cudaGetErrorString(e));
+      if (c != c0) {
+        MC_CUDA(cudaEventRecord(c->evm0, c->stream));
+        MC_CUDA(cudaStreamWaitEvent(c0->stream, c->evm0, 0));
+      }
+      total += m.n_round;
+      const size_t sh = f64 ? mcg::march_batch_smem_fp64(c->nx, c->ny, c->nz) : mcg::march_batch_smem_fp32(c->nx, c->ny, c->nz);
+      smem = sh > smem ? sh : smem;
+      mcg::BatchModel b{};
+      b.g = m.L.g;
+      b.S = m.L.S;
+      b.w = m.L.w;
+      b.cnt = m.L.cnt;
+      hm.push_back(b);
+      ++m.rounds;
+    }
+    if (hm.empty()) break;
+    int blocks = 0;
+    MC_CUDA(f64 ? mcg::launch_wave_march_batch_blocks_fp64(dust, smem, c0->num_sms, &blocks)
+                : mcg::launch_wave_march_batch_blocks_fp32(dust, smem, c0->num_sms, &blocks));
+    // each model's share of one pass of tasks follows its packets
+    unsigned int end = 0;
+    size_t k = 0;
+    for (auto &m : M) {
+      if (!m.live) continue;
+      const double share = (double)blocks * (double)m.n_round / (double)(total ? total : 1);
+      const unsigned int t = share < 1.0 ? 1u : (unsigned int)(share + 0.5);
+      end += t;
+      hm[k++].task_end = end;
+    }
+    MC_CUDA(cudaMemcpyAsync(d_models, hm.data(), hm.size() * sizeof(mcg::BatchModel), cudaMemcpyHostToDevice, c0->stream));
+    MC_CUDA(cudaMemsetAsync(d_task, 0, sizeof(unsigned int), c0->stream));
+    mcg::BatchLaunch B{d_models, (int)hm.size(), end, d_task, smem, blocks, dust, c0->stream};
+    MC_CUDA(cudaEventRecord(c0->evm0, c0->stream));
+    cudaError_t e = f64 ? mcg::launch_wave_march_batch_fp64(B) : mcg::launch_wave_march_batch_fp32(B);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "batched march launch failed: %s", cudaGetErrorString(e));
+    MC_CUDA(cudaEventRecord(c0->evm1, c0->stream));
+    std::vector<unsigned int> hcount(M.size(), 0u);
+    std::vector<int> herr(M.size(), 0);
+    for (size_t i = 0; i < M.size(); ++i) {
+      Model &m = M[i];
+      if (!m.live) continue;
+      if (m.c != c0) MC_CUDA(cudaStreamWaitEvent(m.c->stream, c0->evm1, 0));
+      MC_CUDA(cudaMemcpyAsync(&hcount[i], m.L.w.a_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, m.c->stream));
+      MC_CUDA(cudaMemcpyAsync(&herr[i], &m.L.cnt->error_code, sizeof(int), cudaMemcpyDeviceToHost, m.c->stream));
+    }
+    for (auto &m : M)
+      if (m.live) MC_CUDA(cudaStreamSynchronize(m.c->stream));
+    MC_CUDA(cudaStreamSynchronize(c0->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c0->evm0, c0->evm1);
+    march_ms += ms;
+    for (size_t i = 0; i < M.size(); ++i) {
+      Model &m = M[i];
+      if (!m.live) continue;
+      m.n_round = hcount[i];
+      if (m.n_round == 0 || herr[i] != 0) m.live = false;
+      else if (round > m.L.g.recursion_limit + 1)
+        return set_error(MC_ERR_BOUNDS, "model %d: re-emission rounds exceeded recursionLimit", (int)i);
+    }
+  }
+  mc_status first = MC_OK;
+  for (size_t i = 0; i < M.size(); ++i) {
+    Model &m = M[i];
+    mc_ctx_t *c = m.c;
+    if (!c->identity && m.rounds > 0) {
+      MC_CUDA(mcg::launch_wave_fold(c->jste_m.as<double>(), c->jste.as<double>(), m.L.w.lin2cell, c->ncell3, c->nc + 1,
+                                    c->nb, c->stream));
+      if (c->jdif_m.p)
+        MC_CUDA(mcg::launch_wave_fold(c->jdif_m.as<double>(), c->jdif.as<double>(), m.L.w.lin2cell, c->ncell3,
+                                      c->nc + 1, c->nb, c->stream));
+    }
+    MC_CUDA(cudaEventRecord(c->ev1, c->stream));
+    MC_CUDA(cudaMemcpyAsync(&m.h, c->counters.p, sizeof m.h, cudaMemcpyDeviceToHost, c->stream));
+    MC_CUDA(cudaStreamSynchronize(c->stream));
+    c->rounds = m.rounds;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (stats) {
+      mc_stats_t &t = stats[i];
+      t.crossings = (int64_t)m.h.crossings;
+      t.absorptions = (int64_t)m.h.absorptions;
+      t.scatterings = (int64_t)m.h.scatterings;
+      t.escaped = (int64_t)m.h.escaped;
+      t.lines = (int64_t)m.h.lines;
+      t.trapped = (int64_t)m.h.trapped;
+      t.silent_exits = (int64_t)m.h.silent;
+      t.safe_limit_hits = (int64_t)m.h.safe_hits;
+      t.qphot = m.h.qphot;
+      t.kernel_ms = ms;
+      t.error_code = m.h.error_code;
+      t.error_packet = m.h.error_packet;
+      t.march_ms = march_ms;
+      t.rounds = m.rounds;
+    }
+    if (m.h.error_code != 0 && first == MC_OK)
+      first = set_error((mc_status)m.h.error_code, "model %d: device error %d in packet %d", (int)i, m.h.error_code,
+                        m.h.error_packet);
+  }
+  return first;
 }
 
 mc_status mc_ctx_download(mc_ctx_t *c, double *jste, double *jdif, double *escaped, int32_t accumulate) {

@@ -70,6 +70,30 @@ template <bool Dust, bool Replay> static cudaError_t march_impl(const WaveLaunch
   k<<<L.num_sms * per_sm, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, L.cnt);
   return cudaGetLastError();
 }
+template <bool Dust> static cudaError_t march_batch_blocks(size_t smem, int num_sms, int *blocks) {
+  auto k = wave_march_batch_kernel<float, true, Dust>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+  if (e != cudaSuccess) return e;
+  *blocks = num_sms * (per_sm < 1 ? 1 : per_sm);
+  return cudaSuccess;
+}
+cudaError_t launch_wave_march_batch_blocks_fp32(bool dust, size_t smem, int num_sms, int *blocks) {
+  return dust ? march_batch_blocks<true>(smem, num_sms, blocks) : march_batch_blocks<false>(smem, num_sms, blocks);
+}
+cudaError_t launch_wave_march_batch_fp32(const BatchLaunch &B) {
+  if (B.dust)
+    wave_march_batch_kernel<float, true, true><<<B.blocks, 256, B.smem, B.stream>>>(B.models, B.nmodels, B.tasks_per_pass,
+                                                                                  B.task_ctr);
+  else
+    wave_march_batch_kernel<float, true, false><<<B.blocks, 256, B.smem, B.stream>>>(B.models, B.nmodels, B.tasks_per_pass,
+                                                                                   B.task_ctr);
+  return cudaGetLastError();
+}
+size_t march_batch_smem_fp32(int nx, int ny, int nz) { return march_smem_bytes<float>(nx, ny, nz, 256 / 32); }
+
 cudaError_t launch_wave_march_fp32(const WaveLaunch &L) {
   const bool dust = L.g.flags & MC_FLAG_DUST;
   if (L.rp.draws) return dust ? march_impl<true, true>(L) : march_impl<false, true>(L);

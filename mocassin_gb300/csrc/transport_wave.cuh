@@ -982,12 +982,11 @@ template <typename Real> __host__ __device__ inline size_t table_bytes(int nx, i
 // its registers.
 template <bool Fast, bool Dust> struct MarchOccupancy { static constexpr int kMinBlocks = Fast ? (Dust ? 3 : 4) : 1; };
 
+// The march of one model's round by one block: tables, accumulators and
+// counters in `smem`, then the warps drain the model's sorted queue.
 template <typename Real, bool Fast, bool Dust, bool Replay>
-__global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks)) wave_march_kernel(const __grid_constant__ DevGrid g,
-                                                        const __grid_constant__ DevSources S,
-                                                        const __grid_constant__ DevReplay rp,
-                                                        const __grid_constant__ WaveGrid w, DevCounters *cnt) {
-  extern __shared__ __align__(16) char smem[];
+__device__ __forceinline__ void march_body(const DevGrid &g, const DevSources &S, const DevReplay &rp,
+                                           const WaveGrid &w, DevCounters *cnt, char *smem) {
   Tables<Real> T;
   build_tables<Real>(g, smem, T);
   LocalCounts lc;
@@ -1111,6 +1110,57 @@ __global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
     }
   }
   flush_counts(cnt, lc);
+}
+
+template <typename Real, bool Fast, bool Dust, bool Replay>
+__global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks)) wave_march_kernel(const __grid_constant__ DevGrid g,
+                                                        const __grid_constant__ DevSources S,
+                                                        const __grid_constant__ DevReplay rp,
+                                                        const __grid_constant__ WaveGrid w, DevCounters *cnt) {
+  extern __shared__ __align__(16) char smem[];
+  march_body<Real, Fast, Dust, Replay>(g, S, rp, w, cnt, smem);
+}
+
+// One persistent march over the same round of many models.  Each model's
+// round is split into `share` tasks, listed twice (every model's first
+// shares, then every model's second ones) so that all models start at once
+// and blocks freed by a small model join the larger ones; a block takes
+// tasks from one global counter, copies the model's descriptors into shared
+// memory, builds its axis tables and joins that model's queue until it is
+// empty.  Philox draws only (no replay).
+template <typename Real, bool Fast, bool Dust>
+__global__ void __launch_bounds__(256, (MarchOccupancy<Fast, Dust>::kMinBlocks))
+    wave_march_batch_kernel(const BatchModel *models, int nmodels, unsigned int tasks_per_pass,
+                            unsigned int *task_ctr) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ __align__(16) BatchModel bm;
+  __shared__ int s_model;
+  const DevReplay rp{nullptr, 0};
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned int t = atomicAdd(task_ctr, 1u);
+      int m = -1;
+      if (t < 2u * tasks_per_pass) {
+        const unsigned int tp = t % tasks_per_pass;
+        int lo = 0, hi = nmodels - 1;  // first model whose task_end > tp
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (models[mid].task_end > tp) hi = mid;
+          else lo = mid + 1;
+        }
+        m = lo;
+      }
+      s_model = m;
+    }
+    __syncthreads();
+    const int m = s_model;
+    if (m < 0) break;
+    const int *src = (const int *)(models + m);
+    for (int i = threadIdx.x; i < (int)(sizeof(BatchModel) / sizeof(int)); i += blockDim.x) ((int *)&bm)[i] = src[i];
+    __syncthreads();
+    march_body<Real, Fast, Dust, false>(bm.g, bm.S, rp, bm.w, bm.cnt, smem);
+    __syncthreads();
+  }
 }
 
 template <typename Real> __host__ __device__ inline size_t march_smem_bytes(int nx, int ny, int nz, int warps) {

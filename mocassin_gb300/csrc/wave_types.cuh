@@ -47,6 +47,26 @@ struct WaveGrid {
   void *a_r;                // Real[3]
 };
 
+// One model of a batched march (wave_march_batch_kernel).
+struct BatchModel {
+  DevGrid g;
+  DevSources S;
+  WaveGrid w;
+  DevCounters *cnt;
+  unsigned int task_end;  // tasks of models 0..this one in one pass
+};
+
+struct BatchLaunch {
+  const BatchModel *models;   // device array
+  int nmodels;
+  unsigned int tasks_per_pass;
+  unsigned int *task_ctr;     // device, zeroed before the launch
+  size_t smem;                // dynamic shared memory: the largest model's
+  int blocks;                 // from launch_wave_march_batch_blocks_*
+  bool dust;
+  cudaStream_t stream;
+};
+
 struct WaveLaunch {
   DevGrid g;
   DevSources S;

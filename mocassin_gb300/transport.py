@@ -53,6 +53,9 @@ def library():
         lib.mc_ctx_zero.restype = C.c_int
         lib.mc_ctx_zero.argtypes = [C.c_void_p]
         lib.mc_ctx_run.restype = C.c_int
+        lib.mc_batch_run.restype = C.c_int
+        lib.mc_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.POINTER(abi.McSource)),
+                                     C.POINTER(C.c_int32), C.POINTER(abi.McRunOpts), C.POINTER(abi.McStats)]
         lib.mc_ctx_run.argtypes = [C.c_void_p, C.POINTER(abi.McSource), C.c_int32, C.POINTER(abi.McRunOpts),
                                    C.POINTER(abi.McStats)]
         lib.mc_ctx_download.restype = C.c_int
@@ -459,3 +462,29 @@ class TransportContext:
             self.close()
         except Exception:
             pass
+
+
+def batch_run(contexts, n_packets=None, seeds=None, iteration=1, precision="fp32", recursion_limit=0,
+              safe_limit=0, zero_first=False):
+    """One transport iteration of many resident models, their rounds in step and
+    every round's march one persistent launch over all of them (mc_batch_run).
+    Model i draws as ``contexts[i].run(seed=seeds[i], ...)`` would, so its
+    estimators and counters are those of that call.  Returns the per-model stats."""
+    contexts = list(contexts)
+    n = len(contexts)
+    if n == 0:
+        return []
+    lib = library()
+    seeds = list(range(1, n + 1)) if seeds is None else list(seeds)
+    npk = [n_packets] * n if n_packets is None or np.isscalar(n_packets) else list(n_packets)
+    marsh = [abi.Marshalled(ctx.neb, n_packets=npk[i]) for i, ctx in enumerate(contexts)]
+    prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
+    opts = (abi.McRunOpts * n)(*[abi.make_opts(seed=seeds[i], iteration=iteration, precision=prec,
+                                               recursion_limit=recursion_limit, safe_limit=safe_limit,
+                                               run_flags=_flags("wave", zero_first)) for i in range(n)])
+    handles = (C.c_void_p * n)(*[ctx.handle for ctx in contexts])
+    srcs = (C.POINTER(abi.McSource) * n)(*[C.cast(m.sources, C.POINTER(abi.McSource)) for m in marsh])
+    nsrcs = (C.c_int32 * n)(*[m.nsrc for m in marsh])
+    stats = (abi.McStats * n)()
+    _check(lib.mc_batch_run(handles, n, srcs, nsrcs, opts, stats))
+    return [st.as_dict() for st in stats]
