@@ -24,7 +24,10 @@ ending in a full crossing or an interaction (source/photon_mod.f90:1517,
           batch's FP64 cell states), and of the plain form (FP64 update), with
           the converged states compared against the plain form's
   batched_models  the request loop over the first --batch-models of the
-          64-model batch: wall, p50 / p99 latency per Lambda iteration
+          64-model batch: wall, p50 / p99 latency per Lambda iteration; the
+          same requests served in lockstep (the resident models' transports in
+          one mc_batch_run per iteration); one transport iteration of those
+          models one call after another against one batched call
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -257,6 +260,15 @@ def batched_models(args):
         srv.submit(sp)
     rep = srv.run()
     rep["batch"] = "%d of the 64-model batch (seed 1)" % len(specs)
+    # the same requests served in lockstep: the group's transports in one
+    # mc_batch_run per Lambda iteration (one march launch per round)
+    lk = serve.ModelServer(memory_budget=200e9, workers=args.batch_workers, iterations=3,
+                           autotune_packets=200_000, lockstep=True, group=len(specs))
+    for sp in specs:
+        lk.submit(sp)
+    lrep = lk.run()
+    rep["lockstep"] = {k: lrep[k] for k in ("models", "errors", "wall_s", "crossings_per_s", "latency_ms_p50",
+                                            "latency_ms_p99", "peak_resident_models", "mode")}
     rep["one_launch_transport"] = batch_launch_transport(specs)
     return rep
 

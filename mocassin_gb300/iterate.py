@@ -102,6 +102,12 @@ class LambdaIteration:
         tr = self.ctx.run(n_packets=n_packets, seed=seed, iteration=len(self.history) + 1, precision="fp32",
                           zero_first=True, form=self.form)
         t1 = time.perf_counter()
+        return self.after_transport(tr, t0, t1)
+
+    def after_transport(self, tr, t0, t1):
+        """The rest of a Lambda iteration once its transport (stats tr, timed
+        t0..t1) has filled the resident Jste: cell update, surrogate, grain
+        temperatures, opacity and emission CDFs."""
         warm = self.trained
         up = self.ctx.update_cells(self.w, self.scale, xhi_limit=self.xhi, precision=self.update, warm=warm)
         t2 = time.perf_counter()
@@ -191,6 +197,23 @@ class LambdaIteration:
 
     def close(self):
         self.ctx.close()
+
+
+def batched_step(models, seeds, pool=None):
+    """One Lambda iteration of several resident models in step: their
+    transports in one mc_batch_run (the rounds of all models in step, one
+    persistent march launch per round), then each model's cell update,
+    opacity and emission CDFs (on ``pool``'s threads when given: every model
+    has its own stream).  Returns the models' iteration records; a model's
+    wall_s is the batched transport plus its own rest."""
+    t0 = time.perf_counter()
+    stats = transport.batch_run([m.ctx for m in models], seeds=seeds, iteration=len(models[0].history) + 1,
+                                precision="fp32", zero_first=True)
+    t1 = time.perf_counter()
+    if pool is None:
+        return [m.after_transport(st, t0, t1) for m, st in zip(models, stats)]
+    futs = [pool.submit(m.after_transport, st, t0, t1) for m, st in zip(models, stats)]
+    return [f.result() for f in futs]
 
 
 def training_rows(specs, max_rows=1_000_000, iterations=2, update="fp64", form="graph", seed=1):

@@ -11,11 +11,19 @@ reused), runs the iterations, and frees the device memory.  The C-ABI calls
 release the Python interpreter lock, so the models' kernels run concurrently
 on their streams and the host-side builds overlap with the GPU work.
 
+With lockstep=True the server instead admits a group of models (in request
+order, up to ``group`` of them and the memory budget) and advances the
+group one Lambda iteration at a time: the group's transports are one
+mc_batch_run (the rounds of all its models in step, one persistent march
+launch per round), then every model's cell update, opacity and emission
+CDFs run at once, one thread per model of the group.
+
 Reported: wall time, aggregate cell crossings per second, the p50 / p99 of
 the per-iteration latency, the peak number of resident models and bytes.
 """
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -35,7 +43,9 @@ def device_bytes(neb):
 
 class ModelServer:
     def __init__(self, memory_budget=200e9, workers=4, iterations=3, form="graph", update="fp32",
-                 autotune_packets=0):
+                 autotune_packets=0, lockstep=False, group=16):
+        self.lockstep = bool(lockstep)
+        self.group = int(group)
         self.budget = float(memory_budget)
         self.workers = int(workers)
         self.iterations = int(iterations)
@@ -102,8 +112,83 @@ class ModelServer:
         finally:
             self._release(nbytes)
 
+    def _tune(self, li, neb, form):
+        key = neb.nx
+        with self._lock:
+            tuned = self.tuning.get(key)
+        if tuned is None and self.autotune_packets > 0:
+            tuned, _ = autotune.autotune(li.ctx, min(self.autotune_packets, sum(neb.n_packets)), repeats=1,
+                                         candidates=((4, 4), (8, 4), (8, 8), (8, 16), (16, 8)), form=form)
+            with self._lock:
+                self.tuning[key] = tuned
+        if tuned is not None:
+            li.ctx.set_tuning(*tuned)
+
+    def _run_lockstep(self):
+        todo = list(self.requests)
+        # one thread per model of a group: every model's update, opacity and
+        # CDFs run at once on their own streams after the batched transport
+        with ThreadPoolExecutor(max(1, self.workers, self.group)) as pool:
+            i = 0
+            while i < len(todo):
+                t_req = time.perf_counter()
+                group = todo[i:i + self.group]
+                nebs = list(pool.map(lambda r: nebula.build(r[0]), group))
+                take, total = 0, 0
+                for neb in nebs:  # the group's models that fit in the budget (at least one)
+                    nb = device_bytes(neb)
+                    if take and total + nb > self.budget:
+                        break
+                    take, total = take + 1, total + nb
+                group, nebs = group[:take], nebs[:take]
+                i += take
+                self._admit(total)
+                self._resident_models += take - 1
+                self.peak_models = max(self.peak_models, self._resident_models)
+                lis = []
+                try:
+                    for neb in nebs:
+                        li = iterate.LambdaIteration(neb, form="wave", update=self.update)
+                        lis.append(li)
+                        self._tune(li, neb, "wave")
+                    t0 = time.perf_counter()
+                    lat = [[] for _ in lis]
+                    cross = [0] * len(lis)
+                    last = [None] * len(lis)
+                    for it in range(max(r[1] for r in group)):
+                        live = [k for k, r in enumerate(group) if it < r[1]]
+                        # mc_batch_run takes gas-only or dusty grids, not both
+                        for dusty in (False, True):
+                            ks = [k for k in live if bool(lis[k].dust is not None) == dusty]
+                            if not ks:
+                                continue
+                            recs = iterate.batched_step([lis[k] for k in ks], [1000 + it] * len(ks), pool=pool)
+                            for k, rec in zip(ks, recs):
+                                lat[k].append(rec["wall_s"])
+                                cross[k] += rec["crossings"]
+                                last[k] = rec
+                    t1 = time.perf_counter()
+                    for k, (spec, iters) in enumerate(group):
+                        self.results.append({"model": spec.name, "cells": nebs[k].ncells,
+                                             "packets": int(sum(nebs[k].n_packets)), "iterations": iters,
+                                             "latency_s": lat[k], "crossings": cross[k],
+                                             "converged_pct": last[k]["converged_pct"] if last[k] else None,
+                                             "run_s": t1 - t0, "queue_s": t0 - t_req,
+                                             "bytes": device_bytes(nebs[k])})
+                except Exception as exc:  # reported, the next group goes on
+                    self.errors.append("%s: %s" % (",".join(r[0].name for r in group), exc))
+                finally:
+                    for li in lis:
+                        li.close()
+                    self._resident_models -= take - 1
+                    self._release(total)
+
     def run(self):
         """Serves every submitted request; returns the report."""
+        if self.lockstep:
+            t0 = time.perf_counter()
+            self._run_lockstep()
+            return self._report(time.perf_counter() - t0)
         todo = list(self.requests)
         idx = [0]
         lock = threading.Lock()
@@ -126,7 +211,9 @@ class ModelServer:
             t.start()
         for t in threads:
             t.join()
-        wall = time.perf_counter() - t0
+        return self._report(time.perf_counter() - t0)
+
+    def _report(self, wall):
         lat = np.array([x for r in self.results for x in r["latency_s"]]) * 1e3
         cross = sum(r["crossings"] for r in self.results)
         return {"models": len(self.results), "errors": self.errors, "wall_s": wall,
@@ -138,4 +225,5 @@ class ModelServer:
                 "latency_ms_p99": float(np.percentile(lat, 99)) if len(lat) else None,
                 "peak_resident_models": self.peak_models, "peak_resident_bytes": self.peak_bytes,
                 "workers": self.workers, "memory_budget_bytes": self.budget,
+                "mode": "lockstep (mc_batch_run)" if self.lockstep else "threads (one context and stream each)",
                 "tuning": {str(k): list(v) for k, v in self.tuning.items()}}

@@ -88,3 +88,42 @@ def test_batch_rejects_gas_and_dust_together(gpu_lib):
     finally:
         for c in ctxs:
             c.close()
+
+
+def test_lockstep_lambda_iteration_matches_each_models_own(gpu_lib):
+    """iterate.batched_step: the models' transports in one mc_batch_run, then
+    their own updates.  The first iteration draws as each model's own step
+    (same crossings); the states after two iterations agree with the own
+    iterations' to the FP32 noise of the accumulators' flush order."""
+    import numpy as np
+
+    from mocassin_gb300 import iterate
+    specs = [GAS[0], GAS[2]]
+    a = [iterate.LambdaIteration(nebula.build(s), form="wave") for s in specs]
+    b = [iterate.LambdaIteration(nebula.build(s), form="wave") for s in specs]
+    try:
+        ra = iterate.batched_step(a, [50, 50])
+        rb = [m.step(seed=50) for m in b]
+        for x, y in zip(ra, rb):
+            assert x["crossings"] == y["crossings"]
+        iterate.batched_step(a, [51, 51])
+        for m in b:
+            m.step(seed=51)
+        for x, y in zip(a, b):
+            ta, tb = x.ctx.get_cell_state()[0], y.ctx.get_cell_state()[0]
+            ok = (ta > 0) & (tb > 0)
+            assert ok.sum() > 0
+            assert float(np.median(np.abs(ta[ok] / tb[ok] - 1))) < 1e-3
+    finally:
+        for m in a + b:
+            m.close()
+
+
+def test_lockstep_server_serves_every_request(gpu_lib):
+    from mocassin_gb300 import serve
+    srv = serve.ModelServer(workers=2, iterations=2, lockstep=True, group=2)
+    for s in (GAS[0], GAS[1], GAS[2]):
+        srv.submit(s)
+    rep = srv.run()
+    assert rep["errors"] == [] and rep["models"] == 3 and rep["iterations"] == 6
+    assert rep["latency_ms_p50"] > 0 and rep["mode"].startswith("lockstep")
