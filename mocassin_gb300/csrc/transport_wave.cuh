@@ -754,7 +754,6 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     const int stride = a == 0 ? g.ny * g.nz : (a == 1 ? g.nz : 1);
     lin += up ? stride : -stride;
     kap = (Real)__ldg(orow + lin);
-    if (segI >= g.safe_limit) return EV_SAFE;
     return EV_NONE;
   }
 
@@ -823,10 +822,15 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
   // with many lanes instead of one or two)
   __device__ void advance(int k) {
     int ev = EV_NONE, ea = 0;
-    for (int i = 0; i < k; ++i) {
+    // at most the crossings left before safeLimit: the run then ends in
+    // EV_SAFE after the crossing that reaches it, as a per-crossing test would
+    const int left = g.safe_limit - segI;
+    const int kk = left < k ? left : k;
+    for (int i = 0; i < kk; ++i) {
       ev = cross(ea);
       if (ev != EV_NONE) break;
     }
+    if (ev == EV_NONE && segI >= g.safe_limit) ev = EV_SAFE;
     pev = ev | (ea << 2);
   }
   __device__ void handle_parked() {

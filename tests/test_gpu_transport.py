@@ -121,6 +121,20 @@ def test_counted_stellar_escapes_equal_one_by_one_sums(gpu_lib, form, sym):
     np.testing.assert_allclose(es_w, es_p, rtol=1e-12, atol=0)
 
 
+@pytest.mark.parametrize("form,prec", [("wave", "fp32"), ("graph", "fp32"), ("wave", "fp64")])
+def test_safe_limit_known_answer(gpu_lib, form, prec):
+    """safeLimit (photon_mod.f90:1190) ends a packet's pathSegment after that
+    many loop bodies.  In a vacuum octant of 9 cells per axis with the star in
+    the corner cell a packet needs at least 9 crossings to leave, so with a
+    limit of 3 every packet stops after exactly 3."""
+    spec = nebula.NebulaSpec("vacsafe", 9, 3.0e18, True, [nebula.Star(40000.0, 10.0, (0, 0, 0), 20000)],
+                             nh_median=100.0, r_in=0.0)
+    neb = helpers.vacuum(nebula.build(spec))
+    _, _, _, st = transport.energy_packet_driver(neb, precision=prec, seed=9, form=form, safe_limit=3)
+    n = int(neb.n_packets[0])
+    assert st["safe_limit_hits"] == n and st["crossings"] == 3 * n and st["escaped"] == 0
+
+
 @pytest.mark.parametrize("form", FORMS)
 def test_zero_packets_and_errors(gpu_lib, form):
     neb = nebula.build(CASES[0])
