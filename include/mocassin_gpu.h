@@ -488,10 +488,17 @@ mc_status mc_ctx_get_opacity(mc_ctx_t *ctx, float *opacity);
  * the library holds until exit; grids above 1024 cells along an axis or
  * more than 16 sources are rejected with MC_ERR_UNSUPPORTED.  All calls
  * share that array, so calls that overlap on the GPU race: serialise them.
- * The first call on a device looks up the array's address; make it before
- * any stream capture.  `stream` is a cudaStream_t (NULL: default stream);
- * the call returns after the stream has finished its work.  Results equal
- * mc_transport_run with MC_RUN_FORM_PLAIN on the same inputs and draws. */
+ * Every call looks up the array's device address with the caller's device
+ * current (so a cudaDeviceReset, which moves it, is harmless); the first
+ * call on a device also loads the module there, so make it before any
+ * stream capture.  Every argument is checked before anything is written:
+ * the host-side ones first, then the caller's `active` array on the device
+ * (a negative entry, a sub-grid pointer, is MC_ERR_UNSUPPORTED; one above
+ * ncells is MC_ERR_ARG, as mc_transport_run reports them), and a rejected
+ * call returns with the estimators untouched.  `stream` is a cudaStream_t
+ * (NULL: default stream); the call returns after the stream has finished
+ * its work.  Results equal mc_transport_run with MC_RUN_FORM_PLAIN on the
+ * same inputs and draws. */
 mc_status mc_transport_run_noalloc(const mc_grid_t *grid, const mc_source_t *src, int32_t nsrc,
                                    const mc_run_opts_t *opts, double *jste, double *jdif,
                                    double *escaped, mc_stats_t *stats, void *stream);

@@ -17,15 +17,24 @@
 // MC_ERR_UNSUPPORTED).  The array takes kNoAllocScratchBytes of every GPU
 // that loads the library, until the process exits.  All calls share it:
 // calls that overlap on the GPU (two streams, two host threads) race on it,
-// so serialise them.  The first call on a device looks up the array's device
-// address (cudaGetSymbolAddress); make that first call before any stream
-// capture begins.
+// so serialise them.  Every call looks up the array's device address
+// (cudaGetSymbolAddress) with the caller's device current; the first call on
+// a device also loads the module there, so make that first call before any
+// stream capture begins.  Looking the address up per call keeps it right
+// after a cudaDeviceReset, which reloads the module elsewhere.
+//
+// Order of work: every host-side argument check runs first; then one small
+// kernel checks the caller's `active` array on the device (a negative entry
+// is a sub-grid pointer, MC_ERR_UNSUPPORTED; one above ncells is MC_ERR_ARG,
+// as mc_transport_run reports them) and the call waits for its verdict.  A
+// rejected call therefore returns before anything writes the caller's
+// estimators, and with nothing of its own left running on the stream.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/mocassin_gpu.h"
@@ -36,41 +45,50 @@
 namespace {
 
 constexpr int kNoAllocMaxAxis = 1024;
-constexpr int kNoAllocMaxDevices = 64;
-// layout: DevCounters | dx32 dy32 dz32 (floats) | dx64 dy64 dz64 (doubles)
+// layout: DevCounters (+ the active check's two first indices at
+// kCheckOffset) | dx32 dy32 dz32 (floats) | dx64 dy64 dz64 (doubles)
 constexpr size_t kCountersBytes = 256;
+constexpr size_t kCheckOffset = 128;
 constexpr size_t kF32Bytes = 3 * kNoAllocMaxAxis * sizeof(float);
 constexpr size_t kF64Bytes = 3 * kNoAllocMaxAxis * sizeof(double);
 constexpr size_t kNoAllocScratchBytes = kCountersBytes + kF32Bytes + kF64Bytes;
-static_assert(sizeof(mcg::DevCounters) <= kCountersBytes, "counters do not fit their slot");
+static_assert(sizeof(mcg::DevCounters) <= kCheckOffset, "counters do not fit their slot");
 
 // Host code must not use this name as an address: it is a host-side stand-in.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_setup_mutex;
-void *g_scratch_ptr[kNoAllocMaxDevices] = {nullptr};
+// First (lowest) index of a negative `active` entry and of one above ncells;
+// INT_MAX when there is none.
+struct ActiveCheck {
+  int first_negative;
+  int first_too_large;
+};
 
 mc_status fail(mc_status code, const char *msg) {
   mcg::set_last_error_text(msg);
   return code;
 }
 
-// Device address of the scratch array on the current device (looked up once
-// per device, with that device current).
+// Device address of the scratch array on the current device, looked up with
+// that device current.
 mc_status scratch_address(unsigned char **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(MC_ERR_NO_DEVICE, "no current CUDA device");
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(MC_ERR_UNSUPPORTED, "device index above 63");
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(MC_ERR_CUDA, (std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e)).c_str());
-    g_scratch_ptr[dev] = p;
-  }
-  *out = (unsigned char *)g_scratch_ptr[dev];
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(MC_ERR_CUDA, (std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e)).c_str());
+  *out = (unsigned char *)p;
   return MC_OK;
+}
+
+// The caller's active(nx,ny,nz) against the rows the march may touch.
+__global__ void noalloc_active_check_kernel(const int32_t *active, long long n, int ncells, ActiveCheck *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int a = active[i];
+    if (a < 0) atomicMin(&out->first_negative, (int)i);
+    if (a > ncells) atomicMin(&out->first_too_large, (int)i);
+  }
 }
 
 // dV widths / 1e15 of every cell index (photon_mod.f90:1469-1512), from the
@@ -125,19 +143,40 @@ extern "C" mc_status mc_transport_run_noalloc(const mc_grid_t *g, const mc_sourc
   if (o->precision != MC_PREC_FP32 && o->precision != MC_PREC_FP64) return fail(MC_ERR_ARG, "bad precision");
   if (o->rng == MC_RNG_REPLAY && (!o->replay || o->replay_stride <= 0)) return fail(MC_ERR_ARG, "replay needs draws");
 
+  // Sources: every host-side check before any device work is queued.
+  mcg::DevSources S{};
+  S.nsrc = nsrc;
+  long long tot = 0;
+  for (int i = 0; i < nsrc; ++i) {
+    const mc_source_t &x = src[i];
+    if (!x.spec_cdf || x.n_packets < 0) return fail(MC_ERR_ARG, "source needs a device spec_cdf and n >= 0");
+    if (x.cell[0] < 1 || x.cell[0] > g->nx || x.cell[1] < 1 || x.cell[1] > g->ny || x.cell[2] < 1 ||
+        x.cell[2] > g->nz)
+      return fail(MC_ERR_BOUNDS, "source cell outside the grid");
+    mcg::DevSource &s = S.s[i];
+    s.cdf = x.spec_cdf;  // device pointer, sampled by the linear scan
+    for (int k = 0; k < 3; ++k) { s.cell[k] = x.cell[k]; s.pos[k] = x.pos[k]; }
+    s.delta_e = x.delta_e;
+    s.k0 = (uint32_t)o->seed;
+    s.k1 = (uint32_t)(o->seed >> 32) ^ ((o->iteration & 0xFFFFFFu) << 8) ^ ((uint32_t)x.istar & 0xFFu);
+    s.n = x.n_packets;
+    s.base = tot;
+    tot += x.n_packets;
+  }
+  S.total = tot;
+
   unsigned char *base = nullptr;
   mc_status st = scratch_address(&base);
   if (st) return st;
   cudaStream_t stream = (cudaStream_t)stream_handle;
   const bool sym = g->flags & MC_FLAG_SYMMETRIC_XYZ;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) sms = 1;
 
-  // per-axis widths into the scratch tables (they keep the last call's grid)
-  float *d32 = (float *)(base + kCountersBytes);
-  double *d64 = (double *)(base + kCountersBytes + kF32Bytes);
-  noalloc_widths_kernel<<<1, 256, 0, stream>>>(g->x_axis, g->y_axis, g->z_axis, g->nx, g->ny, g->nz, sym ? 1 : 0,
-                                               d32, d64);
-  if (cudaGetLastError() != cudaSuccess) return fail(MC_ERR_CUDA, "width-table launch failed");
-  // the counters must start at zero every call (they keep the last call's values)
+  // The counters must start at zero every call (they keep the last call's
+  // values), and so must the active check.
   mcg::DevCounters h{};
   h.error_packet = -1;
   const char *be = getenv("MC_KERNEL_BUDGET_S");
@@ -145,8 +184,41 @@ extern "C" mc_status mc_transport_run_noalloc(const mc_grid_t *g, const mc_sourc
   if (!(budget > 0)) budget = 120.0;
   h.budget_ns = (unsigned long long)(budget * 1e9);
   mcg::DevCounters *dcnt = (mcg::DevCounters *)base;
-  if (cudaMemcpyAsync(dcnt, &h, sizeof h, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+  ActiveCheck chk{INT_MAX, INT_MAX};
+  ActiveCheck *dchk = (ActiveCheck *)(base + kCheckOffset);
+  if (cudaMemcpyAsync(dcnt, &h, sizeof h, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+      cudaMemcpyAsync(dchk, &chk, sizeof chk, cudaMemcpyHostToDevice, stream) != cudaSuccess)
     return fail(MC_ERR_CUDA, "counter reset failed");
+
+  // active(x,y,z) on the device: the march indexes opacity and Jste by it, so
+  // a row outside 0..ncells must stop the call before the march runs.
+  const long long ncell3 = (long long)g->nx * g->ny * g->nz;
+  {
+    const long long want = (ncell3 + 255) / 256;
+    const unsigned blocks = (unsigned)(want < (long long)sms * 4 ? want : (long long)sms * 4);
+    noalloc_active_check_kernel<<<blocks, 256, 0, stream>>>(g->active, ncell3, g->ncells, dchk);
+    if (cudaGetLastError() != cudaSuccess) return fail(MC_ERR_CUDA, "active-check launch failed");
+    if (cudaMemcpyAsync(&chk, dchk, sizeof chk, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
+      return fail(MC_ERR_CUDA, "reading the active check back failed");
+    const int neg = chk.first_negative, big = chk.first_too_large;
+    if (neg != INT_MAX || big != INT_MAX) {
+      char buf[96];
+      if (neg <= big) {
+        snprintf(buf, sizeof buf, "active < 0 (sub-grid pointer) at %d", neg);
+        return fail(MC_ERR_UNSUPPORTED, buf);
+      }
+      snprintf(buf, sizeof buf, "active entry %d exceeds ncells %d", big, g->ncells);
+      return fail(MC_ERR_ARG, buf);
+    }
+  }
+
+  // per-axis widths into the scratch tables (they keep the last call's grid)
+  float *d32 = (float *)(base + kCountersBytes);
+  double *d64 = (double *)(base + kCountersBytes + kF32Bytes);
+  noalloc_widths_kernel<<<1, 256, 0, stream>>>(g->x_axis, g->y_axis, g->z_axis, g->nx, g->ny, g->nz, sym ? 1 : 0,
+                                               d32, d64);
+  if (cudaGetLastError() != cudaSuccess) return fail(MC_ERR_CUDA, "width-table launch failed");
   if (o->run_flags & MC_RUN_ZERO_FIRST) {
     const size_t nj = (size_t)(g->ncells + 1) * g->nbins, ne = (size_t)(g->ncells + 1) * (g->nbins + 1);
     if (cudaMemsetAsync(jste, 0, nj * sizeof(double), stream) != cudaSuccess ||
@@ -176,31 +248,8 @@ extern "C" mc_status mc_transport_run_noalloc(const mc_grid_t *g, const mc_sourc
   d.safe_limit = o->safe_limit > 0 ? o->safe_limit : 500000;
   d.jste = jste; d.jdif = jdif; d.esc = escaped;
 
-  mcg::DevSources S{};
-  S.nsrc = nsrc;
-  long long tot = 0;
-  for (int i = 0; i < nsrc; ++i) {
-    const mc_source_t &x = src[i];
-    if (!x.spec_cdf || x.n_packets < 0) return fail(MC_ERR_ARG, "source needs a device spec_cdf and n >= 0");
-    if (x.cell[0] < 1 || x.cell[0] > g->nx || x.cell[1] < 1 || x.cell[1] > g->ny || x.cell[2] < 1 ||
-        x.cell[2] > g->nz)
-      return fail(MC_ERR_BOUNDS, "source cell outside the grid");
-    mcg::DevSource &s = S.s[i];
-    s.cdf = x.spec_cdf;  // device pointer, sampled by the linear scan
-    for (int k = 0; k < 3; ++k) { s.cell[k] = x.cell[k]; s.pos[k] = x.pos[k]; }
-    s.delta_e = x.delta_e;
-    s.k0 = (uint32_t)o->seed;
-    s.k1 = (uint32_t)(o->seed >> 32) ^ ((o->iteration & 0xFFFFFFu) << 8) ^ ((uint32_t)x.istar & 0xFFu);
-    s.n = x.n_packets;
-    s.base = tot;
-    tot += x.n_packets;
-  }
-  S.total = tot;
   mcg::DevReplay rp{o->rng == MC_RNG_REPLAY ? o->replay : nullptr, o->rng == MC_RNG_REPLAY ? o->replay_stride : 0};
 
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (tot > 0) {
     const long long want = (tot + 255) / 256;
     const long long blocks = want < (long long)sms * 2 ? want : (long long)sms * 2;
