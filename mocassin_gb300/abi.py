@@ -1,7 +1,7 @@
 """ctypes mirror of include/mocassin_gpu.h and marshalling from a Nebula.
 
 The structs here are byte-for-byte the C-ABI structs; a Fortran caller would
-declare the same layout with ``bind(C)`` derived types (see INTEGRATION.md).
+declare the same layout with ``bind(C)`` derived types.
 """
 from __future__ import annotations
 

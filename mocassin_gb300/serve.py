@@ -23,11 +23,18 @@ the per-iteration latency, the peak number of resident models and bytes.
 """
 import threading
 import time
+import zlib
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
 from . import autotune, iterate, nebula
+
+
+def model_seed(name, iteration):
+    """Philox seed of one model's Lambda iteration: distinct per model (from
+    its name) and per iteration, the same in threaded and lockstep serving."""
+    return 1000 + (zlib.crc32(name.encode()) & 0xFFFFF) * 64 + iteration
 
 
 def device_bytes(neb):
@@ -100,7 +107,7 @@ class ModelServer:
             lat = []
             cross = 0
             for it in range(iters):
-                rec = li.step(seed=1000 + it)
+                rec = li.step(seed=model_seed(spec.name, it))
                 lat.append(rec["wall_s"])
                 cross += rec["crossings"]
             t1 = time.perf_counter()
@@ -162,7 +169,8 @@ class ModelServer:
                             ks = [k for k in live if bool(lis[k].dust is not None) == dusty]
                             if not ks:
                                 continue
-                            recs = iterate.batched_step([lis[k] for k in ks], [1000 + it] * len(ks), pool=pool)
+                            recs = iterate.batched_step([lis[k] for k in ks],
+                                                        [model_seed(group[k][0].name, it) for k in ks], pool=pool)
                             for k, rec in zip(ks, recs):
                                 lat[k].append(rec["wall_s"])
                                 cross[k] += rec["crossings"]

@@ -46,7 +46,11 @@ def test_groups_follow_the_group_size_and_iterations(monkeypatch):
     assert rep["errors"] == [] and rep["models"] == 3 and rep["iterations"] == 7
     # group 1: gas[0] (2 iterations) and gas[1] (3) together, then gas[1] alone; group 2: gas[2]
     assert [len(c[0]) for c in calls] == [2, 2, 1, 1, 1]
-    assert [c[2][0] for c in calls] == [1000, 1001, 1002, 1000, 1001]
+    # every model draws its own stream per iteration, as in threaded serving
+    seed = lambda spec, it: serve.model_seed(spec.name, it)
+    assert [c[2] for c in calls] == [[seed(gas[0], 0), seed(gas[1], 0)], [seed(gas[0], 1), seed(gas[1], 1)],
+                                     [seed(gas[1], 2)], [seed(gas[2], 0)], [seed(gas[2], 1)]]
+    assert len({serve.model_seed(s.name, 0) for s in gas}) == len(gas)
     assert all(m.closed for m in _FakeModel.made)
     assert rep["peak_resident_models"] == 2
     assert rep["mode"].startswith("lockstep")
