@@ -122,24 +122,48 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(neb, seconds_target=15.0, threads=None):
-    """FP32 oracle on the host cores over a bounded packet sample."""
-    from oracle import runner
-    threads = threads or os.cpu_count() or 1
-    n = 20000
-    t0 = time.perf_counter()
-    _, _, _, st = runner.run(neb, n_packets=n, precision="fp32", seed=1, threads=threads)
-    dt = time.perf_counter() - t0
-    rate = st["crossings"] / dt
-    # grow the sample to ~seconds_target of CPU work
-    n2 = int(min(max(n * seconds_target / max(dt, 1e-3), n), 2_000_000))
-    t0 = time.perf_counter()
-    _, _, _, st = runner.run(neb, n_packets=n2, precision="fp32", seed=2, threads=threads)
-    dt = time.perf_counter() - t0
-    rate = st["crossings"] / dt
-    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d packets of the %d-packet step (%d crossings, %.1f s, FP32 march, FP64 sums)"
-                      % (n2, sum(neb.n_packets), st["crossings"], dt)}
+def workload_config(neb):
+    """The workload of one step, the same in both arms' JSON lines."""
+    l2 = "inputs larger than L2 (opacity %d MB, Jste %d MB)" % (neb.opacity.nbytes // 2**20,
+                                                                  2 * neb.opacity.nbytes // 2**20)
+    return {"workload": neb.spec.name, "grid": "%d^3" % neb.nx, "cells": neb.ncells, "nbins": neb.nbins,
+            "stars": len(neb.n_packets), "packets_per_step": int(sum(neb.n_packets)), "l2": l2}
+
+
+class OracleStep:
+    """One transport iteration of the FP32 oracle (the C++ restatement of the
+    reference's Fortran path) on the host cores: all packets of every star
+    (or n_packets per star), estimators zeroed inside the step as iterateMC
+    zeroes them; the grid marshalling and the estimator allocation are made
+    once, outside."""
+
+    def __init__(self, neb, n_packets=None, threads=None):
+        from mocassin_gb300 import abi
+        self.neb = neb
+        self.n = n_packets
+        self.threads = threads or os.cpu_count() or 1
+        self.m = abi.Marshalled(neb, n_packets=n_packets)
+        self.out = abi.estimator_arrays(neb)
+        for a in self.out:
+            a.fill(1.0)  # touch the pages once
+
+    def __call__(self, seed):
+        from oracle import runner
+        t0 = time.perf_counter()
+        st = runner.run(self.neb, n_packets=self.n, precision="fp32", seed=seed, threads=self.threads, out=self.out,
+                        marshalled=self.m)[3]
+        return time.perf_counter() - t0, st["crossings"]
+
+
+def cpu_baseline(neb, threads=None):
+    """FP32 oracle on the host cores: one full step after one warm-up step
+    (about 10 s of CPU work on the 61^3 workload)."""
+    step = OracleStep(neb, threads=threads)
+    step(1)
+    dt, cross = step(2)
+    return {"value": cross / dt, "unit": UNIT, "cores": step.threads, "kind": "port",
+            "sample": "the full %d-packet step after one warm-up step (%d crossings, %.1f s, FP32 march, FP64 sums; "
+                      "estimators zeroed inside, allocated outside)" % (sum(neb.n_packets), cross, dt)}
 
 
 def dist_env():
@@ -150,33 +174,41 @@ def dist_env():
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU path for this transport, the
+    FP32 oracle (the Fortran cannot be built on either machine), on all host
+    cores, over the same step as the GPU arm: every packet of the workload's
+    transport iteration per timed step.  Warm-up steps are bounded samples
+    (--ref-packets) of the same workload."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from oracle import runner
     from mocassin_gb300 import nebula
-    neb = nebula.build(workload(args.config))
-    threads = os.cpu_count() or 1
-    n = args.ref_packets
+    spec = workload(args.config)
+    if args.packets:
+        for st in spec.stars:
+            st.n_packets = int(args.packets // len(spec.stars))
+    neb = nebula.build(spec)
+    warm = OracleStep(neb, n_packets=args.ref_packets)
     for w in range(args.warmup):
-        runner.run(neb, n_packets=max(n // 10, 1000), precision="fp32", seed=100 + w, threads=threads)
+        warm(100 + w)
+    del warm
+    step = OracleStep(neb)
     cross, total = 0, 0.0
     for k in range(args.steps):
-        t0 = time.perf_counter()
-        _, _, _, st = runner.run(neb, n_packets=n, precision="fp32", seed=1 + k, threads=threads)
-        total += time.perf_counter() - t0
-        cross += st["crossings"]
+        dt, c = step(1 + k)
+        total += dt
+        cross += c
     value = cross / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": neb.spec.name, "cells": neb.ncells, "nbins": neb.nbins,
-                       "packets_per_step": n, "packets_per_iteration": sum(neb.n_packets),
-                       "note": "each step is a bounded packet sample of the iteration"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d packets per step x %d steps, FP32 oracle (C++ restatement of "
+            "config": workload_config(neb),
+            "impl_detail": {"crossings_per_step": cross / args.steps, "threads": step.threads,
+                            "warmup_packets": args.ref_packets},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": step.threads, "kind": "port",
+                             "sample": "the full %d-packet step x %d steps, FP32 oracle (C++ restatement of "
                                        "photon_mod.f90; the Fortran reference has no compiler here)"
-                                       % (n, args.steps)},
+                                       % (sum(neb.n_packets), args.steps)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -519,12 +551,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": float(step_ms.mean()), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision.replace("fp", "f"),
             "data": "synthetic",
-            "config": {"workload": neb.spec.name, "grid": "%d^3" % neb.nx, "cells": neb.ncells, "nbins": neb.nbins,
-                       "packets_per_step": npk, "crossings_per_step": per_launch_cross,
-                       "march": args.precision, "estimators": "f64", "form": args.form,
-                       "l2": "inputs larger than L2 (opacity %.0f MB, Jste %.0f MB)"
-                             % (neb.opacity.nbytes / 1e6, neb.opacity.size * 8 / 1e6),
-                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "config": workload_config(neb),
+            "impl_detail": {"crossings_per_step": per_launch_cross, "march": args.precision, "estimators": "f64",
+                            "form": args.form, "parallelism": "replicas" if ws > 1 else "1 GPU"},
             # per step and round: sample, scan, scatter, emit, march (+ the round control in the graph
             # form), or one kernel (plain)
             "roofline": roof, "e2e": e2e,

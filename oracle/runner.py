@@ -33,14 +33,25 @@ def library():
 
 
 def run(neb, n_packets=None, seed=1, iteration=1, precision="fp64", replay=None, threads=0, acc32=False,
-        recursion_limit=0, safe_limit=0):
-    """Oracle transport of all stars of ``neb``; returns (jste, jdif, escaped, stats)."""
+        recursion_limit=0, safe_limit=0, out=None, marshalled=None):
+    """Oracle transport of all stars of ``neb``; returns (jste, jdif, escaped, stats).
+
+    out: (jste, jdif, escaped) arrays of abi.estimator_arrays(neb) to zero
+    and fill instead of new ones; marshalled: an abi.Marshalled(neb,
+    n_packets) to reuse (a timing loop keeps both out of its timed region)."""
     lib = library()
-    m = abi.Marshalled(neb, n_packets=n_packets)
+    m = marshalled if marshalled is not None else abi.Marshalled(neb, n_packets=n_packets)
     prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
     opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
                          recursion_limit=recursion_limit, safe_limit=safe_limit)
-    js, jd, es = abi.estimator_arrays(neb)
+    if out is None:
+        js, jd, es = abi.estimator_arrays(neb)
+    else:
+        js, jd, es = out
+        js.fill(0.0)
+        es.fill(0.0)
+        if neb.flags & (1 << 4):  # MC_FLAG_DEBUG: Jdif is written only in debug mode
+            jd.fill(0.0)
     st = abi.McStats()
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     rc = lib.oracle_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), dp(js), dp(jd), dp(es),
