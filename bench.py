@@ -348,7 +348,7 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="override the grid size n (odd for full grids)")
     ap.add_argument("--ref-packets", type=int, default=200000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--form", default="graph", choices=["graph", "wave", "plain"],
                     help="graph: the chosen form with its rounds in one CUDA graph; wave: the same with host-driven "
                          "rounds; plain: one thread per history")
@@ -511,14 +511,18 @@ def main():
     # the grid's own 4-byte estimator arrays (mc_transport_run_f32): FP64 sums on the device, rounded once
     js = torch.zeros((neb.nbins, neb.ncells + 1), dtype=torch.float32).pin_memory()
     es = torch.zeros((neb.nbins + 1, neb.ncells + 1), dtype=torch.float32).pin_memory()
-    d2h = (js.numel() + es.numel()) * 4
-    # the estimators start each iteration at zero (MC_RUN_ZERO_FIRST: not uploaded)
-    e2e_t, e2e_c = 0.0, 0
+    # the estimators start each iteration at zero: the Fortran driver zeroes
+    # Jste and escapedPackets before every iteration (iteration_mod.f90:458-472),
+    # here between calls, outside the timed region; MC_RUN_HOST_ZEROED then
+    # brings back only the entries the transport made nonzero
+    e2e_t, e2e_c, h2d, d2h = 0.0, 0, 0, 0
     for k in range(args.e2e_steps + 1):
+        js.zero_()
+        es.zero_()
         opts = abi.make_opts(seed=77 + k, iteration=1, precision=abi.MC_PREC_FP32 if args.precision == "fp32"
                              else abi.MC_PREC_FP64,
                              run_flags={"plain": abi.MC_RUN_FORM_PLAIN, "graph": abi.MC_RUN_GRAPH}.get(args.form, 0)
-                             | abi.MC_RUN_ZERO_FIRST)
+                             | abi.MC_RUN_HOST_ZEROED)
         st = abi.McStats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -531,11 +535,18 @@ def main():
         if k > 0:  # first call is a warm-up
             e2e_t += dt
             e2e_c += st.crossings
-    e2e = {"value": e2e_c / e2e_t if e2e_t > 0 else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-           "call": "mc_transport_run_f32 (host pinned buffers: grid upload, CDF re-layout, transport, estimator "
-                   "download into the grid's own FP32 Jste and escapedPackets, FP64 sums rounded once on the device; "
-                   "the estimators start at zero (MC_RUN_ZERO_FIRST); device buffers kept between calls of the same "
-                   "grid shape)"}
+            h2d += st.h2d_bytes
+            d2h += st.d2h_bytes
+    ne2e = max(args.e2e_steps, 1)
+    e2e = {"value": e2e_c / e2e_t if e2e_t > 0 else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d // ne2e),
+           "d2h_bytes_per_step": int(d2h // ne2e),
+           "call": "mc_transport_run_f32 with MC_RUN_HOST_ZEROED (host pinned buffers: grid upload (the opacity "
+                   "rows a packet can march in, recPDF re-laid out on a side stream during round 0), transport, "
+                   "download into the grid's own FP32 Jste of the frequency rows that received a deposit and "
+                   "scatter of the nonzero escapedPackets entries, FP64 sums rounded once on the device; the "
+                   "caller's estimators zeroed between calls outside the timed region, as the Fortran driver "
+                   "zeroes them before each iteration; device buffers kept between calls of the same grid "
+                   "shape); bytes are those the call reports having copied"}
 
     peak, peak_kind = measured_peak()
     # dominant kernel: the march (its own CUDA events on the library stream)

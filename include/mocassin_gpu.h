@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define MC_ABI_VERSION 1
+#define MC_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 typedef enum mc_status {
@@ -83,6 +83,19 @@ typedef enum mc_status {
 #define MC_RUN_GRAPH 4      /* the chosen form's rounds inside one CUDA graph (a
                                WHILE node on the device's absorbed count): no
                                host round trip per round; march_ms is then 0 */
+#define MC_RUN_HOST_ZEROED 8 /* mc_transport_run / _f32 only: the caller's host
+                               estimators hold zeros on entry, as the Fortran
+                               driver zeroes Jste and escapedPackets before each
+                               iteration (iteration_mod.f90:458-472).  Implies
+                               MC_RUN_ZERO_FIRST; the call then writes only the
+                               entries the transport made nonzero: the Jste /
+                               Jdif rows (frequency bins) that received a
+                               deposit, and the escapedPackets entries that
+                               received an escape (compacted on the device;
+                               scattered by the device straight into pinned
+                               host arrays, by the host into pageable ones).
+                               Entries it does not write keep the caller's
+                               zeros.                                          */
 
 /* Read-only description of one (mother) grid for one iteration.  All
  * pointers are HOST pointers owned by the caller; they are read during the
@@ -160,6 +173,10 @@ typedef struct mc_stats {
   int32_t error_packet;    /* packet index of that error, -1 if none          */
   double march_ms;         /* device time of the march kernel(s) alone        */
   int64_t rounds;          /* march rounds (re-emission generations) run      */
+  int64_t h2d_bytes;       /* mc_transport_run / _f32: host-to-device bytes the
+                              call copied (grid arrays, sources, estimators);
+                              0 for the other entry points                    */
+  int64_t d2h_bytes;       /* the same for device-to-host (estimators)         */
 } mc_stats_t;
 
 /* ---- library ----------------------------------------------------------- */

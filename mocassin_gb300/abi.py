@@ -17,6 +17,7 @@ MC_RNG_REPLAY = 1
 MC_RUN_ZERO_FIRST = 1
 MC_RUN_FORM_PLAIN = 2
 MC_RUN_GRAPH = 4
+MC_RUN_HOST_ZEROED = 8
 
 STATUS_NAMES = {0: "MC_OK", 1: "MC_ERR_ARG", 2: "MC_ERR_CUDA", 3: "MC_ERR_BOUNDS", 4: "MC_ERR_NAN",
                 5: "MC_ERR_REPLAY", 6: "MC_ERR_TIMEOUT", 7: "MC_ERR_UNSUPPORTED", 8: "MC_ERR_NOMEM",
@@ -54,7 +55,8 @@ class McStats(C.Structure):
                 ("escaped", C.c_int64), ("lines", C.c_int64), ("trapped", C.c_int64),
                 ("silent_exits", C.c_int64), ("safe_limit_hits", C.c_int64), ("qphot", C.c_double),
                 ("kernel_ms", C.c_double), ("error_code", C.c_int32), ("error_packet", C.c_int32),
-                ("march_ms", C.c_double), ("rounds", C.c_int64)]
+                ("march_ms", C.c_double), ("rounds", C.c_int64), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

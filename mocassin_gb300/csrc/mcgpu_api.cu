@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -123,6 +124,15 @@ struct mc_ctx {
   DBuf dx32, dy32, dz32, dx64, dy64, dz64;
   DBuf jste, jdif, esc;
   DBuf stage_j, stage_d, stage_e;  // FP32 staging of the drop-in call's estimators
+  // MC_RUN_HOST_ZEROED downloads: per-bin nonzero flags of Jste / Jdif, the
+  // compacted escapedPackets entries (indices, values) and their count
+  DBuf z_mask, z_idx, z_val, z_cnt;
+  // bytes the drop-in call copied host -> device / device -> host
+  long long xfer_h2d = 0, xfer_d2h = 0;
+  // the drop-in call's last geometry (axes, active, frequencies): a call with
+  // the same geometry skips its re-upload and the march-order rebuild
+  std::vector<float> geo_f;
+  std::vector<int32_t> geo_a;
   // the drop-in call uploads and re-lays out recPDF on a side stream while
   // round 0 (stellar packets only) runs; round 1 waits for ev_cdf
   cudaStream_t side = nullptr;
@@ -270,12 +280,17 @@ mc_status view_table(const mc_grid_t *g, mcg::DevGrid &d, std::vector<uint8_t> &
   return MC_OK;
 }
 
-mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t cdf_stream = nullptr) {
+// opac_row0 > 0: the opacity rows (frequency bins) below it are not copied:
+// the caller guarantees no packet marches there (the non-ionising bins of a
+// gas-only grid escape before any march).
+mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t cdf_stream = nullptr,
+                        int opac_row0 = 0) {
   const int nc1 = g->ncells + 1, nb = g->nbins;
   const size_t plane = (size_t)nc1 * nb * sizeof(float);
   cudaStream_t s = c->stream;
   mc_status st;
   auto put = [&](DBuf &b, const void *h, size_t bytes) -> mc_status {
+    if (h) c->xfer_h2d += (long long)bytes;
     if (first || !b.p) return upload(b, h, bytes, s);
     if (h) {
       cudaError_t e = cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, s);
@@ -283,7 +298,15 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t 
     }
     return MC_OK;
   };
-  if ((st = put(c->opacity, g->opacity, plane))) return st;
+  if (!first && c->opacity.p && opac_row0 > 0 && opac_row0 < nb) {
+    const size_t off = (size_t)opac_row0 * nc1 * sizeof(float);
+    c->xfer_h2d += (long long)(plane - off);
+    cudaError_t e = cudaMemcpyAsync((char *)c->opacity.p + off, (const char *)g->opacity + off, plane - off,
+                                    cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
+  } else if ((st = put(c->opacity, g->opacity, plane))) {
+    return st;
+  }
   if (g->sca_opac && (st = put(c->sca, g->sca_opac, plane))) return st;
   if (!c->identity) {
     const size_t mplane = (size_t)c->ncell3 * nb * sizeof(float);
@@ -300,6 +323,7 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t 
   if (g->g_sca && (st = put(c->gsca, g->g_sca, (size_t)nb * sizeof(float)))) return st;
   if (g->rec_pdf) {
     const cudaStream_t cs = cdf_stream ? cdf_stream : s;
+    c->xfer_h2d += (long long)plane;
     if (first || !c->rec_raw.p) {
       if ((st = upload(c->rec_raw, g->rec_pdf, plane, cs))) return st;
     } else {
@@ -496,6 +520,29 @@ namespace {
 // frequencies, cell widths, march order).  Returns MC_ERR_ARG when the
 // active map changes which cells are active in a way that changes the march
 // layout (the caller then builds a new context).
+// true when g's axes, active map and frequencies equal the ones the last
+// drop-in call left in the context (and records them otherwise)
+bool same_geometry(mc_ctx *c, const mc_grid_t *g) {
+  const size_t nf = (size_t)g->nx + g->ny + g->nz + g->nbins;
+  const size_t n3 = (size_t)g->nx * g->ny * g->nz;
+  bool same = c->geo_f.size() == nf && c->geo_a.size() == n3;
+  const float *parts[4] = {g->x_axis, g->y_axis, g->z_axis, g->nu_array};
+  const size_t lens[4] = {(size_t)g->nx, (size_t)g->ny, (size_t)g->nz, (size_t)g->nbins};
+  if (same) {
+    size_t o = 0;
+    for (int k = 0; k < 4 && same; o += lens[k], ++k)
+      same = memcmp(c->geo_f.data() + o, parts[k], lens[k] * sizeof(float)) == 0;
+    same = same && memcmp(c->geo_a.data(), g->active, n3 * sizeof(int32_t)) == 0;
+  }
+  if (!same) {
+    c->geo_f.resize(nf);
+    size_t o = 0;
+    for (int k = 0; k < 4; o += lens[k], ++k) memcpy(c->geo_f.data() + o, parts[k], lens[k] * sizeof(float));
+    c->geo_a.assign(g->active, g->active + n3);
+  }
+  return same;
+}
+
 mc_status refresh_geometry(mc_ctx *c, const mc_grid_t *g) {
   const bool sym = g->flags & MC_FLAG_SYMMETRIC_XYZ;
   const size_t n3 = (size_t)g->nx * g->ny * g->nz;
@@ -517,6 +564,8 @@ mc_status refresh_geometry(mc_ctx *c, const mc_grid_t *g) {
   MC_CUDA(cudaMemcpyAsync(c->active.p, g->active, n3 * sizeof(int32_t), cudaMemcpyHostToDevice, s));
   MC_CUDA(cudaMemcpyAsync(c->nu.p, g->nu_array, g->nbins * sizeof(float), cudaMemcpyHostToDevice, s));
   MC_CUDA(cudaMemcpyAsync(c->lin2cell.p, l2c.data(), n3 * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  c->xfer_h2d += (long long)((g->nx + g->ny + g->nz) * (sizeof(float) * 2 + sizeof(double)) + 2 * n3 * sizeof(int32_t) +
+                             g->nbins * sizeof(float));
   std::vector<float> w32[3];
   std::vector<double> w64[3];
   const float *ax[3] = {g->x_axis, g->y_axis, g->z_axis};
@@ -885,6 +934,8 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
     stats->error_packet = h.error_packet;
     stats->march_ms = mms;
     stats->rounds = plain ? 1 : c->rounds;
+    stats->h2d_bytes = 0;
+    stats->d2h_bytes = 0;
   }
   if (h.error_code != 0)
     return set_error((mc_status)h.error_code, "device error %d in packet %d", h.error_code, h.error_packet);
@@ -1070,6 +1121,8 @@ mc_status mc_batch_run(mc_ctx_t *const *ctxs, int32_t n, const mc_source_t *cons
       t.error_packet = m.h.error_packet;
       t.march_ms = march_ms;
       t.rounds = m.rounds;
+      t.h2d_bytes = 0;
+      t.d2h_bytes = 0;
     }
     if (m.h.error_code != 0 && first == MC_OK)
       first = set_error((mc_status)m.h.error_code, "model %d: device error %d in packet %d", (int)i, m.h.error_code,
@@ -2412,6 +2465,160 @@ __global__ void narrow_kernel(const double *__restrict__ in, float *__restrict__
     out[i] = (float)in[i];
 }
 
+// The first frequency bin a packet can march in: on a gas-only grid the
+// packets below ionEdge(1) escape before any march (energyPacketRun,
+// photon_mod.f90:370-465), so their opacity rows are never read.
+int first_marched_bin(const mc_grid_t *g) {
+  if (g->flags & MC_FLAG_DUST) return 0;
+  int b = 0;
+  while (b < g->nbins && g->nu_array[b] < g->ion_edge1) ++b;
+  return b;
+}
+
+// flag[row] = 1 when row `row` of a [rows][len] array holds a nonzero value
+// (grid: x tiles the row, y = row; flag zeroed before)
+__global__ void row_nonzero_kernel(const double *__restrict__ a, long long len, unsigned char *flag) {
+  const double *r = a + (long long)blockIdx.y * len;
+  bool nz = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    nz |= r[i] != 0.0;
+  if (__syncthreads_or(nz) && threadIdx.x == 0) flag[blockIdx.y] = 1;
+}
+
+// the nonzero entries of a[0..n) as (index, value) pairs, in no set order,
+// values as float (f32) or double: *count ends at their number; pairs beyond
+// `cap` are not written
+__global__ void compact_nonzero_kernel(const double *__restrict__ a, unsigned long long n, uint32_t *idx, void *val,
+                                       int f32, unsigned long long cap, unsigned long long *count) {
+  const unsigned int lane = threadIdx.x & 31;
+  for (unsigned long long b = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull; b < n;
+       b += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long i = b + lane;
+    const double v = i < n ? a[i] : 0.0;
+    const unsigned int m = __ballot_sync(0xffffffffu, v != 0.0);
+    if (!m) continue;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (v != 0.0) {
+      const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+      if (slot < cap) {
+        idx[slot] = (uint32_t)i;
+        if (f32) ((float *)val)[slot] = (float)v;
+        else ((double *)val)[slot] = v;
+      }
+    }
+  }
+}
+
+// out[idx[k]] = val[k] for k < n, floats (f32) or doubles (out: a
+// device-visible view of the caller's pinned host array)
+__global__ void scatter_pairs_kernel(const uint32_t *__restrict__ idx, const void *val, unsigned long long n, int f32,
+                                     void *out) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    if (f32) ((float *)out)[idx[k]] = ((const float *)val)[k];
+    else ((double *)out)[idx[k]] = ((const double *)val)[k];
+  }
+}
+
+// Device view of a pinned (page-locked, mapped) host pointer, or nullptr
+// for pageable memory.
+void *pinned_view(void *h) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// MC_RUN_HOST_ZEROED download of one estimator [rows][len] (FP64 on the
+// device; FP32 staged values when stage is given): the rows that hold a
+// nonzero value, in one copy per run of such rows.
+mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, long long rows, long long len) {
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if (c->z_mask.bytes != (size_t)rows && (st = put_buf(c->z_mask, nullptr, (size_t)rows, s))) return st;
+  MC_CUDA(cudaMemsetAsync(c->z_mask.p, 0, (size_t)rows, s));
+  const unsigned int tiles = (unsigned int)std::max(1ll, std::min(64ll, len / 4096));
+  row_nonzero_kernel<<<dim3(tiles, (unsigned int)rows), 256, 0, s>>>(d.as<double>(), len, c->z_mask.as<unsigned char>());
+  MC_CUDA(cudaGetLastError());
+  std::vector<unsigned char> mask((size_t)rows);
+  MC_CUDA(cudaMemcpyAsync(mask.data(), c->z_mask.p, (size_t)rows, cudaMemcpyDeviceToHost, s));
+  c->xfer_d2h += rows;
+  MC_CUDA(cudaStreamSynchronize(s));
+  const size_t elt = stage ? sizeof(float) : sizeof(double);
+  const char *src = stage ? (const char *)stage->p : (const char *)d.p;
+  for (long long r = 0; r < rows;) {
+    if (!mask[r]) { ++r; continue; }
+    long long e = r;
+    while (e < rows && mask[e]) ++e;
+    MC_CUDA(cudaMemcpyAsync((char *)h + r * len * elt, src + r * len * elt, (size_t)((e - r) * len) * elt,
+                            cudaMemcpyDeviceToHost, s));
+    c->xfer_d2h += (long long)((e - r) * len) * (long long)elt;
+    r = e;
+  }
+  return MC_OK;
+}
+
+// MC_RUN_HOST_ZEROED download of escapedPackets: its nonzero entries,
+// compacted on the device and scattered into the caller's array (by the
+// device into pinned memory, by the host otherwise); a dense copy when they
+// are too many for the pair buffers.
+mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32) {
+  cudaStream_t s = c->stream;
+  mc_status st;
+  const unsigned long long n = d.bytes / sizeof(double);
+  const unsigned long long cap = std::min<unsigned long long>(n, 1ull << 24);
+  if (c->z_idx.bytes < cap * sizeof(uint32_t) && (st = put_buf(c->z_idx, nullptr, cap * sizeof(uint32_t), s))) return st;
+  if (c->z_val.bytes < cap * sizeof(double) && (st = put_buf(c->z_val, nullptr, cap * sizeof(double), s))) return st;
+  if (!c->z_cnt.p && (st = put_buf(c->z_cnt, nullptr, sizeof(unsigned long long), s))) return st;
+  MC_CUDA(cudaMemsetAsync(c->z_cnt.p, 0, sizeof(unsigned long long), s));
+  compact_nonzero_kernel<<<c->num_sms * 8, 256, 0, s>>>(d.as<double>(), n, c->z_idx.as<uint32_t>(), c->z_val.p,
+                                                         f32 ? 1 : 0, cap, c->z_cnt.as<unsigned long long>());
+  MC_CUDA(cudaGetLastError());
+  unsigned long long cnt = 0;
+  MC_CUDA(cudaMemcpyAsync(&cnt, c->z_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  const size_t elt = f32 ? sizeof(float) : sizeof(double);
+  c->xfer_d2h += (long long)sizeof cnt;
+  if (cnt > cap) {
+    if (!f32) {
+      MC_CUDA(cudaMemcpyAsync(h, d.p, d.bytes, cudaMemcpyDeviceToHost, s));
+    } else {
+      narrow_kernel<<<c->num_sms * 8, 256, 0, s>>>(d.as<double>(), c->stage_e.as<float>(), (size_t)n);
+      MC_CUDA(cudaGetLastError());
+      MC_CUDA(cudaMemcpyAsync(h, c->stage_e.p, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    }
+    c->xfer_d2h += (long long)(n * elt);
+    return MC_OK;
+  }
+  if (cnt == 0) return MC_OK;
+  // the pairs cross to the host either way: written there by the device, or
+  // copied and scattered by the host
+  c->xfer_d2h += (long long)(cnt * (sizeof(uint32_t) + elt));
+  if (void *hv = pinned_view(h)) {
+    const unsigned int blocks = (unsigned int)std::min<unsigned long long>((unsigned long long)c->num_sms * 4,
+                                                                           (cnt + 255) / 256);
+    scatter_pairs_kernel<<<blocks, 256, 0, s>>>(c->z_idx.as<uint32_t>(), c->z_val.p, cnt, f32 ? 1 : 0, hv);
+    MC_CUDA(cudaGetLastError());
+    return MC_OK;
+  }
+  std::vector<uint32_t> ix(cnt);
+  std::vector<char> vl(cnt * elt);
+  MC_CUDA(cudaMemcpyAsync(ix.data(), c->z_idx.p, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaMemcpyAsync(vl.data(), c->z_val.p, cnt * elt, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  if (f32) {
+    float *out = (float *)h;
+    const float *v = (const float *)vl.data();
+    for (unsigned long long k = 0; k < cnt; ++k) out[ix[k]] = v[k];
+  } else {
+    double *out = (double *)h;
+    const double *v = (const double *)vl.data();
+    for (unsigned long long k = 0; k < cnt; ++k) out[ix[k]] = v[k];
+  }
+  return MC_OK;
+}
+
 // the drop-in call with FP64 (f32 = false) or FP32 host estimators
 mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc, const mc_run_opts_t *o,
                              void *jste, void *jdif, void *escaped, bool f32, mc_stats_t *stats) {
@@ -2435,7 +2642,15 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     // recPDF on the side stream, after whatever the context's stream still runs
     MC_CUDA(cudaEventRecord(c->ev_side0, c->stream));
     MC_CUDA(cudaStreamWaitEvent(c->side, c->ev_side0, 0));
-    if (refresh_geometry(c, g) != MC_OK || upload_arrays(c, g, false, c->side) != MC_OK) {
+    bool geo_ok = true;
+    if (same_geometry(c, g)) {
+      c->g.gc[0] = g->geo_corr[0]; c->g.gc[1] = g->geo_corr[1]; c->g.gc[2] = g->geo_corr[2];
+      c->g.rout = g->r_out;
+      c->g.ion_edge1 = g->ion_edge1;
+    } else {
+      geo_ok = refresh_geometry(c, g) == MC_OK;
+    }
+    if (!geo_ok || upload_arrays(c, g, false, c->side, first_marched_bin(g)) != MC_OK) {
       cudaStreamSynchronize(c->side);
       reuse = false;
     } else {
@@ -2448,7 +2663,18 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     g_cached = nullptr;
     if ((st = mc_ctx_create(g, &c))) return st;
     g_cached = c;
+    same_geometry(c, g);  // records it
+    // a new context uploads the whole grid
+    const size_t plane = (size_t)(g->ncells + 1) * g->nbins * sizeof(float);
+    const size_t n3 = (size_t)g->nx * g->ny * g->nz;
+    c->xfer_h2d = (long long)(plane * (1 + (g->sca_opac ? 1 : 0) + (g->rec_pdf ? 1 : 0) + (g->dust_pdf ? 1 : 0)) +
+                              (g->nx + g->ny + g->nz) * (sizeof(float) * 2 + sizeof(double)) +
+                              2 * n3 * sizeof(int32_t) + g->nbins * sizeof(float) +
+                              (g->total_lines ? (size_t)(g->ncells + 1) * sizeof(float) : 0));
   }
+  long long h2d = c->xfer_h2d, d2h = 0;
+  c->xfer_h2d = 0;
+  for (int i = 0; i < nsrc; ++i) h2d += (long long)g->nbins * (long long)sizeof(float);  // the stars' CDFs
   // the estimators accumulate into the caller's arrays: their current
   // values go to the device first, the kernels add to them, and the sums
   // come back (no host-side pass over the arrays).  With MC_RUN_ZERO_FIRST
@@ -2456,7 +2682,8 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
   // them before each iteration, iteration_mod.f90:458-472): the device
   // copies are cleared instead of uploaded.  FP32 arrays go through a staging
   // buffer per array and a widening / narrowing pass on the device.
-  const bool zero = o->run_flags & MC_RUN_ZERO_FIRST;
+  const bool hostz = o->run_flags & MC_RUN_HOST_ZEROED;
+  const bool zero = (o->run_flags & MC_RUN_ZERO_FIRST) || hostz;
   cudaStream_t s = c->stream;
   struct Item { void *h; DBuf *d; DBuf *stage; } items[3] = {
       {jste, &c->jste, &c->stage_j}, {jdif, &c->jdif, &c->stage_d}, {escaped, &c->esc, &c->stage_e}};
@@ -2468,17 +2695,47 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
       MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, s));
     } else if (!f32) {
       MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, s));
+      h2d += (long long)it.d->bytes;
     } else {
       MC_CUDA(cudaMemcpyAsync(it.stage->p, it.h, n * sizeof(float), cudaMemcpyHostToDevice, s));
+      h2d += (long long)(n * sizeof(float));
       widen_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.stage->as<float>(), it.d->as<double>(), n);
       MC_CUDA(cudaGetLastError());
     }
   }
   mc_run_opts_t o2 = *o;
-  o2.run_flags &= ~MC_RUN_ZERO_FIRST;
+  o2.run_flags &= ~(MC_RUN_ZERO_FIRST | MC_RUN_HOST_ZEROED);
   st = mc_ctx_run(c, src, nsrc, &o2, stats);
   if (st != MC_OK) return st;
-  if (!f32) return mc_ctx_download(c, (double *)jste, (double *)jdif, (double *)escaped, 0);
+  c->xfer_d2h = 0;
+  auto counted = [&](mc_status r) {
+    if (stats) { stats->h2d_bytes = h2d; stats->d2h_bytes = c->xfer_d2h + d2h; }
+    return r;
+  };
+  if (hostz) {
+    // only what the transport made nonzero goes back
+    const long long len = c->nc + 1;
+    for (int k = 0; k < 2; ++k) {
+      Item &it = items[k];
+      if (!it.h || !it.d->p) continue;
+      const long long n = (long long)(it.d->bytes / sizeof(double));
+      if (f32) {
+        narrow_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.d->as<double>(), it.stage->as<float>(), (size_t)n);
+        MC_CUDA(cudaGetLastError());
+      }
+      if ((st = download_rows(c, *it.d, f32 ? it.stage : nullptr, it.h, n / len, len))) return st;
+    }
+    if (escaped && c->esc.p) {
+      if ((st = download_sparse(c, c->esc, escaped, f32))) return st;
+    }
+    MC_CUDA(cudaStreamSynchronize(s));
+    return counted(MC_OK);
+  }
+  if (!f32) {
+    for (auto &it : items)
+      if (it.h && it.d->p) d2h += (long long)it.d->bytes;
+    return counted(mc_ctx_download(c, (double *)jste, (double *)jdif, (double *)escaped, 0));
+  }
   // narrow each array and start its copy back; the next array's narrowing
   // overlaps the previous copy
   for (auto &it : items) {
@@ -2487,9 +2744,10 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     narrow_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.d->as<double>(), it.stage->as<float>(), n);
     MC_CUDA(cudaGetLastError());
     MC_CUDA(cudaMemcpyAsync(it.h, it.stage->p, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    d2h += (long long)(n * sizeof(float));
   }
   MC_CUDA(cudaStreamSynchronize(s));
-  return MC_OK;
+  return counted(MC_OK);
 }
 
 }  // namespace

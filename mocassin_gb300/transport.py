@@ -121,7 +121,7 @@ def library():
         lib.mc_opacity_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, fp, fp, fp, C.c_int32, fp, dp]
         lib.mc_ctx_build_opacity.restype = C.c_int
         lib.mc_ctx_build_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp, fp, C.c_int32, C.c_int32, dp]
-        if lib.mc_abi_version() != 1:
+        if lib.mc_abi_version() != 2:
             raise TransportError(1, "ABI version mismatch")
         _LIB = lib
     return _LIB
@@ -150,18 +150,18 @@ def _check_shapes(neb, jste, jdif, escaped):
             raise ValueError("%s must be a C-contiguous %s array of shape %s" % (name, dt, shape))
 
 
-def _flags(form, zero_first=False):
+def _flags(form, zero_first=False, host_zeroed=False):
     """form: "wave" (rounds driven by the host), "graph" (the same rounds
     inside one CUDA graph) or "plain" (one thread per history)."""
     if form not in ("wave", "plain", "graph"):
         raise ValueError("form must be 'wave', 'graph' or 'plain'")
     f = {"wave": 0, "graph": abi.MC_RUN_GRAPH, "plain": abi.MC_RUN_FORM_PLAIN}[form]
-    return f | (abi.MC_RUN_ZERO_FIRST if zero_first else 0)
+    return f | (abi.MC_RUN_ZERO_FIRST if zero_first else 0) | (abi.MC_RUN_HOST_ZEROED if host_zeroed else 0)
 
 
 def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp32", replay=None,
                          jste=None, jdif=None, escaped=None, recursion_limit=0, safe_limit=0, form="wave",
-                         zero_first=False):
+                         zero_first=False, host_zeroed=False):
     """Runs every packet of every star of ``neb`` through the GPU transport.
 
     Accumulates into ``jste`` / ``jdif`` / ``escaped`` (created zeroed when not
@@ -171,13 +171,16 @@ def energy_packet_driver(neb, n_packets=None, seed=1, iteration=1, precision="fp
     ("wave", the default; "graph" with its rounds in one CUDA graph) or one
     thread per history ("plain").  zero_first: the arrays are overwritten
     with this transport's sums instead of accumulated into (they are not
-    uploaded).
+    uploaded).  host_zeroed: the arrays hold zeros on entry and only the
+    entries this transport made nonzero are written (MC_RUN_HOST_ZEROED);
+    stats then report the bytes the call copied (h2d_bytes, d2h_bytes).
     """
     lib = library()
     m = abi.Marshalled(neb, n_packets=n_packets)
     prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
     opts = abi.make_opts(seed=seed, iteration=iteration, precision=prec, replay=replay,
-                         recursion_limit=recursion_limit, safe_limit=safe_limit, run_flags=_flags(form, zero_first))
+                         recursion_limit=recursion_limit, safe_limit=safe_limit,
+                         run_flags=_flags(form, zero_first, host_zeroed))
     js0, jd0, es0 = abi.estimator_arrays(neb)
     jste = js0 if jste is None else jste
     escaped = es0 if escaped is None else escaped

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     missing = [f for f in declared_functions() if not hasattr(lib, f)]
     assert not missing, missing
     lib.mc_abi_version.restype = C.c_int
-    assert lib.mc_abi_version() == 1
+    assert lib.mc_abi_version() == 2
 
 
 def test_struct_layout_matches_ctypes():
@@ -46,7 +46,8 @@ int main(void) {
   printf("%zu %zu %zu %zu\n", sizeof(mc_grid_t), sizeof(mc_source_t), sizeof(mc_run_opts_t), sizeof(mc_stats_t));
   printf("%zu %zu %zu %zu\n", offsetof(mc_grid_t, geo_corr), offsetof(mc_grid_t, flags),
          offsetof(mc_source_t, spec_cdf), offsetof(mc_run_opts_t, replay_stride));
-  printf("%zu %zu\n", offsetof(mc_stats_t, qphot), offsetof(mc_stats_t, error_packet));
+  printf("%zu %zu %zu\n", offsetof(mc_stats_t, qphot), offsetof(mc_stats_t, error_packet),
+         offsetof(mc_stats_t, d2h_bytes));
   return 0;
 }
 '''
@@ -62,6 +63,7 @@ int main(void) {
     assert vals[4] == abi.McGrid.geo_corr.offset and vals[5] == abi.McGrid.flags.offset
     assert vals[6] == abi.McSource.spec_cdf.offset and vals[7] == abi.McRunOpts.replay_stride.offset
     assert vals[8] == abi.McStats.qphot.offset and vals[9] == abi.McStats.error_packet.offset
+    assert vals[10] == abi.McStats.d2h_bytes.offset
 
 
 def test_product_path_has_no_cpu_fallback(monkeypatch):
