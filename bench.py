@@ -214,9 +214,54 @@ def run_reference(args):
     return 0
 
 
-# Lambda-iteration forms: (transport form, cell update, surrogate options)
-LAMBDA_FORMS = {"chosen": ("graph", "fp32", None), "chosen_surrogate": ("graph", "fp32", {"train_after": 2}),
-                "plain": ("plain", "fp64", None)}
+# Lambda-iteration forms: transport form, march arithmetic, cell update, opacity build, surrogate.
+#  plain: the method without the three patterns on the best kernel (the frequency-sorted wave march
+#         with host-driven rounds, all FP64 but the FP32 CUDA-core opacity; no warm start, one model)
+#  naive: one thread per packet history (FP32 march), FP64 update
+#  chosen: the precision pattern (FP32 march, FP32 update, split-BF16 tensor-core opacity) with the
+#         rounds in one CUDA graph; chosen_surrogate: plus the learned warm start
+LAMBDA_FORMS = {"chosen": ("graph", "fp32", "fp32", "bf16x3", None),
+                "chosen_surrogate": ("graph", "fp32", "fp32", "bf16x3", {"train_after": 2}),
+                "plain": ("wave", "fp64", "fp64", "fp32", None),
+                "naive": ("plain", "fp32", "fp64", "fp32", None)}
+DTE_RULE_PCT = 50.0  # the |dTe| < 1 % rule: this share of the updated cells changed Te by less than 1 %
+
+
+def _wall_to_dte_rule(hist):
+    """Wall time up to the first iteration after which >= DTE_RULE_PCT % of
+    the updated cells changed Te by less than 1 % (None if none did)."""
+    t = 0.0
+    for h in hist:
+        t += h["wall_s"]
+        if h["dte_lt_1pc_pct"] >= DTE_RULE_PCT and h["iteration"] > 1:
+            return t, h["iteration"]
+    return None, None
+
+
+def _lambda_form(neb, name, args, rows):
+    from mocassin_gb300 import iterate
+    form, march, upd, opac, sur = LAMBDA_FORMS[name]
+    if sur is not None and rows is not None:
+        sur = {"rows": rows, "train_after": None, "steps": 2000, "batch": 4096, "lr": 2e-3}
+    li = iterate.LambdaIteration(neb, form=form, march=march, update=upd, opacity_method=opac, surrogate=sur)
+    pre = li.pretrain
+    wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
+    state = li.ctx.get_cell_state()
+    li.close()
+    last = hist[-1]
+    dte_wall, dte_it = _wall_to_dte_rule(hist)
+    rec = {"transport": form, "march": march, "update": upd, "opacity": opac, "surrogate": sur is not None,
+           "wall_s": wall, "iterations": len(hist), "surrogate_s": sum(h["surrogate_s"] for h in hist),
+           "converged": last["converged_pct"] >= 95.0, "converged_pct": last["converged_pct"],
+           "dte_lt_1pc_pct": last["dte_lt_1pc_pct"],
+           "wall_to_dte_rule_s": dte_wall, "iterations_to_dte_rule": dte_it,
+           "transport_s": sum(h["transport_s"] for h in hist), "update_s": sum(h["update_s"] for h in hist),
+           "opacity_s": sum(h["opacity_s"] for h in hist),
+           "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist])),
+           "warm_fallback_pct": float(np.mean([h["warm_fallback_pct"] for h in hist]))}
+    if pre is not None:
+        rec["pretrain"] = pre
+    return rec, state
 
 
 def converged_model(neb, args):
@@ -232,6 +277,8 @@ def converged_model(neb, args):
     ``--surrogate-rows 0``, on the model's own first two iterations."""
     from mocassin_gb300 import iterate, nebula
     out = {"rule": "converged cells (|dX(H0)/X(H0)| <= 5%) >= 95% (iterateMC minConvergence)",
+           "dte_rule": "wall_to_dte_rule_s: up to the first iteration after which >= %g%% of the updated cells "
+                       "changed Te by less than 1%%" % DTE_RULE_PCT,
            "max_iterations": args.lambda_max, "packets_per_iteration": int(sum(neb.n_packets))}
     rows = None
     if args.surrogate_rows > 0:
@@ -239,25 +286,8 @@ def converged_model(neb, args):
         rows = (x, t)
         out["surrogate_dataset"] = info
     states = {}
-    for name, (form, upd, sur) in LAMBDA_FORMS.items():
-        if sur is not None and rows is not None:
-            sur = {"rows": rows, "train_after": None, "steps": 2000, "batch": 4096, "lr": 2e-3}
-        li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
-        pre = li.pretrain
-        wall, hist = li.run(seed=1000, max_iterations=args.lambda_max)
-        states[name] = li.ctx.get_cell_state()
-        li.close()
-        last = hist[-1]
-        out[name] = {"transport": form, "update": upd, "surrogate": sur is not None, "wall_s": wall,
-                     "iterations": len(hist), "surrogate_s": sum(h["surrogate_s"] for h in hist),
-                     "converged": last["converged_pct"] >= 95.0, "converged_pct": last["converged_pct"],
-                     "dte_lt_1pc_pct": last["dte_lt_1pc_pct"],
-                     "transport_s": sum(h["transport_s"] for h in hist), "update_s": sum(h["update_s"] for h in hist),
-                     "opacity_s": sum(h["opacity_s"] for h in hist),
-                     "t_steps_per_cell": float(np.mean([h["t_steps_per_cell"] for h in hist])),
-                     "warm_fallback_pct": float(np.mean([h["warm_fallback_pct"] for h in hist]))}
-        if pre is not None:
-            out[name]["pretrain"] = pre
+    for name in LAMBDA_FORMS:
+        out[name], states[name] = _lambda_form(neb, name, args, rows)
     # the converged states against the plain FP64 form's (same draws, same initial state): Te and
     # the ionic fractions above 1e-3 of every cell the last update reached and balanced in Te in
     # both forms (where the update gives up on Te balance, noTeBal, its Te means nothing)
@@ -275,6 +305,28 @@ def converged_model(neb, args):
                                  "cells": int(reached.sum())}
     out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
     out["speedup_chosen_surrogate_vs_plain"] = out["plain"]["wall_s"] / out["chosen_surrogate"]["wall_s"]
+    # where the chosen form's gain comes from, per Lambda iteration: the transport (FP64 wave march to the
+    # FP32 march in a graph) and the cell update (FP64 to FP32); the warm start against the chosen form
+    per = lambda n, k: out[n][k] / max(out[n]["iterations"], 1)
+    out["speedup_parts"] = {"transport_per_iteration": per("plain", "transport_s") / per("chosen", "transport_s"),
+                            "update_per_iteration": per("plain", "update_s") / per("chosen", "update_s"),
+                            "warm_start_wall": out["chosen"]["wall_s"] / out["chosen_surrogate"]["wall_s"]}
+    return out
+
+
+def breakdown(neb, args, runs):
+    """mean +- sd over `runs` repetitions of each Lambda form: wall, transport
+    and update time, iterations, wall to the |dTe| rule (the warm start's
+    network is trained on the model's own first iterations here)."""
+    out = {}
+    for name in LAMBDA_FORMS:
+        recs = [_lambda_form(neb, name, args, None)[0] for _ in range(runs)]
+        stat = {}
+        for k in ("wall_s", "transport_s", "update_s", "iterations", "wall_to_dte_rule_s"):
+            v = np.array([r[k] for r in recs if r[k] is not None], dtype=float)
+            stat[k] = {"mean": float(v.mean()) if len(v) else None,
+                       "sd": float(v.std(ddof=1)) if len(v) > 1 else None, "n": int(len(v))}
+        out[name] = stat
     return out
 
 
@@ -362,7 +414,9 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--surrogate-rows", type=int, default=1_000_000,
                     help="batch cell states (FP64 update) the warm start is trained on; 0: the model's own")
-    ap.add_argument("--lambda-only", default="", choices=["", "chosen", "chosen_surrogate", "plain"],
+    ap.add_argument("--breakdown", type=int, default=0,
+                    help="only the Lambda forms, each run this many times: mean and sd of their times")
+    ap.add_argument("--lambda-only", default="", choices=["", "chosen", "chosen_surrogate", "plain", "naive"],
                     help="run only the Lambda iteration of one form and print its record (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -388,12 +442,16 @@ def main():
     npk = sum(neb.n_packets)
     if args.lambda_only:
         from mocassin_gb300 import iterate
-        form, upd, sur = LAMBDA_FORMS[args.lambda_only]
-        li = iterate.LambdaIteration(neb, form=form, update=upd, surrogate=sur)
+        form, march, upd, opac, sur = LAMBDA_FORMS[args.lambda_only]
+        li = iterate.LambdaIteration(neb, form=form, march=march, update=upd, opacity_method=opac, surrogate=sur)
         wall, hist = li.run(seed=1000, max_iterations=max(args.lambda_max, 1))
         li.close()
         print(json.dumps({"lambda_only": args.lambda_only, "workload": neb.spec.name, "wall_s": wall,
                           "iterations": hist}))
+        return 0
+    if args.breakdown > 0:
+        print(json.dumps({"breakdown": breakdown(neb, args, args.breakdown), "workload": neb.spec.name,
+                          "runs": args.breakdown, "packets_per_iteration": int(sum(neb.n_packets))}))
         return 0
 
     ctx = transport.TransportContext(neb)

@@ -24,8 +24,9 @@ the sublimation temperature (the reference drops it there).
 
 ``form`` picks the transport ("graph": the frequency-sorted persistent march
 with its rounds in one CUDA graph; "wave": the same with host-driven rounds;
-"plain": one thread per history) and ``update`` the arithmetic of the cell
-update ("fp64": the FP64 method; "fp32": the reference's own 4-byte
+"plain": one thread per history), ``march`` its arithmetic ("fp32", or
+"fp64": the exact per-crossing method) and ``update`` the arithmetic of the
+cell update ("fp64": the FP64 method; "fp32": the reference's own 4-byte
 precision).  ``surrogate`` adds the learned warm start: the cell states of
 the first iterations train an MLP on the GPU, which then predicts the state
 each later update starts from (mc_ctx_update_cells_warm).
@@ -45,7 +46,7 @@ class LambdaIteration:
     """A nebula resident on the GPU with its cell state."""
 
     def __init__(self, neb, form="graph", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None,
-                 emission="auto"):
+                 emission="auto", march="fp32"):
         """surrogate: None (updates start from the previous state, as the
         reference's) or a dict with train_after (cold iterations whose cell
         states train the MLP first; None: never), steps, batch, lr,
@@ -56,6 +57,7 @@ class LambdaIteration:
         mc_ctx_surrogate_rule)."""
         self.neb = neb
         self.form = form
+        self.march = march
         self.update = update
         self.xhi = xhi_limit
         self.opacity_method = opacity_method
@@ -99,7 +101,7 @@ class LambdaIteration:
 
     def step(self, seed, n_packets=None):
         t0 = time.perf_counter()
-        tr = self.ctx.run(n_packets=n_packets, seed=seed, iteration=len(self.history) + 1, precision="fp32",
+        tr = self.ctx.run(n_packets=n_packets, seed=seed, iteration=len(self.history) + 1, precision=self.march,
                           zero_first=True, form=self.form)
         t1 = time.perf_counter()
         return self.after_transport(tr, t0, t1)
