@@ -155,15 +155,23 @@ class OracleStep:
         return time.perf_counter() - t0, st["crossings"]
 
 
-def cpu_baseline(neb, threads=None):
-    """FP32 oracle on the host cores: one full step after one warm-up step
-    (about 10 s of CPU work on the 61^3 workload)."""
-    step = OracleStep(neb, threads=threads)
-    step(1)
-    dt, cross = step(2)
-    return {"value": cross / dt, "unit": UNIT, "cores": step.threads, "kind": "port",
-            "sample": "the full %d-packet step after one warm-up step (%d crossings, %.1f s, FP32 march, FP64 sums; "
-                      "estimators zeroed inside, allocated outside)" % (sum(neb.n_packets), cross, dt)}
+def cpu_baseline(args):
+    """FP32 oracle on the host cores: one full step of the reference arm (a
+    bounded warm-up sample, then every packet of the step), run as a child
+    process so that it times exactly what --impl reference times (about
+    10 s of CPU work on the 61^3 workload)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", "1", "--warmup", "1",
+           "--config", args.config]
+    if args.packets:
+        cmd += ["--packets", str(args.packets)]
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    out = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1200)
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    cb = dict(line["cpu_baseline"])
+    cb["sample"] = ("the full %d-packet step after a %d-packet warm-up step, timed by --impl reference in a "
+                    "child process (FP32 march, FP64 sums; estimators zeroed inside, allocated outside)"
+                    % (line["config"]["packets_per_step"], line["impl_detail"]["warmup_packets"]))
+    return cb
 
 
 def dist_env():
@@ -288,21 +296,23 @@ def converged_model(neb, args):
     states = {}
     for name in LAMBDA_FORMS:
         out[name], states[name] = _lambda_form(neb, name, args, rows)
-    # the converged states against the plain FP64 form's (same draws, same initial state): Te and
-    # the ionic fractions above 1e-3 of every cell the last update reached and balanced in Te in
+    # the converged states of the chosen forms against (vs_fp64_update) the naive form's, the same FP32
+    # draws and march with the FP64 cell update, which isolates the update's precision, and against
+    # (vs_plain) the plain FP64 method, whose march takes other paths, so that packet noise dominates:
+    # Te and the ionic fractions above 1e-3 of every cell the last update reached and balanced in Te in
     # both forms (where the update gives up on Te balance, noTeBal, its Te means nothing)
-    te_p, _, x_p = states["plain"][:3]
-    for name in ("chosen", "chosen_surrogate"):
-        te, _, x = states[name][:3]
-        reached = (states["plain"][4] > 0) & ((states["plain"][5] & 1) == 0) & ((states[name][5] & 1) == 0)
-        dte = np.abs(te[reached] / te_p[reached] - 1)
-        big = (x_p[reached] > 1e-3)
-        dx = np.abs(x[reached][big] / x_p[reached][big] - 1)
-        out[name]["vs_plain"] = {"te_rel_median": float(np.median(dte)), "te_rel_p95": float(np.quantile(dte, 0.95)),
-                                 "ion_frac_rel_median": float(np.median(dx)),
-                                 "ion_frac_rel_p95": float(np.quantile(dx, 0.95)),
-                                 "ion_frac_within_2pct": float(np.mean(dx <= 0.02)),
-                                 "cells": int(reached.sum())}
+    for ref in ("naive", "plain"):
+        te_p, _, x_p = states[ref][:3]
+        for name in ("chosen", "chosen_surrogate"):
+            te, _, x = states[name][:3]
+            reached = (states[ref][4] > 0) & ((states[ref][5] & 1) == 0) & ((states[name][5] & 1) == 0)
+            dte = np.abs(te[reached] / te_p[reached] - 1)
+            big = (x_p[reached] > 1e-3)
+            dx = np.abs(x[reached][big] / x_p[reached][big] - 1)
+            out[name]["vs_fp64_update" if ref == "naive" else "vs_plain"] = {
+                "te_rel_median": float(np.median(dte)), "te_rel_p95": float(np.quantile(dte, 0.95)),
+                "ion_frac_rel_median": float(np.median(dx)), "ion_frac_rel_p95": float(np.quantile(dx, 0.95)),
+                "ion_frac_within_2pct": float(np.mean(dx <= 0.02)), "cells": int(reached.sum())}
     out["speedup_chosen_vs_plain"] = out["plain"]["wall_s"] / out["chosen"]["wall_s"]
     out["speedup_chosen_surrogate_vs_plain"] = out["plain"]["wall_s"] / out["chosen_surrogate"]["wall_s"]
     # where the chosen form's gain comes from, per Lambda iteration: the transport (FP64 wave march to the
@@ -317,10 +327,15 @@ def converged_model(neb, args):
 def breakdown(neb, args, runs):
     """mean +- sd over `runs` repetitions of each Lambda form: wall, transport
     and update time, iterations, wall to the |dTe| rule (the warm start's
-    network is trained on the model's own first iterations here)."""
+    network trained on the batch's FP64 cell states, as in the main run)."""
+    from mocassin_gb300 import iterate, nebula
+    rows = None
+    if args.surrogate_rows > 0:
+        x, t, _ = iterate.training_rows(nebula.batch64(), max_rows=args.surrogate_rows)
+        rows = (x, t)
     out = {}
     for name in LAMBDA_FORMS:
-        recs = [_lambda_form(neb, name, args, None)[0] for _ in range(runs)]
+        recs = [_lambda_form(neb, name, args, rows)[0] for _ in range(runs)]
         stat = {}
         for k in ("wall_s", "transport_s", "update_s", "iterations", "wall_to_dte_rule_s"):
             v = np.array([r[k] for r in recs if r[k] is not None], dtype=float)
@@ -640,7 +655,7 @@ def main():
     if args.batch_models > 0 and rank == 0:
         line["batched_models"] = batched_models(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(neb)
+        line["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
