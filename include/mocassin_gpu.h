@@ -373,6 +373,41 @@ mc_status mc_ctx_get_cell_state(mc_ctx_t *ctx, double *te, double *ne, double *i
  * the reference's own updateCell (`real`), ~64x the FP64 rate on GB300. */
 mc_status mc_ctx_update_cells(mc_ctx_t *ctx, const float *w, double scale, double xhi_limit, int32_t precision,
                               mc_update_stats_t *stats);
+
+/* Grains in the gas update (lgDust and lgGas with lgPhotoelectric, the
+ * reference's default): every T step of every cell then runs
+ * setGrainPotential, setPhotoelHeatCool and setDustGasCollHeatCool
+ * (source/update_mod.f90:527-930, called at :367-386) between ionBalance and
+ * thermBalance, which adds the photoelectric heating and the collisional
+ * cooling of the gas (:1251-1254).  The collision terms use the grain
+ * temperatures the last mc_ctx_dust_temperatures left on the device (0 K
+ * before the first, as the reference's Tdust starts), and the next
+ * mc_ctx_dust_temperatures adds each size's gasDustColl_d - photoelHeat_d of
+ * the last update to its absorbed integral (getDustT, :1886-1889).  The cell
+ * flag 8 marks a grain potential that did not converge within 100 steps in
+ * the cell's last T step.  One grain species in nsizes size bins. */
+typedef struct mc_grain_physics {
+  int32_t nsizes;            /* 1..32 size bins                                */
+  const float *xs_abs;       /* [nsizes][nbins] absorption cross-section per
+                                grain [cm^2] (xSecArray at dustAbsXsecP)       */
+  const double *radius_um;   /* [nsizes] grainRadius [um]                      */
+  const double *weight;      /* [nsizes] grainWeight                           */
+  double abundance;          /* grainAbun of the species                       */
+  double vn;                 /* grainVn [Ryd] (the species' n,k file header)   */
+  double msurf;              /* MsurfAtom (the same header)                    */
+  const double *ion_nu;      /* [33] threshold [Ryd] of each balance ion: the
+                                IP whose energy a recombining stage above it
+                                leaves on the grain (IPerg)                    */
+  const float *ndust;        /* [Nc+1] grains per cm^3 (Ndust)                 */
+} mc_grain_physics_t;
+
+/* grains NULL: a gas-only update again.  Replaces nothing on the Fortran
+ * side: the reference reads the same quantities from its dust module. */
+mc_status mc_ctx_set_grain_physics(mc_ctx_t *ctx, const mc_grain_physics_t *grains);
+/* The grain block of each cell's last T step in the last update with
+ * grains, host arrays [nsizes][Nc+1]: the potential grainPot [Ryd],
+ * photoelHeat_d and gasDustColl_d (any pointer may be NULL). */
+mc_status mc_ctx_grain_state(mc_ctx_t *ctx, double *potential, double *photoel_cool, double *coll_heat);
 /* Rebuilds the resident opacity from the cell state: den[k][cell] =
  * ionden(elem_k, stage_k) * abund(elem_k) * Hden(cell) for the nspecies rows
  * (elem, stage) = species[k], then the contraction with xs [nspecies][nbins]

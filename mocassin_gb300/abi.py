@@ -110,6 +110,29 @@ def emission_tables_struct(t):
     return s
 
 
+class McGrainPhysics(C.Structure):
+    _fields_ = [("nsizes", C.c_int32), ("xs_abs", _fp), ("radius_um", _dp), ("weight", _dp),
+                ("abundance", C.c_double), ("vn", C.c_double), ("msurf", C.c_double), ("ion_nu", _dp),
+                ("ndust", _fp)]
+
+
+def grain_physics_struct(gp):
+    """McGrainPhysics over the arrays of mocassin_gb300.dust.grain_physics()."""
+    keep = {}
+
+    def arr(name, dt):
+        a = np.ascontiguousarray(gp[name], dtype=dt)
+        keep[name] = a
+        return a.ctypes.data_as(_fp if dt == np.float32 else _dp)
+
+    xs = np.asarray(gp["xs_abs"])
+    s = McGrainPhysics(nsizes=xs.shape[0], xs_abs=arr("xs_abs", np.float32), radius_um=arr("radius_um", np.float64),
+                       weight=arr("weight", np.float64), abundance=float(gp["abundance"]), vn=float(gp["vn"]),
+                       msurf=float(gp["msurf"]), ion_nu=arr("ion_nu", np.float64), ndust=arr("ndust", np.float32))
+    s._keep = keep
+    return s
+
+
 class McUpdateStats(C.Structure):
     _fields_ = [("hit", C.c_int64), ("converged", C.c_int64), ("no_te_balance", C.c_int64),
                 ("no_ion_balance", C.c_int64), ("t_iterations", C.c_int64), ("dte_max", C.c_double),

@@ -63,6 +63,18 @@ def moment_weights(xs, nu, ions):
     return np.ascontiguousarray(w.astype(np.float32))
 
 
+def ion_thresholds(xs, nu, ions):
+    """Threshold energy [Ryd] of each of the 33 balance ions: nu at the first
+    bin with a nonzero cross-section (the IP of the heating sums)."""
+    rows = {tuple(int(v) for v in r): k for k, r in enumerate(ions)}
+    out = np.zeros(NBAL)
+    for b, key in enumerate(BALANCE_IONS):
+        x = xs[rows[key]].astype(np.float64)
+        nz = np.nonzero(x >= 1e-35)[0]
+        out[b] = float(nu[nz[0]]) if len(nz) else 0.0
+    return out
+
+
 def initial_state(neb):
     """(te, ne, X) at the start of an iteration from the nebula's ion rows:
     X[cell, element, stage] fractions, the top stage the remainder."""

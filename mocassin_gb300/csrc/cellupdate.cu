@@ -65,7 +65,14 @@ cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int nu
   int blocks = (cells + kW - 1) / kW;
   if (blocks > num_sms * 16) blocks = num_sms * 16;
   if (blocks < 1) blocks = 1;
-  cell_update_kernel<double, false><<<blocks, kW * 32, 0, stream>>>(a);
+  // grains: each warp stages its cell's photon flux per bin in shared memory
+  const size_t sh = a.g.nsizes > 0 ? (size_t)kW * a.g.nb * sizeof(double) : 0;
+  if (sh > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(cell_update_kernel<double, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    if (e != cudaSuccess) return e;
+  }
+  cell_update_kernel<double, false><<<blocks, kW * 32, sh, stream>>>(a);
   return cudaGetLastError();
 }
 

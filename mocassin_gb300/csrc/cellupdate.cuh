@@ -20,7 +20,10 @@
 // without pivoting, in local memory).  Sums that the reference forms in one
 // order (Ne, the cooling and heating totals) are formed by lane 0 in that
 // order, so the FP64 instantiation (compiled with -fmad=false) follows the
-// FP64 oracle operation by operation.  Per cell and T step the work is
+// FP64 oracle operation by operation.  In a cell with grains the warp also
+// runs the grain block of each T step (grains.cuh) between ionBalance and
+// thermBalance, on the cell's Jste row staged once in shared memory.  Per
+// cell and T step the work is
 // ~1e4-1e5 operations, most of them in the level populations: the FP64 form
 // is bound by GB300's FP64 rate, the FP32 form by issue and local memory.
 #pragma once
@@ -29,6 +32,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "grains.cuh"
 #include "mc_launch.h"
 
 namespace mcg {
@@ -326,6 +330,17 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       if (lane == 0) { a.conv[c] = 0; a.niter[c] = 0; a.flags[c] = 0; a.dte[c] = -1.; }
       continue;
     }
+    // grains: this cell's photon flux Jste x scale / (hcRyd nu) per bin
+    const int ngr = a.g.nsizes;
+    const size_t gnc1 = (size_t)a.nc + 1;
+    Real *pf = (Real *)(cu_dyn + (Fast ? (size_t)kW * a.ncel * a.mat_stride * sizeof(Real) : 0)) + (size_t)w * a.g.nb;
+    Real gvg = (Real)0., gpd = (Real)0., gcd = (Real)0., gtd = (Real)0., gheat = (Real)0., gcool = (Real)0.;
+    bool gconv = true;
+    if (ngr > 0) {
+      for (int i = lane; i < a.g.nb; i += 32)
+        pf[i] = (Real)((a.g.jste[(size_t)i * gnc1 + c] * a.g.jscale) / (2.1799153e-11 * (double)a.g.nu[i]));
+      if (lane < ngr && a.g.tdust) gtd = (Real)a.g.tdust[(size_t)(1 + lane) * gnc1 + c];
+    }
     double *Xc = a.X + (size_t)c * kNE * kNX;
     for (int i = lane; i < kNE * kNX; i += 32) sX[w][i / kNX][i % kNX] = (Real)Xc[i];
     const Real hden = (Real)a.hden[c];
@@ -412,6 +427,15 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
         if (off && nIterX == 25) ionConv = false;
         break;
       }
+      if (ngr > 0) {
+        __syncwarp();
+        auto Xf = [&](int e, int s) -> Real { return sX[w][e][s]; };
+        const GrainOut go = grain_step<Real>(a.g, a.bal_z, a.bal_first, T.ab, Te, Ne, hden, (Real)a.g.ndust[c], Xf, pf,
+                                             gtd, lane, gvg, gpd, gcd);
+        gheat = (Real)go.heat;
+        gcool = (Real)go.cool;
+        gconv = go.converged;
+      }
       // thermBalance
       if (lane < a.ncel) {
         const UpdCelT<Real> &C = T.cel[lane];
@@ -460,6 +484,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
           coolColl += sCel[w][k] * T.ab[C.e] * sX[w][C.e][C.ion] * (Real)1.9865e-16;
         }
         coolInt = coolFF + coolRec + coolColl;
+        if (ngr > 0) coolInt = coolInt + gcool;
       }
       // heating: the sums live in the lanes' registers; gathered in order
       {
@@ -472,7 +497,7 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
             hs += hb * sX[w][B.e][B.ion] * T.ab[B.e];
           }
         }
-        if (lane == 0) heatInt = hs;
+        if (lane == 0) heatInt = ngr > 0 ? hs + gheat : hs;
       }
       heatInt = __shfl_sync(0xffffffffu, heatInt, 0);
       coolInt = __shfl_sync(0xffffffffu, coolInt, 0);
@@ -534,8 +559,13 @@ __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_const
       if (a.forb_ok) a.forb_ok[c] = 0;  // this form keeps no line totals
       a.conv[c] = fabs((sX[w][0][1] - XOldHI) / XOldHI) <= (Real)a.xhi ? 1 : 0;
       a.niter[c] = nIterT;
-      a.flags[c] = (noTe ? 1 : 0) | (ionConv ? 0 : 2) | (cold ? 4 : 0);
+      a.flags[c] = (noTe ? 1 : 0) | (ionConv ? 0 : 2) | (cold ? 4 : 0) | (gconv ? 0 : 8);
       a.dte[c] = fabs((double)Te - (double)Te0) / (double)Te0;
+    }
+    if (ngr > 0 && lane < ngr) {
+      a.g.out[(size_t)lane * gnc1 + c] = (double)gvg;
+      a.g.out[(size_t)(ngr + lane) * gnc1 + c] = (double)gpd;
+      a.g.out[(size_t)(2 * ngr + lane) * gnc1 + c] = (double)gcd;
     }
     __syncwarp();
   }

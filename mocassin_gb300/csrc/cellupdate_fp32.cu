@@ -9,6 +9,9 @@
 // time, so every lane of a warp does the same work:
 //   wave_ion_kernel    one thread per active cell: calcAlpha and the
 //                      ionBalance passes (at most 25) at the cell's Te;
+//   wave_grain_kernel  (cells with grains) one warp per active cell: the
+//                      grain potentials, photoelectric and collision terms
+//                      of the T step (grains.cuh) at the new ion fractions;
 //   wave_cel_kernel    one thread per (line ion, active cell): the level
 //                      populations and forbidden-line cooling of that ion
 //                      (equilibrium, emission_mod.f90:1913-2115); the 32
@@ -38,6 +41,8 @@ struct WaveArgs {
   float *sec;         // [5][nc+1]: Thigh, Tlow, resHigh, resLow, fstep
   int *nit, *flags;   // [nc+1]: T steps, bit 1 = ion balance not converged in the last step
   float *cool;        // [ncel][nc+1] forbidden-line cooling per H
+  float *gheat, *gcool;  // [nc+1] grains: photoelectric heating and collisional cooling of the gas per H
+  float *gpf;            // [nc+1][nbp] grains: each cell's photon flux Jste x scale / (hcRyd nu) per bin
   int *act[2];        // active lists
   int *count;         // [2] their lengths
 };
@@ -137,6 +142,67 @@ __global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ W
   }
 }
 
+// each cell's photon flux per bin for the grain block, once per update:
+// Jste [nb][nc+1] (bin-major) -> gpf [nc+1][nbp] (cell-major), through 32 x
+// 32 tiles in shared memory so that both sides are coalesced
+__global__ void grain_flux_kernel(const __grid_constant__ WaveArgs w) {
+  __shared__ float tile[32][33];
+  const GrainArgs &g = w.a.g;
+  const int nc1 = w.a.nc + 1, nb = g.nb, nbp = (nb + 1) & ~1;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  const int tiles_c = (nc1 + 31) / 32, tiles_b = (nb + 31) / 32;
+  for (int t = blockIdx.x; t < tiles_c * tiles_b; t += gridDim.x) {
+    const int c0 = (t % tiles_c) * 32, b0 = (t / tiles_c) * 32;
+    for (int r = ty; r < 32; r += 8) {
+      const int b = b0 + r, c = c0 + tx;
+      float v = 0.f;
+      if (b < nb && c < nc1) v = (float)(g.jste[(size_t)b * nc1 + c] * g.jscale * g.inv_hnu[b]);
+      tile[r][tx] = v;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const int c = c0 + r, b = b0 + tx;
+      if (c < nc1 && b < nb) w.gpf[(size_t)c * nbp + b] = tile[tx][r];
+    }
+    __syncthreads();
+  }
+}
+
+// the grain block of every active cell at its current Te and ion fractions
+// (one warp per cell; the cell's photon flux per bin staged in shared memory)
+__global__ void __launch_bounds__(128) wave_grain_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  extern __shared__ __align__(16) float gr_pf[];
+  const UpdArgs &a = w.a;
+  const GrainArgs &g = a.g;
+  const int n = w.count[cur], ns = g.nsizes, nb = g.nb;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t nc1 = (size_t)a.nc + 1;
+  const int nbp = (nb + 1) & ~1;
+  float *pf = gr_pf + (size_t)wid * nbp;
+  float *sfx = gr_pf + 4 * (size_t)nbp + (size_t)wid * ns * 2 * kGrWin;
+  for (int k = blockIdx.x * 4 + wid; k < n; k += gridDim.x * 4) {
+    const int c = w.act[cur][k];
+    for (int i = lane; i < nb; i += 32) pf[i] = w.gpf[(size_t)c * nbp + i];
+    const float td = (lane < ns && g.tdust) ? g.tdust[(size_t)(1 + lane) * nc1 + c] : 0.f;
+    __syncwarp();
+    auto Xf = [&](int e, int s) -> float { return XS(w, e * kNX + s, c); };
+    float vg = 0.f, pd = 0.f, cd = 0.f;
+    const GrainOut go = grain_step_fast(g, a.bal_z, a.bal_first, a.f.ab, w.Te[c], w.Ne[c], (float)a.hden[c],
+                                        g.ndust[c], Xf, pf, sfx, td, lane, vg, pd, cd);
+    if (lane == 0) {
+      w.gheat[c] = (float)go.heat;
+      w.gcool[c] = (float)go.cool;
+      w.flags[c] = (w.flags[c] & ~8) | (go.converged ? 0 : 8);
+    }
+    if (lane < ns) {
+      g.out[(size_t)lane * nc1 + c] = (double)vg;
+      g.out[(size_t)(ns + lane) * nc1 + c] = (double)pd;
+      g.out[(size_t)(2 * ns + lane) * nc1 + c] = (double)cd;
+    }
+    __syncwarp();
+  }
+}
+
 // forbidden-line cooling per H of line ion `ion` in every active cell.  The
 // level-population matrix of each thread is in local memory with the row
 // length of the largest ion (mat_rows): the fewer bytes a thread touches, the
@@ -200,7 +266,11 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
       const UpdIonT<float> &B = T.bal[b];
       heat += a.mom[(size_t)(1 + kNB + b) * a.mstride + c] * XS(w, B.e * kNX + B.ion, c) * T.ab[B.e];
     }
-    const float cool = coolFF + coolRec + coolColl;
+    float cool = coolFF + coolRec + coolColl;
+    if (a.g.nsizes > 0) {
+      cool += w.gcool[c];
+      heat += w.gheat[c];
+    }
     const float res = heat - cool;
     float Thigh = w.sec[0 * nc1 + c], Tlow = w.sec[1 * nc1 + c];
     float resHigh = w.sec[2 * nc1 + c], resLow = w.sec[3 * nc1 + c], fstep = w.sec[4 * nc1 + c];
@@ -271,7 +341,7 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
     const double xh = (double)xH1;
     a.conv[c] = fabs((xh - x0) / x0) <= a.xhi ? 1 : 0;
     a.niter[c] = nIterT;
-    a.flags[c] = (noTe ? 1 : 0) | (w.flags[c] & 6);
+    a.flags[c] = (noTe ? 1 : 0) | (w.flags[c] & 14);
     a.dte[c] = fabs((double)Te - te0) / te0;
   }
 }
@@ -283,15 +353,28 @@ __global__ void wave_reset_kernel(int *count, int slot) { count[slot] = 0; }
 // blocks per SM of the level-population kernels: as many as are resident
 int cel_blocks_per_sm() { return 32; }
 
-cudaError_t cell_update_fp32_prepare(const UpdArgs &) {
+// shared memory of wave_grain_kernel: per warp the cell's photon flux per
+// bin and each size's two suffix sums over the bins above grainVn
+static size_t grain_smem(const GrainArgs &g) {
+  const size_t nbp = (size_t)((g.nb + 1) & ~1);
+  return 4 * nbp * sizeof(float) + 4 * (size_t)g.nsizes * 2 * kGrWin * sizeof(float);
+}
+
+cudaError_t cell_update_fp32_prepare(const UpdArgs &a) {
+  if (a.g.nsizes > 0) {
+    cudaError_t e = cudaFuncSetAttribute(wave_grain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)grain_smem(a.g));
+    if (e != cudaSuccess) return e;
+  }
   return cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
 }
 
-size_t cell_update_fp32_scratch(int nc, int ncel) {
+size_t cell_update_fp32_scratch(int nc, int ncel, int nsizes, int nb) {
   const size_t nc1 = (size_t)nc + 1;
   // the arrays of launch_cell_update_fp32, each rounded up to 256 bytes
   auto r = [](size_t b) { return (b + 255) / 256 * 256; };
-  return r(nc1 * kX * 4) + 2 * r(nc1 * 4) + r(nc1 * 5 * 4) + r(nc1 * (size_t)ncel * 4) + 4 * r(nc1 * 4) + r(8);
+  return r(nc1 * kX * 4) + 2 * r(nc1 * 4) + r(nc1 * 5 * 4) + r(nc1 * (size_t)ncel * 4) + 4 * r(nc1 * 4) + r(8) +
+         (nsizes > 0 ? 2 * r(nc1 * 4) + r(nc1 * (size_t)((nb + 1) & ~1) * 4) : 0);
 }
 
 cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream) {
@@ -310,16 +393,23 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
   w.act[0] = (int *)take(nc1 * sizeof(int));
   w.act[1] = (int *)take(nc1 * sizeof(int));
   w.count = (int *)take(2 * sizeof(int));
+  if (a.g.nsizes > 0) {
+    w.gheat = (float *)take(nc1 * sizeof(float));
+    w.gcool = (float *)take(nc1 * sizeof(float));
+    w.gpf = (float *)take(nc1 * (size_t)((a.g.nb + 1) & ~1) * sizeof(float));
+  }
   cudaError_t e = cudaMemsetAsync(w.count, 0, 2 * sizeof(int), stream);
   if (e != cudaSuccess) return e;
   const int blocks = num_sms * 8;
   wave_init_kernel<<<blocks, 256, 0, stream>>>(w);
+  if (a.g.nsizes > 0) grain_flux_kernel<<<num_sms * 8, 256, 0, stream>>>(w);
   // a warm start may send a cell back to the cold solve after its first step
   const int steps = a.x_prev ? 26 : 25;
   for (int t = 0; t < steps; ++t) {
     const int cur = t & 1;
     wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
     wave_ion_kernel<<<blocks, 128, 0, stream>>>(w, cur);
+    if (a.g.nsizes > 0) wave_grain_kernel<<<blocks, 128, grain_smem(a.g), stream>>>(w, cur);
     wave_cel_kernel<<<num_sms * cel_blocks_per_sm(), 128, 0, stream>>>(w, cur);
     wave_therm_kernel<<<blocks, 128, 0, stream>>>(w, cur);
   }

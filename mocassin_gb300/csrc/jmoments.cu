@@ -159,14 +159,18 @@ __global__ void __launch_bounds__(128, 4) jmoment_tc_kernel(const __grid_constan
 // locate: nt above the table, 0 below it, else the last entry <= A, and 1
 // when no entry exceeds A), then T = i + (A - E(i)) / (E(i+1) - E(i));
 // below the table T = 1, above it T = nt.  Row 0 of tdust is the
-// weighted mean over sizes; cells no packet reached get 0.
+// weighted mean over sizes; cells no packet reached get 0.  With gas and
+// grains (gcd, gpd non-null: [nsizes][nc1] of the last cell update) the
+// absorbed integral gains gasDustColl_d - photoelHeat_d (:1886-1889).
 __global__ void dust_temperature_kernel(int nc1, int nsizes, int nt, const float *A, const float *E,
-                                        const float *gw, const float *hit, float *tdust) {
+                                        const float *gw, const float *hit, float *tdust, const double *gcd,
+                                        const double *gpd) {
   for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c < nc1; c += gridDim.x * blockDim.x) {
     const bool reached = hit[c] > 0.f;
     float mean = 0.f;
     for (int k = 0; k < nsizes; ++k) {
-      const float x = A[(size_t)k * nc1 + c];
+      float x = A[(size_t)k * nc1 + c];
+      if (gcd) x = (float)(((double)x + gcd[(size_t)k * nc1 + c]) - gpd[(size_t)k * nc1 + c]);
       const float *e = E + (size_t)k * nt;
       float t = 0.f;
       if (reached) {
@@ -194,8 +198,9 @@ __global__ void dust_temperature_kernel(int nc1, int nsizes, int nt, const float
 }
 
 cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
-                                    const float *hit, float *tdust, int num_sms, cudaStream_t stream) {
-  dust_temperature_kernel<<<num_sms * 4, 256, 0, stream>>>(nc1, nsizes, nt, A, E, gw, hit, tdust);
+                                    const float *hit, float *tdust, const double *gcd, const double *gpd, int num_sms,
+                                    cudaStream_t stream) {
+  dust_temperature_kernel<<<num_sms * 4, 256, 0, stream>>>(nc1, nsizes, nt, A, E, gw, hit, tdust, gcd, gpd);
   return cudaGetLastError();
 }
 

@@ -79,6 +79,27 @@ template <typename Real> struct UpdTabs {
 struct UpdStatsDev {
   unsigned long long hit, converged, no_te, no_ion, iters, small, dmax_bits, fallback;
 };
+// The grains of the photoelectric and gas-grain collision terms of the cell
+// update (grains.cuh); nsizes = 0: a gas-only update.
+struct GrainArgs {
+  int nsizes, nb;
+  int ivn;                              // first bin above grainVn (0-based)
+  double vn, msurf, abundance;          // grainVn [Ryd], MsurfAtom, grainAbun
+  const float *nu;                      // [nb] Ryd
+  const float *xs;                      // [nsizes][nb] Cabs per grain [cm^2]
+  const double *radius_um, *weight;     // [nsizes] grainRadius [um], grainWeight
+  const double *ion_nu;                 // [33] threshold of each balance ion [Ryd]
+  const double *yn_d, *dnu_d, *qa_d;    // [nb] yield Yn, nu - Vn; [nsizes][nb] Cabs / (1e-8 a^2)
+  const float *yn_f, *dnu_f, *qa_f;     // the same in FP32
+  const float *idnu_f;                  // [nb] 1 / (nu - Vn) (the FP32 form)
+  const double *inv_hnu;                // [nb] 1 / (hcRyd nu) (the FP32 form's photon flux)
+  const double *jste;                   // Jste [nb][nc+1] (not normalised)
+  double jscale;                        // its normalisation
+  const float *ndust;                   // [nc+1] grains per cm^3
+  const float *tdust;                   // [nsizes+1][nc+1] grain temperatures (rows 1..), null: 0 K
+  double *out;                          // [3][nsizes][nc+1] potential, photoelHeat_d, gasDustColl_d
+};
+
 struct UpdArgs {
   int nc, ncel, ndirec, naldro;
   int bal_z[7], bal_first[7];
@@ -106,13 +127,14 @@ struct UpdArgs {
   int *forb_ok;
   double step0;                      // first unbracketed Te step factor (1.2: iterateT's)
   int step_grow;                     // warm start: (factor - 1) doubles per unbracketed step, up to 0.2
+  GrainArgs g;                       // grains (g.nsizes = 0: none)
 };
 cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int num_sms, cudaStream_t stream);
 cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream);
 // sets the cache preference of the FP32 form's kernels (before a capture)
 cudaError_t cell_update_fp32_prepare(const UpdArgs &a);
 int cel_blocks_per_sm();
-size_t cell_update_fp32_scratch(int nc, int ncel);
+size_t cell_update_fp32_scratch(int nc, int ncel, int nsizes, int nb);
 cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const int *flags, const double *dte,
                                 UpdStatsDev *s, int num_sms, cudaStream_t stream);
 cudaError_t launch_species(int nc, int nsp, const int *sp_e, const int *sp_s, const double *X, const double *ab,
@@ -148,7 +170,8 @@ cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const flo
                              cudaStream_t s);
 
 cudaError_t launch_dust_temperature(int nc1, int nsizes, int nt, const float *A, const float *E, const float *gw,
-                                    const float *hit, float *tdust, int num_sms, cudaStream_t stream);
+                                    const float *hit, float *tdust, const double *gcd, const double *gpd, int num_sms,
+                                    cudaStream_t stream);
 
 cudaError_t launch_wave_round_control(const WaveLaunch &L, cudaGraphConditionalHandle h);
 

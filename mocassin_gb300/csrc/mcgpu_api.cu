@@ -158,6 +158,12 @@ struct mc_ctx {
   DBuf e_tab, e_forb;
   DBuf e_ok, e_list, e_cnt;  // per cell: the line totals in e_forb belong to the state (1); stale-cell list
   DBuf d_tdust;      // grain temperatures of the last mc_ctx_dust_temperatures [nsizes+1][nc+1]
+  // grains in the gas update (mc_ctx_set_grain_physics): tables and the
+  // grain state of the last update with grains [3][nsizes][nc+1]
+  DBuf g_nu, g_xs, g_rad, g_w, g_ip, g_ynd, g_dnud, g_qad, g_ynf, g_dnuf, g_qaf, g_nd, g_out, g_ihnu, g_idnuf;
+  int g_ns = 0, g_ivn = 0;
+  double g_vn = 0., g_msurf = 0., g_abun = 0.;
+  bool g_fresh = false;  // g_out belongs to the last update
   DBuf o_fix_den, o_fix_xs;  // opacity rows that do not follow the cell state (grains)
   int o_nfix = 0;
   int d_nsizes = 0;
@@ -1272,6 +1278,8 @@ extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const
   if (nsizes < 1 || nsizes > 127) return set_error(MC_ERR_ARG, "nsizes must be 1..127 (got %d)", nsizes);
   if (ntemps < 2) return set_error(MC_ERR_ARG, "ntemps must be >= 2");
   const int nc1 = c->nc + 1, nb = c->nb, nout = nsizes + 1;
+  // gas and grains: the grain terms of the last update join the absorbed integrals
+  const bool grains = c->g_ns > 0 && c->g_fresh && c->g_ns == nsizes;
   // column 0 = 1: the hit test of updateCell (any Jste > 0)
   std::vector<float> w((size_t)nb * nout);
   for (int i = 0; i < nb; ++i) {
@@ -1297,8 +1305,10 @@ extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const
   cudaError_t e = mcg::launch_jmoments(nc1, nb, nout, c->jste.as<double>(), dw.as<float>(), scale, dm.as<float>(),
                                        err.as<int>(), c->num_sms, s);
   if (e == cudaSuccess)
-    e = mcg::launch_dust_temperature(nc1, nsizes, ntemps, dm.as<float>() + nc1, de.as<float>(), dg.as<float>(),
-                                     dm.as<float>(), dt.as<float>(), c->num_sms, s);
+    e = mcg::launch_dust_temperature(
+        nc1, nsizes, ntemps, dm.as<float>() + nc1, de.as<float>(), dg.as<float>(), dm.as<float>(), dt.as<float>(),
+        grains ? c->g_out.as<double>() + (size_t)2 * nsizes * nc1 : nullptr,
+        grains ? c->g_out.as<double>() + (size_t)nsizes * nc1 : nullptr, c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "dust temperature launch failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(c->evm1, s));
   int herr = 0;
@@ -1656,8 +1666,32 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
     a.forb_out = precision == MC_PREC_FP32 ? c->e_forb.as<float>() : nullptr;
     a.forb_ok = c->e_ok.as<int>();
   }
+  if (c->g_ns > 0) {
+    mcg::GrainArgs &g = a.g;
+    g.nsizes = c->g_ns;
+    g.nb = nb;
+    g.ivn = c->g_ivn;
+    g.vn = c->g_vn; g.msurf = c->g_msurf; g.abundance = c->g_abun;
+    g.nu = c->g_nu.as<float>(); g.xs = c->g_xs.as<float>();
+    g.radius_um = c->g_rad.as<double>(); g.weight = c->g_w.as<double>(); g.ion_nu = c->g_ip.as<double>();
+    g.yn_d = c->g_ynd.as<double>(); g.dnu_d = c->g_dnud.as<double>(); g.qa_d = c->g_qad.as<double>();
+    g.yn_f = c->g_ynf.as<float>(); g.dnu_f = c->g_dnuf.as<float>(); g.qa_f = c->g_qaf.as<float>();
+    g.idnu_f = c->g_idnuf.as<float>();
+    g.inv_hnu = c->g_ihnu.as<double>();
+    g.jste = c->jste.as<double>();
+    g.jscale = scale;
+    g.ndust = c->g_nd.as<float>();
+    g.tdust = (c->d_tdust.p && c->d_nsizes == c->g_ns) ? c->d_tdust.as<float>() : nullptr;
+    mc_status gs = c->g_out.bytes == (size_t)3 * c->g_ns * nc1 * sizeof(double)
+                       ? MC_OK
+                       : put_buf(c->g_out, nullptr, (size_t)3 * c->g_ns * nc1 * sizeof(double), s);
+    if (gs) return gs;
+    MC_CUDA(cudaMemsetAsync(c->g_out.p, 0, c->g_out.bytes, s));
+    g.out = c->g_out.as<double>();
+    c->g_fresh = true;
+  }
   if (precision == MC_PREC_FP32) {
-    const size_t need = mcg::cell_update_fp32_scratch(c->nc, c->u_ncel);
+    const size_t need = mcg::cell_update_fp32_scratch(c->nc, c->u_ncel, c->g_ns, nb);
     mc_status ss = c->s_wave.bytes == need ? MC_OK : put_buf(c->s_wave, nullptr, need, s);
     if (ss) return ss;
   }
@@ -1727,6 +1761,84 @@ extern "C" mc_status mc_ctx_update_cells(mc_ctx_t *c, const float *w, double sca
 extern "C" mc_status mc_ctx_update_cells_warm(mc_ctx_t *c, const float *w, double scale, double xhi_limit,
                                              int32_t precision, mc_update_stats_t *stats) {
   return update_cells_impl(c, w, scale, xhi_limit, precision, true, stats);
+}
+
+extern "C" mc_status mc_ctx_set_grain_physics(mc_ctx_t *c, const mc_grain_physics_t *gp) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  c->g_fresh = false;
+  if (!gp) { c->g_ns = 0; return MC_OK; }
+  const int ns = gp->nsizes, nb = c->nb, nc1 = c->nc + 1;
+  if (ns < 1 || ns > 32) return set_error(MC_ERR_ARG, "grain nsizes must be 1..32 (got %d)", ns);
+  if (!gp->xs_abs || !gp->radius_um || !gp->weight || !gp->ion_nu || !gp->ndust)
+    return set_error(MC_ERR_ARG, "grains: xs_abs, radius_um, weight, ion_nu and ndust are required");
+  if (!(gp->vn >= 0.) || !(gp->msurf > 0.)) return set_error(MC_ERR_ARG, "grains: vn >= 0 and msurf > 0 required");
+  for (int k = 0; k < ns; ++k)
+    if (!(gp->radius_um[k] > 0.)) return set_error(MC_ERR_ARG, "grains: radius %d must be > 0", k);
+  if (!c->nu.p) return set_error(MC_ERR_ARG, "the context has no frequency grid");
+  std::vector<float> nu(nb);
+  MC_CUDA(cudaMemcpy(nu.data(), c->nu.p, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost));
+  // the per-bin factors of the grain sums that do not depend on the
+  // potential: yield Yn = min(Y0 (1 - Vn/nu), Y1) (Y0 = 0.5, Y1 = 0.2,
+  // update_mod.f90:20), nu - Vn, and Qa = Cabs / (1e-8 a^2) per size
+  std::vector<double> ynd(nb), dnud(nb), qad((size_t)ns * nb), ihnu(nb);
+  std::vector<float> ynf(nb), dnuf(nb), qaf((size_t)ns * nb), idnuf(nb);
+  const double vn = gp->vn;
+  for (int i = 0; i < nb; ++i) {
+    const double v = (double)nu[i];
+    ynd[i] = std::min(0.5 * (1. - vn / v), 0.2);
+    dnud[i] = v - vn;
+    ihnu[i] = 1. / (2.1799153e-11 * v);
+    ynf[i] = (float)ynd[i];
+    dnuf[i] = (float)dnud[i];
+    idnuf[i] = 1.f / dnuf[i];
+  }
+  for (int k = 0; k < ns; ++k) {
+    const double r = gp->radius_um[k], qden = 1.e-8 * (r * r);
+    for (int i = 0; i < nb; ++i) {
+      qad[(size_t)k * nb + i] = (double)gp->xs_abs[(size_t)k * nb + i] / qden;
+      qaf[(size_t)k * nb + i] = (float)qad[(size_t)k * nb + i];
+    }
+  }
+  cudaStream_t s = c->stream;
+  mc_status st;
+  if ((st = put_buf(c->g_nu, nu.data(), (size_t)nb * 4, s)) ||
+      (st = put_buf(c->g_xs, gp->xs_abs, (size_t)ns * nb * 4, s)) ||
+      (st = put_buf(c->g_rad, gp->radius_um, (size_t)ns * 8, s)) ||
+      (st = put_buf(c->g_w, gp->weight, (size_t)ns * 8, s)) ||
+      (st = put_buf(c->g_ip, gp->ion_nu, 33 * 8, s)) ||
+      (st = put_buf(c->g_ynd, ynd.data(), (size_t)nb * 8, s)) ||
+      (st = put_buf(c->g_dnud, dnud.data(), (size_t)nb * 8, s)) ||
+      (st = put_buf(c->g_qad, qad.data(), qad.size() * 8, s)) ||
+      (st = put_buf(c->g_ynf, ynf.data(), (size_t)nb * 4, s)) ||
+      (st = put_buf(c->g_dnuf, dnuf.data(), (size_t)nb * 4, s)) ||
+      (st = put_buf(c->g_qaf, qaf.data(), qaf.size() * 4, s)) ||
+      (st = put_buf(c->g_nd, gp->ndust, (size_t)nc1 * 4, s)) ||
+      (st = put_buf(c->g_ihnu, ihnu.data(), (size_t)nb * 8, s)) ||
+      (st = put_buf(c->g_idnuf, idnuf.data(), (size_t)nb * 4, s)))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(s));
+  // the first bin above Vn (locate's 1-based index of the last bin <= Vn)
+  int ivn = 0;
+  if (vn > (double)nu[nb - 1]) ivn = nb;
+  else if (vn >= (double)nu[0])
+    while (ivn < nb && !((double)nu[ivn] > vn)) ++ivn;
+  c->g_ivn = ivn;
+  c->g_ns = ns;
+  c->g_vn = vn;
+  c->g_msurf = gp->msurf;
+  c->g_abun = gp->abundance;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_grain_state(mc_ctx_t *c, double *potential, double *photoel_cool, double *coll_heat) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  if (c->g_ns <= 0 || !c->g_fresh) return set_error(MC_ERR_ARG, "no update with grains has run");
+  const size_t n = (size_t)c->g_ns * (c->nc + 1);
+  double *dst[3] = {potential, photoel_cool, coll_heat};
+  for (int q = 0; q < 3; ++q)
+    if (dst[q]) MC_CUDA(cudaMemcpyAsync(dst[q], c->g_out.as<double>() + q * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
 }
 
 // ------------------------------------------------------------ surrogate

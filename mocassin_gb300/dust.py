@@ -16,6 +16,8 @@ import numpy as np
 from . import nebula
 
 NTEMPS = 3000                      # constants_mod.f90:55
+GRAIN_VN = 0.588                   # grainVn [Ryd] of the silicate of dustData/sil-dlee.nk
+GRAIN_MSURF = 20.077               # MsurfAtom of the same file (ph_mod.f90:910-911)
 HPLANCK = 6.6262e-27               # constants_mod.f90:14
 FR1RYD = 3.28984e15                # constants_mod.f90:13
 HCRYD_K = 157893.94                # continuum_mod.f90:10
@@ -62,3 +64,21 @@ def emission_table(xs_abs, nu):
 def absorption_weights(xs_abs):
     """Moment weights [nbins, nsizes]: xSecAbs / pi."""
     return np.ascontiguousarray((xs_abs / np.pi).T.astype(np.float32))
+
+
+def grain_physics(neb, abundance=1.0):
+    """The grains of the photoelectric and gas-grain collision terms of the
+    cell update (setGrainPotential, setPhotoelHeatCool,
+    setDustGasCollHeatCool, source/update_mod.f90:527-930): the absorption
+    cross-sections per grain [nsizes][nbins] (FP32, as the opacity and the
+    grain temperatures use them), radii [um], number weights, the species
+    abundance, grainVn and MsurfAtom, the frequency grid and the threshold
+    of every balance ion (the first bin with a nonzero cross-section, the
+    same IP as the heating sums), and Ndust per cell."""
+    from . import balance
+    xs, w, a = grains(neb.nu)
+    ions = [tuple(int(v) for v in r) for r in nebula.atomic_table()["ions"]]
+    return {"xs_abs": np.ascontiguousarray(xs.astype(np.float32)), "radius_um": a * 1e4, "weight": w,
+            "abundance": float(abundance), "vn": GRAIN_VN, "msurf": GRAIN_MSURF,
+            "nu": neb.nu.astype(np.float64), "ion_nu": balance.ion_thresholds(neb.xs, neb.nu, ions),
+            "ndust": np.ascontiguousarray(neb.ndust, dtype=np.float32)}

@@ -20,7 +20,12 @@ On a grid with grains the grain temperatures (getDustT) follow the update,
 the grains' opacity (Ndust x (abs + sca) per grain, the dust add of
 iteration_mod.f90:166-227) is added to every opacity rebuild, and their
 thermal emission joins the recPDF rows.  The grains keep their opacity above
-the sublimation temperature (the reference drops it there).
+the sublimation temperature (the reference drops it there).  With
+``photoelectric`` (lgPhotoelectric, on by default in the reference) every T
+step of the update also charges the grains and adds the photoelectric
+heating and the gas-grain collisional cooling to the gas (setGrainPotential,
+setPhotoelHeatCool, setDustGasCollHeatCool, update_mod.f90:527-930), and the
+grain temperatures take the matching terms (getDustT :1886-1889).
 
 ``form`` picks the transport ("graph": the frequency-sorted persistent march
 with its rounds in one CUDA graph; "wave": the same with host-driven rounds;
@@ -46,7 +51,7 @@ class LambdaIteration:
     """A nebula resident on the GPU with its cell state."""
 
     def __init__(self, neb, form="graph", update="fp32", xhi_limit=0.05, opacity_method="bf16x3", surrogate=None,
-                 emission="auto", march="fp32"):
+                 emission="auto", march="fp32", photoelectric=True):
         """surrogate: None (updates start from the previous state, as the
         reference's) or a dict with train_after (cold iterations whose cell
         states train the MLP first; None: never), steps, batch, lr,
@@ -71,6 +76,8 @@ class LambdaIteration:
             xs_abs, gw, _ = dust.grains(neb.nu)
             self.dust = (dust.absorption_weights(xs_abs), dust.emission_table(xs_abs, neb.nu), gw)
             self.ctx.set_fixed_opacity(neb.ndust, neb.dust_kappa)
+            if photoelectric:
+                self.ctx.set_grain_physics(dust.grain_physics(neb))
         if emission == "auto":
             emission = True
         self.emission = bool(emission)

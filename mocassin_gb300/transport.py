@@ -111,6 +111,10 @@ def library():
         lib.mc_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.mc_ctx_get_tuning.restype = C.c_int
         lib.mc_ctx_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        lib.mc_ctx_set_grain_physics.restype = C.c_int
+        lib.mc_ctx_set_grain_physics.argtypes = [C.c_void_p, C.POINTER(abi.McGrainPhysics)]
+        lib.mc_ctx_grain_state.restype = C.c_int
+        lib.mc_ctx_grain_state.argtypes = [C.c_void_p, dp, dp, dp]
         lib.mc_ctx_dust_temperatures.restype = C.c_int
         lib.mc_ctx_dust_temperatures.argtypes = [C.c_void_p, C.c_int32, fp, fp, C.c_int32, fp, C.c_double, fp, dp]
         lib.mc_ctx_get_opacity.restype = C.c_int
@@ -428,6 +432,28 @@ class TransportContext:
         _check(self.lib.mc_ctx_dust_temperatures(self.handle, nsizes, _fptr(w_abs), _fptr(em), em.shape[1], _fptr(gw),
                                                  float(scale), _fptr(out), C.byref(ms)))
         return out, ms.value
+
+    def set_grain_physics(self, grains):
+        """Grains in the gas update (photoelectric heating and gas-grain
+        collisions, update_mod.f90:527-930) from the description of
+        dust.grain_physics; None: a gas-only update again."""
+        if grains is None:
+            _check(self.lib.mc_ctx_set_grain_physics(self.handle, None))
+            self._grains = None
+            return
+        s = abi.grain_physics_struct(grains)
+        _check(self.lib.mc_ctx_set_grain_physics(self.handle, C.byref(s)))
+        self._grains = int(s.nsizes)
+
+    def grain_state(self):
+        """(potential [Ryd], photoelHeat_d, gasDustColl_d), each [nsizes][Nc+1],
+        of every cell's last T step in the last update with grains."""
+        ns = getattr(self, "_grains", None)
+        if not ns:
+            raise TransportError(1, "no grain physics set")
+        out = [np.empty((ns, self.neb.ncells + 1)) for _ in range(3)]
+        _check(self.lib.mc_ctx_grain_state(self.handle, *[o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]))
+        return tuple(out)
 
     def get_opacity(self):
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)

@@ -2,7 +2,7 @@
 // mocassin's per-cell gas update, used to check the GPU cell-update kernel.
 // Nothing in the product links or calls this file.
 //
-// Follows, for a gas-only cell with the debug field off (nPhotoDif unused):
+// Follows, for a cell with the debug field off (nPhotoDif unused):
 //   updateCell     source/update_mod.f90:15-335 (lgHit, state set-up)
 //   iterateT       source/update_mod.f90:339-525 (bracketed secant in Te)
 //   ionBalance     source/update_mod.f90:1320-1622 (photo + collisional
@@ -20,6 +20,12 @@
 //   luSlv          source/emission_mod.f90:2119-2190 (no pivoting)
 //   spline/splint  source/interpolation_mod.f90:182-311 (natural spline)
 //   getOuterShell  source/hydro_mod.f90:89-182 (statistical weights)
+// and, in a cell with gas and grains (lgPhotoelectric, the default):
+//   setGrainPotential / getGrainEmission / getGrainRecombination
+//                  source/update_mod.f90:527-741 (grain charge balance)
+//   setPhotoelHeatCool      :745-806 (photoelectric gas heating, grain cooling)
+//   setDustGasCollHeatCool  :810-930 (gas-grain collisions)
+//   called per T step at :367-386 and added in thermBalance :1251-1254
 // for the elements H, He, C, N, O, Ne, S (nstages = 7).  The reference
 // computes in 4-byte `real` with a few double-precision arrays; this is the
 // FP64 restatement.  Photoionisation sums nPhotoSte (without the 1e-20
@@ -67,6 +73,20 @@ struct upd_tables_t {
   const double *cel_ad;      // [ncel][5]
 };
 
+// The grains of a dusty gas cell (one species in nsizes size bins), for the
+// photoelectric and gas-grain collision terms of the update.
+struct upd_grains_t {
+  int32_t nsizes, nbins;
+  const double *nu;         // [nbins] frequency grid [Ryd]
+  const double *xs_abs;     // [nsizes][nbins] absorption cross-section per grain [cm^2]
+  const double *radius_um;  // [nsizes] grainRadius [um]
+  const double *weight;     // [nsizes] grainWeight
+  double abundance;         // grainAbun of the species
+  double vn;                // grainVn [Ryd]
+  double msurf;             // MsurfAtom
+  const double *ion_nu;     // [33] threshold energy of each balance ion [Ryd]
+};
+
 }  // extern "C"
 
 namespace {
@@ -84,6 +104,15 @@ struct Cell {
   double thResHigh = 0, thResLow = 0, Thigh = 0, Tlow = 0;
   bool ionConv = true;
   int noTeBal = 0, noIonBal = 0;
+  // grains (null: a gas-only cell): this cell's Jste x scale [nbins], grains
+  // per cm^3, the grain temperatures of the previous iteration [nsizes]
+  const upd_grains_t *g = nullptr;
+  const double *J = nullptr;
+  double ndust = 0.;
+  const double *tdust = nullptr;
+  double photoG = 0., collG = 0.;       // photoelHeat_g, gasDustColl_g
+  double vg[32], photoD[32], collD[32];  // grainPot, photoelHeat_d, gasDustColl_d
+  bool gcConv = true;                   // every grain potential converged (last T step)
 
   static int nion(int e) { return std::min(kZ[e], kNS - 1); }  // ion 1..min(elem, nstages-1)
   static int nstage(int e) { return std::min(kZ[e] + 1, kNS); }
@@ -356,6 +385,212 @@ struct Cell {
     return cool;
   }
 
+  // ---- grains: setGrainPotential, getGrainEmission, getGrainRecombination,
+  // setPhotoelHeatCool, setDustGasCollHeatCool (update_mod.f90:527-930)
+  //
+  // Sums over frequency are formed in the order of the GPU's warp (lane l
+  // adds the terms of the bins i = l mod 32, i >= i0, in ascending order,
+  // then the 32 partial sums are combined by the xor butterfly over offsets
+  // 16, 8, 4, 2, 1), and so is the sum of the 33 ion currents in the
+  // recombination rate (ion pair b in lane b mod 32); the sums over grain
+  // sizes of the two gas terms go size by size after each size's own sum.
+  // The reference adds the same terms one by one; only the rounding differs.
+  template <class F>
+  static double warpSum(int i0, int n, F term) {
+    double p[32], q[32];
+    for (int l = 0; l < 32; ++l) {
+      p[l] = 0.;
+      for (int i = i0 + ((l - i0) & 31); i < n; i += 32) p[l] += term(i);
+    }
+    for (int o = 16; o; o >>= 1) {
+      for (int l = 0; l < 32; ++l) q[l] = p[l] + p[l ^ o];
+      std::memcpy(p, q, sizeof p);
+    }
+    return p[0];
+  }
+
+  // interpolation_mod locate (1-based): n above the grid, 0 below it, else
+  // the last entry <= x, and 1 where no entry exceeds x
+  static int locate(const double *xa, int n, double x) {
+    if (x > xa[n - 1]) return n;
+    if (x < xa[0]) return 0;
+    int lo = 0, hi = n;  // first index with xa > x (0-based), n if none
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (xa[m] > x) hi = m;
+      else lo = m + 1;
+    }
+    return lo == n ? 1 : (lo > 1 ? lo : 1);
+  }
+
+  static constexpr double kPi = 3.141592654, kFourPi = 4. * 3.141592654, kHcRyd = 2.1799153e-11;
+  static constexpr double kY0 = 0.5, kY1 = 0.2, kAmu = 1.66053e-24, kMe = 9.109382e-28;
+  static constexpr double kRyd2erg = 2.1799e-11, kBoltz = 1.380658e-16;
+  static double aWeight(int e) {
+    static const double w[kNE] = {1.0080, 4.0026, 12.0111, 14.0067, 15.9994, 20.179, 32.06};
+    return w[e];
+  }
+
+  // getGrainEmission (:610-663): photoelectrons per second from a grain of
+  // size k at potential Vg [Ryd], the field above max(Vn + Vg, Vn)
+  double grainEmission(int k, double Vg) const {
+    const double vn = g->vn, *nu = g->nu, *xs = g->xs_abs + (size_t)k * g->nbins;
+    const double r = g->radius_um[k], qden = 1.e-8 * (r * r);
+    const double thres = std::max(vn + Vg, vn);
+    const int ip = locate(nu, g->nbins, thres);  // the loop starts at ip + 1 (1-based)
+    return warpSum(ip, g->nbins, [&](int i) {
+      const double Yn = std::min(kY0 * (1. - vn / nu[i]), kY1);
+      const double Yhat = Yn * std::min(1., std::max(0., 1. - Vg / (nu[i] - vn)));
+      double photFlux = J[i] / (kHcRyd * nu[i]);
+      photFlux = photFlux * kFourPi;
+      const double Qa = xs[i] / qden;
+      return Yhat * photFlux * Qa;
+    });
+  }
+
+  // getGrainRecombination (:669-741): electron minus ion capture rate at Vg
+  double grainRecombination(double Vg) const {
+    const double kT = 6.336e-6 * Te, eightkT_pi = (1.1045e-15) * Te / kPi;
+    double vmean = std::sqrt(eightkT_pi / kMe);
+    double eta = -Vg / kT;
+    eta = eta <= 0. ? 1. - eta : std::exp(-eta);
+    const double rec = 0. + Ne * vmean * 1. * eta;
+    double term[33];
+    int b = 0;
+    for (int e = 0; e < kNE; ++e)
+      for (int s = 2; s <= nstage(e); ++s, ++b) {
+        const double cpDen = X[e][s] * ab[e] * hden;
+        const double mcp = aWeight(e) * kAmu;
+        vmean = std::sqrt(eightkT_pi / mcp);
+        const double Z = (double)(s - 1);
+        double et = Z * Vg / kT;
+        et = et <= 0. ? 1. - et : std::exp(-et);
+        term[b] = cpDen * vmean * 1. * et;
+      }
+    return rec - warpSum(0, 33, [&](int i) { return term[i]; });
+  }
+
+  // setGrainPotential (:527-604) as a loop: from Vg = 0 a secant in Vg on
+  // emission - recombination, steps at most 5 % of the threshold, until the
+  // two agree within 0.5 % of their mean or after maxIterateGC = 100
+  // evaluations.  `slope` is a `save` variable in the reference; here it
+  // carries over the sizes of one T step of one cell, starting at 0.
+  double grainPotential(int k, double &slope, bool &conv) const {
+    const double errorLim = 0.005, dm = 0.05, vn = g->vn;
+    double Vg = 0., VgOld = 0., emiOld = grainEmission(k, 0.), recOld = grainRecombination(0.);
+    Vg = VgOld + 0.05;
+    for (int n = 1;; ++n) {
+      const double threshold = std::max(vn + Vg, vn);
+      const double emi = grainEmission(k, Vg), rec = grainRecombination(Vg);
+      double delta = emi - rec;
+      double delta1 = std::fabs(delta / (0.5 * std::max(1.e-35, emi + rec)));
+      if (delta1 < errorLim) return Vg;
+      if (Vg != VgOld) {
+        const double fac = (emi - emiOld) - (rec - recOld);
+        if (fac != 0.) slope = fac / (Vg - VgOld);
+      }
+      VgOld = Vg;
+      recOld = rec;
+      emiOld = emi;
+      delta1 = -delta / slope;
+      delta = std::fabs(delta1);
+      delta = std::min(delta, dm * threshold);
+      delta = std::copysign(delta, delta1);
+      Vg = Vg + delta;
+      if (n >= 100) { conv = false; return Vg; }
+    }
+  }
+
+  // setPhotoelHeatCool (:745-806): the grains' photoelectric cooling per
+  // size and the gas heating per H
+  void photoelHeatCool() {
+    const double vn = g->vn, *nu = g->nu;
+    photoG = 0.;
+    for (int k = 0; k < g->nsizes; ++k) {
+      const double Vg = vg[k], *xs = g->xs_abs + (size_t)k * g->nbins;
+      const double th = std::max(vn + Vg, vn);
+      int thP = locate(nu, g->nbins, th);
+      if (thP <= 0) thP = 1;
+      auto pieces = [&](int i, double &Qflux, double &EY, double &Yhat) {
+        const double Yn = std::min(kY0 * (1. - vn / nu[i]), kY1);
+        Yhat = Yn * std::min(1., std::max(0., 1. - Vg / (nu[i] - vn)));
+        const double photFlux = J[i] / (kHcRyd * nu[i]);
+        const double Qa = xs[i];
+        const double d = nu[i] - vn;
+        EY = Yn * 0.5 * std::min(d, std::max(0., (d * d - Vg * Vg) / d));
+        Qflux = Qa * photFlux;
+      };
+      photoD[k] = warpSum(thP - 1, g->nbins, [&](int i) {
+        double Qf, EY, Yh;
+        pieces(i, Qf, EY, Yh);
+        return Qf * EY * kHcRyd / kPi;
+      });
+      const double gk = warpSum(thP - 1, g->nbins, [&](int i) {
+        double Qf, EY, Yh;
+        pieces(i, Qf, EY, Yh);
+        return Qf * (EY - Yh * Vg) * g->abundance * g->weight[k];
+      });
+      photoG = photoG + gk;
+    }
+    photoG = photoG * ndust * kHcRyd / hden;
+  }
+
+  // setDustGasCollHeatCool (:810-930): collisions of the gas particles
+  // (every stage of every element, then electrons) with the grains.  IPerg
+  // of a neutral stage is the value left from the element before it, as in
+  // the reference (an unset local there for H0, taken as 0 here).
+  void dustGasColl() {
+    const int ns = g->nsizes;
+    const double kT = 6.336e-6 * Te, eightkT_pi = (1.1045e-15) * Te / kPi;
+    double cg[32];
+    for (int k = 0; k < ns; ++k) { collD[k] = 0.; cg[k] = 0.; }
+    double IPerg = 0.;
+    for (int e = 0; e < kNE; ++e)
+      for (int s = 1; s <= nstage(e); ++s) {
+        const double Z = (double)(s - 1);
+        const double mcp = aWeight(e) * kAmu;
+        const double vmean = std::sqrt(eightkT_pi / mcp);
+        if (s > 1) IPerg = g->ion_nu[bidx(e, s - 1)] * kRyd2erg;
+        const double S = s == 1 ? 2. * mcp * g->msurf / ((mcp + g->msurf) * (mcp + g->msurf)) : 1.;
+        for (int k = 0; k < ns; ++k) {
+          const double r = g->radius_um[k], Vg = vg[k], Td = tdust ? tdust[k] : 0.;
+          const double psi = Z * Vg / kT;
+          double eta, xi;
+          if (psi <= 0.) { eta = 1. - psi; xi = 1. - psi / 2.; }
+          else { eta = std::exp(-psi); xi = (1. + psi / 2.) * eta; }
+          collD[k] = collD[k] + X[e][s] * ab[e] * hden * kPi * r * r * 1.e-8 * S * vmean *
+                                    (2. * kT * kRyd2erg * xi - eta * (Z * Vg * kRyd2erg - IPerg + 2. * kBoltz * Td));
+          cg[k] = cg[k] + X[e][s] * g->weight[k] * g->abundance * ndust * ab[e] * kPi * r * r * 1.e-8 * S * vmean *
+                              (2. * kT * kRyd2erg * xi - eta * 2. * kBoltz * Td);
+        }
+      }
+    const double vmean = std::sqrt(eightkT_pi / kMe);
+    for (int k = 0; k < ns; ++k) {
+      const double r = g->radius_um[k], Vg = vg[k];
+      const double S = 1., Z = -1.;
+      const double psi = Z * Vg / kT;
+      double eta, xi;
+      if (psi <= 0.) { eta = 1. - psi; xi = 1. - psi / 2.; }
+      else { eta = std::exp(-psi); xi = (1. + psi / 2.) * eta; }
+      collD[k] = collD[k] + Ne * kPi * r * r * 1.e-8 * S * vmean * (2. * kT * kRyd2erg * xi - eta * (Z * Vg * kRyd2erg));
+      cg[k] = cg[k] + Ne * g->weight[k] * g->abundance * ndust * kPi * r * r * 1.e-8 * S * vmean *
+                          (2. * kT * kRyd2erg * xi) / hden;
+    }
+    collG = 0.;
+    for (int k = 0; k < ns; ++k) collG = collG + cg[k];
+    for (int k = 0; k < ns; ++k) collD[k] = collD[k] / kFourPi;
+    collG = collG / kFourPi;
+  }
+
+  // the grain block of one T step (iterateT :367-386)
+  void grainTerms() {
+    double slope = 0.;
+    gcConv = true;
+    for (int k = 0; k < g->nsizes; ++k) vg[k] = grainPotential(k, slope, gcConv);
+    photoelHeatCool();
+    dustGasColl();
+  }
+
   void thermBalance(double &heatInt, double &coolInt) {
     const double kB = 1.380658e-16, hcRyd = 2.1799153e-11;
     const double log10Te = std::log10(Te), Te4 = Te / 1.e4;
@@ -393,6 +628,10 @@ struct Cell {
       for (int ion = 1; ion <= nion(e); ++ion) heatSte += heat[bidx(e, ion)] * X[e][ion] * ab[e];
     heatInt = heatSte;
     coolInt = coolFF + coolRec + coolColl;
+    if (g) {
+      coolInt = coolInt + collG;
+      heatInt = heatInt + photoG;
+    }
   }
 
   // iterateT as a loop (the recursion re-enters with the new TeUsed)
@@ -402,6 +641,7 @@ struct Cell {
       calcAlpha();
       nIterX = 1;
       ionBalance();
+      if (g) grainTerms();
       double heatInt, coolInt;
       thermBalance(heatInt, coolInt);
       const double thResidual = heatInt - coolInt;
@@ -444,10 +684,20 @@ extern "C" {
 // O Ne S, stage index 1..7); photo / heat: [Nc+1][33] balance-ion sums (Jste
 // normalised, nPhotoSte without the 1e-20 floor); hit: cell was reached by a
 // packet.  Outputs per cell: te, ne, ionden, conv (|dX(H0)/X(H0)| <= xhi_limit),
-// niter (T iterations), flags (1 = no T balance, 2 = no ion balance).
-int oracle_update_cells(const upd_tables_t *t, int32_t ncells, const double *abund, const double *hden,
-                        const double *photo, const double *heat, const int32_t *hit, double xhi_limit, double *te,
-                        double *ne, double *ionden, int32_t *conv, int32_t *niter, int32_t *flags, int32_t nthreads) {
+// niter (T iterations), flags (1 = no T balance, 2 = no ion balance, 8 = a
+// grain potential did not converge in the last T step).
+//
+// With grains (g non-null): jste [nbins][Nc+1] is the normalised Jste
+// (x scale), ndust [Nc+1] the grains per cm^3, tdust [nsizes][Nc+1] the
+// grain temperatures of the previous iteration (null: 0 K); gout
+// [3][nsizes][Nc+1] receives each cell's grain potential [Ryd],
+// photoelHeat_d and gasDustColl_d of its last T step.
+static void update_cells_impl(const upd_tables_t *t, int32_t ncells, const double *abund, const double *hden,
+                              const double *photo, const double *heat, const int32_t *hit, double xhi_limit,
+                              double *te, double *ne, double *ionden, int32_t *conv, int32_t *niter, int32_t *flags,
+                              int32_t nthreads, const upd_grains_t *g, const double *jste, const double *ndust,
+                              const double *tdust, double *gout) {
+  const size_t nc1 = (size_t)ncells + 1;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 64)
@@ -462,6 +712,18 @@ int oracle_update_cells(const upd_tables_t *t, int32_t ncells, const double *abu
     C.heat = heat + (size_t)c * 33;
     C.Te = te[c];
     C.Ne = ne[c];
+    std::vector<double> jrow, trow;
+    if (g) {
+      jrow.resize(g->nbins);
+      for (int i = 0; i < g->nbins; ++i) jrow[i] = jste[(size_t)i * nc1 + c];
+      trow.assign(g->nsizes, 0.);
+      if (tdust)
+        for (int k = 0; k < g->nsizes; ++k) trow[k] = tdust[(size_t)k * nc1 + c];
+      C.g = g;
+      C.J = jrow.data();
+      C.ndust = ndust[c];
+      C.tdust = trow.data();
+    }
     double *X = ionden + (size_t)c * kNE * (kNS + 1);
     for (int e = 0; e < kNE; ++e)
       for (int s = 0; s <= kNS; ++s) C.X[e][s] = X[e * (kNS + 1) + s];
@@ -473,8 +735,69 @@ int oracle_update_cells(const upd_tables_t *t, int32_t ncells, const double *abu
       for (int s = 0; s <= kNS; ++s) X[e * (kNS + 1) + s] = C.X[e][s];
     conv[c] = std::fabs((C.X[0][1] - XOldHI) / XOldHI) <= xhi_limit ? 1 : 0;
     niter[c] = C.nIterT;
-    flags[c] = (C.noTeBal ? 1 : 0) | (C.noIonBal ? 2 : 0);
+    flags[c] = (C.noTeBal ? 1 : 0) | (C.noIonBal ? 2 : 0) | (g && !C.gcConv ? 8 : 0);
+    if (g)
+      for (int k = 0; k < g->nsizes; ++k) {
+        gout[((size_t)0 * g->nsizes + k) * nc1 + c] = C.vg[k];
+        gout[((size_t)1 * g->nsizes + k) * nc1 + c] = C.photoD[k];
+        gout[((size_t)2 * g->nsizes + k) * nc1 + c] = C.collD[k];
+      }
   }
+}
+
+int oracle_update_cells(const upd_tables_t *t, int32_t ncells, const double *abund, const double *hden,
+                        const double *photo, const double *heat, const int32_t *hit, double xhi_limit, double *te,
+                        double *ne, double *ionden, int32_t *conv, int32_t *niter, int32_t *flags, int32_t nthreads) {
+  update_cells_impl(t, ncells, abund, hden, photo, heat, hit, xhi_limit, te, ne, ionden, conv, niter, flags,
+                    nthreads, nullptr, nullptr, nullptr, nullptr, nullptr);
+  return 0;
+}
+
+int oracle_update_cells_grains(const upd_tables_t *t, int32_t ncells, const double *abund, const double *hden,
+                               const double *photo, const double *heat, const int32_t *hit, double xhi_limit,
+                               double *te, double *ne, double *ionden, int32_t *conv, int32_t *niter,
+                               int32_t *flags, int32_t nthreads, const upd_grains_t *g, const double *jste,
+                               const double *ndust, const double *tdust, double *gout) {
+  if (!g || g->nsizes < 1 || g->nsizes > 32 || !jste || !ndust || !gout) return 1;
+  update_cells_impl(t, ncells, abund, hden, photo, heat, hit, xhi_limit, te, ne, ionden, conv, niter, flags,
+                    nthreads, g, jste, ndust, tdust, gout);
+  return 0;
+}
+
+// The grain block at a fixed state of one cell (Te, Ne, ionden [7][8],
+// Jste x scale [nbins], tdust [nsizes]): out[0][k] potential, out[1][k]
+// photoelHeat_d, out[2][k] gasDustColl_d; gas[0] photoelHeat_g, gas[1]
+// gasDustColl_g, gas[2] 1 if every potential converged; emi_rec[k][2] the
+// emission and recombination rates at each size's final potential.
+int oracle_grain_pieces(const upd_grains_t *g, const double *abund, double hden, double te, double ne,
+                        const double *ionden, const double *jrow, double ndust, const double *tdust, double *out,
+                        double *gas, double *emi_rec) {
+  if (!g || g->nsizes < 1 || g->nsizes > 32) return 1;
+  Cell C;
+  C.t = nullptr;
+  C.ab = abund;
+  C.hden = hden;
+  C.photo = nullptr;
+  C.heat = nullptr;
+  C.Te = te;
+  C.Ne = ne;
+  for (int e = 0; e < kNE; ++e)
+    for (int s = 0; s <= kNS; ++s) C.X[e][s] = ionden[e * (kNS + 1) + s];
+  C.g = g;
+  C.J = jrow;
+  C.ndust = ndust;
+  C.tdust = tdust;
+  C.grainTerms();
+  for (int k = 0; k < g->nsizes; ++k) {
+    out[k] = C.vg[k];
+    out[g->nsizes + k] = C.photoD[k];
+    out[2 * g->nsizes + k] = C.collD[k];
+    emi_rec[2 * k] = C.grainEmission(k, C.vg[k]);
+    emi_rec[2 * k + 1] = C.grainRecombination(C.vg[k]);
+  }
+  gas[0] = C.photoG;
+  gas[1] = C.collG;
+  gas[2] = C.gcConv ? 1. : 0.;
   return 0;
 }
 

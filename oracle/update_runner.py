@@ -20,13 +20,40 @@ class UpdTables(C.Structure):
                 ("cel_e", _dp), ("cel_br", _dp), ("cel_z", _dp), ("cel_ar", _dp), ("cel_ad", _dp)]
 
 
+class UpdGrains(C.Structure):
+    _fields_ = [("nsizes", C.c_int32), ("nbins", C.c_int32), ("nu", _dp), ("xs_abs", _dp), ("radius_um", _dp),
+                ("weight", _dp), ("abundance", C.c_double), ("vn", C.c_double), ("msurf", C.c_double),
+                ("ion_nu", _dp)]
+
+
 def library():
     global _LIB
     if _LIB is None:
         _LIB = C.CDLL(build_oracle.build())
         _LIB.oracle_update_cells.restype = C.c_int
         _LIB.oracle_update_pieces.restype = C.c_int
+        _LIB.oracle_update_cells_grains.restype = C.c_int
+        _LIB.oracle_grain_pieces.restype = C.c_int
     return _LIB
+
+
+def marshal_grains(gp):
+    """UpdGrains from the grain description of mocassin_gb300.dust.grain_physics
+    (xs_abs [nsizes][nbins], radius_um, weight, abundance, vn, msurf, nu,
+    ion_nu), every array widened to FP64."""
+    keep = {}
+
+    def d(name):
+        a = np.ascontiguousarray(gp[name], dtype=np.float64)
+        keep[name] = a
+        return a.ctypes.data_as(_dp)
+
+    xs = np.asarray(gp["xs_abs"])
+    s = UpdGrains(nsizes=xs.shape[0], nbins=xs.shape[1], nu=d("nu"), xs_abs=d("xs_abs"), radius_um=d("radius_um"),
+                  weight=d("weight"), abundance=float(gp["abundance"]), vn=float(gp["vn"]),
+                  msurf=float(gp["msurf"]), ion_nu=d("ion_nu"))
+    s._keep = keep
+    return s
 
 
 def marshal(t):
@@ -79,9 +106,12 @@ def sums(jste, xs, nu, ions, scale):
     return photo, heat, hit
 
 
-def update_cells(tables, abund, hden, photo, heat, hit, te, ne, X, xhi_limit=0.05, threads=0):
+def update_cells(tables, abund, hden, photo, heat, hit, te, ne, X, xhi_limit=0.05, threads=0, grains=None):
     """Runs the oracle update on copies of (te, ne, X); returns
-    (te, ne, X, conv, niter, flags)."""
+    (te, ne, X, conv, niter, flags), and with grains = (grain_physics dict,
+    jste_scaled [nbins][Nc+1], ndust [Nc+1], tdust [nsizes][Nc+1] or None)
+    also the grain state [3][nsizes][Nc+1] (potential, photoelHeat_d,
+    gasDustColl_d of each cell's last T step)."""
     lib = library()
     t = marshal(tables)
     nc1 = len(te)
@@ -98,12 +128,50 @@ def update_cells(tables, abund, hden, photo, heat, hit, te, ne, X, xhi_limit=0.0
     flags = np.zeros(nc1, dtype=np.int32)
     p = lambda a: a.ctypes.data_as(_dp)
     q = lambda a: a.ctypes.data_as(_ip)
-    rc = lib.oracle_update_cells(C.byref(t), C.c_int32(nc1 - 1), p(ab), p(hden), p(photo), p(heat), q(hit),
-                                 C.c_double(xhi_limit), p(te), p(ne), p(X), q(conv), q(niter), q(flags),
-                                 C.c_int32(threads))
+    if grains is None:
+        rc = lib.oracle_update_cells(C.byref(t), C.c_int32(nc1 - 1), p(ab), p(hden), p(photo), p(heat), q(hit),
+                                     C.c_double(xhi_limit), p(te), p(ne), p(X), q(conv), q(niter), q(flags),
+                                     C.c_int32(threads))
+        if rc != 0:
+            raise RuntimeError("update oracle failed: %d" % rc)
+        return te, ne, X, conv, niter, flags
+    gp, js, nd, td = grains
+    g = marshal_grains(gp)
+    js = np.ascontiguousarray(js, dtype=np.float64)
+    nd = np.ascontiguousarray(nd, dtype=np.float64)
+    tdp = None
+    if td is not None:
+        td = np.ascontiguousarray(td, dtype=np.float64)
+        tdp = p(td)
+    gout = np.zeros((3, g.nsizes, nc1))
+    rc = lib.oracle_update_cells_grains(C.byref(t), C.c_int32(nc1 - 1), p(ab), p(hden), p(photo), p(heat), q(hit),
+                                        C.c_double(xhi_limit), p(te), p(ne), p(X), q(conv), q(niter), q(flags),
+                                        C.c_int32(threads), C.byref(g), p(js), p(nd), tdp, p(gout))
     if rc != 0:
         raise RuntimeError("update oracle failed: %d" % rc)
-    return te, ne, X, conv, niter, flags
+    return te, ne, X, conv, niter, flags, gout
+
+
+def grain_pieces(gp, abund, hden, te, ne, X, jrow, ndust, tdust=None):
+    """The grain block of one cell at a fixed state: (out [3][nsizes] =
+    potential, photoelHeat_d, gasDustColl_d; (photoelHeat_g, gasDustColl_g,
+    all converged); emi_rec [nsizes][2] at the final potentials)."""
+    lib = library()
+    g = marshal_grains(gp)
+    ns = g.nsizes
+    ab = np.ascontiguousarray(abund, dtype=np.float64)
+    Xc = np.ascontiguousarray(X, dtype=np.float64)
+    jr = np.ascontiguousarray(jrow, dtype=np.float64)
+    td = np.ascontiguousarray(np.zeros(ns) if tdust is None else tdust, dtype=np.float64)
+    out = np.zeros((3, ns))
+    gas = np.zeros(3)
+    er = np.zeros((ns, 2))
+    p = lambda a: a.ctypes.data_as(_dp)
+    rc = lib.oracle_grain_pieces(C.byref(g), p(ab), C.c_double(hden), C.c_double(te), C.c_double(ne), p(Xc), p(jr),
+                                 C.c_double(ndust), p(td), p(out), p(gas), p(er))
+    if rc != 0:
+        raise RuntimeError("grain oracle failed: %d" % rc)
+    return out, (gas[0], gas[1], bool(gas[2])), er
 
 
 def pieces(tables, abund, hden, photo, heat, te, ne, X):
