@@ -54,17 +54,21 @@ __device__ __forceinline__ int nstage_of(int z) { return z + 1 < kNS ? z + 1 : k
 // temperature range applies (rows listed on the host in file order),
 // replaced by the last matching Aldrovandi & Pequignot row above 60000 K or
 // where it is zero
+// (the last matching row is the one whose value stands, so the rows are
+// scanned from the end and the first match ends the scan)
 template <typename Real>
 __device__ Real direc_of(const UpdArgs &a, const int *rows, int nrows, int arow, Real Te) {
   const UpdTabs<Real> &T = tabs<Real>(a);
   const Real t = Te / (Real)10000.;
   Real d = 0., al = 0.;
-  for (int k = 0; k < nrows; ++k) {
+  for (int k = nrows - 1; k >= 0; --k) {
     const Real *r = T.direc + 8 * rows[k];
     const int g = (int)r[7];
-    if (g == 0 || (g == 1 && Te < (Real)20000.) || (g == 2 && Te >= (Real)20000.))
+    if (g == 0 || (g == 1 && Te < (Real)20000.) || (g == 2 && Te >= (Real)20000.)) {
       d = (Real)1e-12 * ((Real)r[2] / t + (Real)r[3] + (Real)r[4] * t + (Real)r[5] * t * t) * pow(t, (Real)-1.5) *
           exp(-(Real)r[6] / t);
+      break;
+    }
   }
   if (arow >= 0) {
     const Real *r = T.aldro + 6 * arow;

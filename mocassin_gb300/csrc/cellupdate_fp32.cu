@@ -71,8 +71,17 @@ __global__ void wave_init_kernel(const __grid_constant__ WaveArgs w) {
   }
 }
 
-// calcAlpha and ionBalance of every active cell at its current Te
-__global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ WaveArgs w, int cur) {
+// calcAlpha and ionBalance of every active cell at its current Te.  The
+// per-ion terms that stay fixed through the passes (photoionisation rate,
+// charge-exchange reverse rate, recombination coefficient, charge-exchange
+// rate x Hden) sit in shared memory, one column per thread, so the passes
+// keep only the ion fractions in registers.
+constexpr int kIonThreads = 64;
+__global__ void __launch_bounds__(kIonThreads) wave_ion_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  extern __shared__ float ion_sm[];
+  float *sP = ion_sm, *sRev = ion_sm + kNB * kIonThreads, *sAl = ion_sm + 2 * kNB * kIonThreads,
+        *sChh = ion_sm + 3 * kNB * kIonThreads;
+  const int t = threadIdx.x;
   const UpdArgs &a = w.a;
   const UpdTabs<float> &T = a.f;
   const int n = w.count[cur];
@@ -83,40 +92,34 @@ __global__ void __launch_bounds__(128) wave_ion_kernel(const __grid_constant__ W
     float X[kNE][kNX];
     for (int e = 0; e < kNE; ++e)
       for (int s = 0; s < kNX; ++s) X[e][s] = XS(w, e * kNX + s, c);
-    float alpha[kNB];
-    for (int b = 0; b < kNB; ++b) alpha[b] = alpha_of<float>(a, T.bal[b], Te);
     float Ne = w.Ne[c];
     float expFact = 157893.94f / Te;
     if (expFact > 75.f) expFact = 75.f;
     const float collIon0 = 2.75E-16f * Te * sqrtf(Te) * (157893.94f / Te + 2.f) * expf(-expFact);
     const float t4 = Te / 10000.f;
     // the charge-exchange rates depend on Te only
-    float ch[kNB], rev[kNB];
     for (int b = 0; b < kNB; ++b) {
       const UpdIonT<float> &B = T.bal[b];
       float x = B.chex[0] * powf(t4, B.chex[1]) * (1.f + B.chex[2] * expf(B.chex[3] * t4));
       if (x < 0.f) x = 0.f;
       if (Te < 6000.f || Te > 5.e4f) x = 0.f;
-      ch[b] = x;
-      rev[b] = B.dek > 1.f ? x * hden * 2.f * expf(-B.dek / Te) / B.g0g1 : 0.f;
+      sChh[b * kIonThreads + t] = x * hden;
+      sRev[b * kIonThreads + t] = B.dek > 1.f ? x * hden * 2.f * expf(-B.dek / Te) / B.g0g1 : 0.f;
+      sAl[b * kIonThreads + t] = alpha_of<float>(a, B, Te);
+      sP[b * kIonThreads + t] = a.mom[(size_t)(1 + b) * a.mstride + c] + 1e-20f + (b == 0 ? collIon0 : 0.f);
     }
     bool conv = true;
     for (int pass = 1;; ++pass) {
       conv = true;
       const float HIOld = X[0][1], HeIOld = X[1][1], HeIIOld = X[1][2];
-      float ratio[kNB];
-      for (int b = 0; b < kNB; ++b) {
-        const float P = a.mom[(size_t)(1 + b) * a.mstride + c] + 1e-20f;
-        const float collIon = b == 0 ? collIon0 : 0.f;
-        ratio[b] = (P + collIon + rev[b] * (1.f - HIOld)) / (Ne * alpha[b] + ch[b] * hden * HIOld);
-      }
       float ne = 0.f;
       for (int e = 0; e < kNE; ++e) {
         const int z = a.bal_z[e], b0 = a.bal_first[e], ni = nion_of(z), ns = nstage_of(z);
         float prod[kNS + 1];
         float p = 1.f, den = 1.f;
         for (int ion = 1; ion <= ni; ++ion) {
-          p *= ratio[b0 + ion - 1];
+          const int b = (b0 + ion - 1) * kIonThreads + t;
+          p *= (sP[b] + sRev[b] * (1.f - HIOld)) / (Ne * sAl[b] + sChh[b] * HIOld);
           prod[ion] = p;
           den += p;
         }
@@ -408,7 +411,7 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
   for (int t = 0; t < steps; ++t) {
     const int cur = t & 1;
     wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
-    wave_ion_kernel<<<blocks, 128, 0, stream>>>(w, cur);
+    wave_ion_kernel<<<blocks * 2, kIonThreads, 4 * kNB * kIonThreads * sizeof(float), stream>>>(w, cur);
     if (a.g.nsizes > 0) wave_grain_kernel<<<blocks, 128, grain_smem(a.g), stream>>>(w, cur);
     wave_cel_kernel<<<num_sms * cel_blocks_per_sm(), 128, 0, stream>>>(w, cur);
     wave_therm_kernel<<<blocks, 128, 0, stream>>>(w, cur);
