@@ -417,6 +417,15 @@ mc_status mc_ctx_grain_state(mc_ctx_t *ctx, double *potential, double *photoel_c
  * xs [nrows][nbins] (e.g. the grains' absorption + scattering per grain,
  * the dust add of iteration_mod.f90:166-227); nrows 0 removes them. */
 mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *ctx, int32_t nrows, const float *den, const float *xs);
+/* The grains' opacity in every mc_ctx_opacity_from_state (the dust add of
+ * iteration_mod.f90:166-227): per size bin k and cell, weight(k) Ndust x
+ * (xs_ext(k) = abs + sca per grain) joins the opacity and weight(k) Ndust x
+ * xs_sca(k) the scattering table (scaOpac), for the sizes whose grain
+ * temperature (the last mc_ctx_dust_temperatures; 0 K before the first) is
+ * below t_sublime (TdustSublime: sublimated grains drop out).  One species:
+ * weight = grainAbun x grainWeight.  nsizes 0 removes them. */
+mc_status mc_ctx_set_grain_opacity(mc_ctx_t *ctx, int32_t nsizes, const float *xs_ext, const float *xs_sca,
+                                   const float *weight, const float *ndust, float t_sublime);
 mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32_t *species, const float *xs,
                                     int32_t method, double *kernel_ms);
 
@@ -526,6 +535,8 @@ mc_status mc_ctx_get_tuning(mc_ctx_t *ctx, int32_t *refill_min, int32_t *inner_s
 
 /* Copies the resident opacity [nbins][Nc+1] (cell fastest) to the host. */
 mc_status mc_ctx_get_opacity(mc_ctx_t *ctx, float *opacity);
+/* The resident scattering table (scaOpac, the layout of opacity) of a dusty grid. */
+mc_status mc_ctx_get_scattering(mc_ctx_t *ctx, float *scattering);
 
 /* ---- allocation-free transport ------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

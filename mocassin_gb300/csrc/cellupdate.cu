@@ -57,7 +57,25 @@ __global__ void species_kernel(int nc, int nsp, const int *sp_e, const int *sp_s
   }
 }
 
+// the grains' rows of the opacity rebuild (iteration_mod.f90:193-210):
+// sublimated sizes drop out
+__global__ void grain_density_kernel(int nc1, int nsizes, const float *weight, const float *ndust, const float *tdust,
+                                     float t_sub, float *den) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)nsizes * nc1;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(i / nc1), c = (int)(i % nc1);
+    const bool keep = !tdust || tdust[(size_t)(1 + k) * nc1 + c] < t_sub;
+    den[i] = c == 0 || !keep ? 0.f : weight[k] * ndust[c];
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_grain_density(int nc1, int nsizes, const float *weight, const float *ndust, const float *tdust,
+                                 float t_sub, float *den, int num_sms, cudaStream_t stream) {
+  grain_density_kernel<<<num_sms * 4, 256, 0, stream>>>(nc1, nsizes, weight, ndust, tdust, t_sub, den);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int num_sms, cudaStream_t stream) {
   if (fp32) return launch_cell_update_fp32(a, scratch, num_sms, stream);

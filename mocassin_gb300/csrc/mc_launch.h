@@ -139,6 +139,10 @@ cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const
                                 UpdStatsDev *s, int num_sms, cudaStream_t stream);
 cudaError_t launch_species(int nc, int nsp, const int *sp_e, const int *sp_s, const double *X, const double *ab,
                            const double *hden, float *den, int num_sms, cudaStream_t stream);
+// den[k][cell] = weight(k) Ndust(cell) where the grain temperature of size k
+// is below t_sub (tdust [nsizes+1][nc1], rows 1..; null: every size), else 0
+cudaError_t launch_grain_density(int nc1, int nsizes, const float *weight, const float *ndust, const float *tdust,
+                                 float t_sub, float *den, int num_sms, cudaStream_t stream);
 void spline_natural(const double *x, const double *y, int n, double *y2);
 
 // ---- the learned warm start (mlp.cu) ----

@@ -164,8 +164,14 @@ struct mc_ctx {
   int g_ns = 0, g_ivn = 0;
   double g_vn = 0., g_msurf = 0., g_abun = 0.;
   bool g_fresh = false;  // g_out belongs to the last update
-  DBuf o_fix_den, o_fix_xs;  // opacity rows that do not follow the cell state (grains)
+  DBuf o_fix_den, o_fix_xs;  // opacity rows that do not follow the cell state
   int o_nfix = 0;
+  // the grains' opacity rows (mc_ctx_set_grain_opacity): cross-sections
+  // [nsizes][nbins] (abs + sca, sca), weights, Ndust, and the scattering
+  // table's densities of the last rebuild
+  DBuf go_ext, go_sca, go_w, go_nd, go_den;
+  int go_n = 0;
+  float go_tsub = 0.f;
   int d_nsizes = 0;
   mcg::EmiArgs emi{};
   bool e_ready = false;
@@ -2494,6 +2500,15 @@ extern "C" mc_status mc_ctx_get_opacity(mc_ctx_t *c, float *out) {
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_get_scattering(mc_ctx_t *c, float *out) {
+  if (!c || !out) return set_error(MC_ERR_ARG, "ctx and scattering are required");
+  if (!c->sca.p) return set_error(MC_ERR_ARG, "the grid has no scattering table");
+  MC_CUDA(cudaMemcpyAsync(out, c->sca.p, (size_t)(c->nc + 1) * c->nb * sizeof(float), cudaMemcpyDeviceToHost,
+                          c->stream));
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *c, int32_t nrows, const float *den, const float *xs) {
   if (!c || nrows < 0 || nrows > 16 || (nrows > 0 && (!den || !xs)))
     return set_error(MC_ERR_ARG, "ctx, 0..16 rows, den and xs are required");
@@ -2507,13 +2522,35 @@ extern "C" mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *c, int32_t nrows, const 
   return MC_OK;
 }
 
+extern "C" mc_status mc_ctx_set_grain_opacity(mc_ctx_t *c, int32_t nsizes, const float *xs_ext, const float *xs_sca,
+                                             const float *weight, const float *ndust, float t_sublime) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  if (nsizes == 0) { c->go_n = 0; return MC_OK; }
+  if (nsizes < 0 || nsizes > 32) return set_error(MC_ERR_ARG, "grain opacity: nsizes must be 0..32 (got %d)", nsizes);
+  if (!xs_ext || !xs_sca || !weight || !ndust) return set_error(MC_ERR_ARG, "grain opacity: arrays are required");
+  if (!c->sca.p) return set_error(MC_ERR_ARG, "grain opacity: the grid has no scattering table (not a dusty grid)");
+  if (!(t_sublime > 0.f)) return set_error(MC_ERR_ARG, "grain opacity: t_sublime must be > 0");
+  const int nc1 = c->nc + 1, nb = c->nb;
+  mc_status st;
+  if ((st = put_buf(c->go_ext, xs_ext, (size_t)nsizes * nb * sizeof(float), c->stream)) ||
+      (st = put_buf(c->go_sca, xs_sca, (size_t)nsizes * nb * sizeof(float), c->stream)) ||
+      (st = put_buf(c->go_w, weight, (size_t)nsizes * sizeof(float), c->stream)) ||
+      (st = put_buf(c->go_nd, ndust, (size_t)nc1 * sizeof(float), c->stream)) ||
+      (st = put_buf(c->go_den, nullptr, (size_t)nsizes * nc1 * sizeof(float), c->stream)))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  c->go_n = nsizes;
+  c->go_tsub = t_sublime;
+  return MC_OK;
+}
+
 extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, const int32_t *species,
                                               const float *xs, int32_t method, double *kernel_ms) {
   NvtxRange nvtx_range("mc opacity");
   if (!c || !species || !xs) return set_error(MC_ERR_ARG, "ctx, species and xs are required");
   if (!c->u_ready || !c->s_ready) return set_error(MC_ERR_ARG, "cell state or tables missing");
-  if (nspecies < 1 || nspecies + c->o_nfix > 64)
-    return set_error(MC_ERR_ARG, "nspecies must be 1..%d (got %d)", 64 - c->o_nfix, nspecies);
+  if (nspecies < 1 || nspecies + c->o_nfix + c->go_n > 64)
+    return set_error(MC_ERR_ARG, "nspecies must be 1..%d (got %d)", 64 - c->o_nfix - c->go_n, nspecies);
   if (method != MC_OPAC_FP32 && method != MC_OPAC_BF16X3) return set_error(MC_ERR_ARG, "unknown opacity method");
   std::vector<int32_t> se(nspecies), ss(nspecies);
   for (int k = 0; k < nspecies; ++k) {
@@ -2524,7 +2561,8 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
   const int nc1 = c->nc + 1, nb = c->nb;
   cudaStream_t s = c->stream;
   mc_status st;
-  const int nrows = nspecies + c->o_nfix;
+  const int nrows = nspecies + c->o_nfix + c->go_n;
+  const int g0 = nspecies + c->o_nfix;  // the grains' rows follow the fixed ones
   if ((st = put_buf(c->s_spe, se.data(), nspecies * sizeof(int32_t), s)) ||
       (st = put_buf(c->s_sps, ss.data(), nspecies * sizeof(int32_t), s)) ||
       (st = put_buf(c->s_xs, nullptr, (size_t)nrows * nb * sizeof(float), s)) ||
@@ -2539,6 +2577,9 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
     MC_CUDA(cudaMemcpyAsync(c->s_den.as<float>() + (size_t)nspecies * nc1, c->o_fix_den.p,
                             (size_t)c->o_nfix * nc1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
   }
+  if (c->go_n > 0)
+    MC_CUDA(cudaMemcpyAsync(c->s_xs.as<float>() + (size_t)g0 * nb, c->go_ext.p, (size_t)c->go_n * nb * sizeof(float),
+                            cudaMemcpyDeviceToDevice, s));
   MC_CUDA(cudaStreamSynchronize(s));  // xs is the caller's (pageable) array
   MC_CUDA(cudaMemsetAsync(c->s_err.p, 0, sizeof(int), s));
   cudaEvent_t e0, e1;
@@ -2547,12 +2588,24 @@ extern "C" mc_status mc_ctx_opacity_from_state(mc_ctx_t *c, int32_t nspecies, co
   MC_CUDA(cudaEventRecord(e0, s));
   cudaError_t e = mcg::launch_species(c->nc, nspecies, c->s_spe.as<int>(), c->s_sps.as<int>(), c->s_X.as<double>(),
                                       c->u_ab.as<double>(), c->u_hden.as<double>(), c->s_den.as<float>(), c->num_sms, s);
+  // the grains' densities from the grain temperatures (sublimated sizes drop out)
+  const float *tdust = (c->go_n > 0 && c->d_tdust.p && c->d_nsizes == c->go_n) ? c->d_tdust.as<float>() : nullptr;
+  if (e == cudaSuccess && c->go_n > 0)
+    e = mcg::launch_grain_density(nc1, c->go_n, c->go_w.as<float>(), c->go_nd.as<float>(), tdust, c->go_tsub,
+                                  c->s_den.as<float>() + (size_t)g0 * nc1, c->num_sms, s);
   if (e == cudaSuccess)
     e = mcg::launch_opacity(method, nc1, nrows, nb, c->s_den.as<float>(), c->s_xs.as<float>(), nullptr,
                             c->opacity.as<float>(), c->s_err.as<int>(), c->num_sms, s);
+  // and the scattering table of the grains that are left
+  if (e == cudaSuccess && c->go_n > 0)
+    e = mcg::launch_opacity(method, nc1, c->go_n, nb, c->s_den.as<float>() + (size_t)g0 * nc1, c->go_sca.as<float>(),
+                            nullptr, c->sca.as<float>(), c->s_err.as<int>(), c->num_sms, s);
   if (e == cudaSuccess && !c->identity)
     e = mcg::launch_wave_expand(c->opacity.as<float>(), c->opac_m.as<float>(), c->lin2cell.as<int32_t>(), c->ncell3,
                                 nc1, nb, s);
+  if (e == cudaSuccess && !c->identity && c->go_n > 0)
+    e = mcg::launch_wave_expand(c->sca.as<float>(), c->sca_m.as<float>(), c->lin2cell.as<int32_t>(), c->ncell3, nc1,
+                                nb, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "opacity rebuild failed: %s", cudaGetErrorString(e));
   MC_CUDA(cudaEventRecord(e1, s));
   int herr = 0;

@@ -66,6 +66,19 @@ def absorption_weights(xs_abs):
     return np.ascontiguousarray((xs_abs / np.pi).T.astype(np.float32))
 
 
+def grain_opacity(nu):
+    """Per size bin the extinction (abs + sca) and scattering cross-sections
+    per grain [nsizes, nbins] cm^2 (FP32) and the number weights [nsizes] of
+    the synthetic MRN mix whose sums are the workloads' dust opacity
+    (nebula._dust_kappa: Q_abs = 1 - exp(-x/2), Q_sca = 0.9 x^4 / (1 + x^4))."""
+    xs_abs, w, a = grains(nu)
+    lam = 2.9979250e10 / (nu.astype(np.float64) * FR1RYD)
+    x = 2.0 * np.pi * a[:, None] / lam[None, :]
+    xs_sca = np.pi * a[:, None] ** 2 * (0.9 * x ** 4 / (1.0 + x ** 4))
+    return (np.ascontiguousarray((xs_abs + xs_sca).astype(np.float32)), np.ascontiguousarray(xs_sca.astype(np.float32)),
+            w.astype(np.float32))
+
+
 def grain_physics(neb, abundance=1.0):
     """The grains of the photoelectric and gas-grain collision terms of the
     cell update (setGrainPotential, setPhotoelHeatCool,

@@ -19,8 +19,9 @@ Each iteration runs, on the grid resident in HBM,
 On a grid with grains the grain temperatures (getDustT) follow the update,
 the grains' opacity (Ndust x (abs + sca) per grain, the dust add of
 iteration_mod.f90:166-227) is added to every opacity rebuild, and their
-thermal emission joins the recPDF rows.  The grains keep their opacity above
-the sublimation temperature (the reference drops it there).  With
+thermal emission joins the recPDF rows.  A size bin whose grain temperature
+reaches the sublimation temperature drops out of the opacity and the
+scattering table of the cell (iteration_mod.f90:193-210).  With
 ``photoelectric`` (lgPhotoelectric, on by default in the reference) every T
 step of the update also charges the grains and adds the photoelectric
 heating and the gas-grain collisional cooling to the gas (setGrainPotential,
@@ -75,7 +76,8 @@ class LambdaIteration:
             from . import dust
             xs_abs, gw, _ = dust.grains(neb.nu)
             self.dust = (dust.absorption_weights(xs_abs), dust.emission_table(xs_abs, neb.nu), gw)
-            self.ctx.set_fixed_opacity(neb.ndust, neb.dust_kappa)
+            from . import emission as _em
+            self.ctx.set_grain_opacity(*dust.grain_opacity(neb.nu), neb.ndust, _em.T_SUBLIME)
             if photoelectric:
                 self.ctx.set_grain_physics(dust.grain_physics(neb))
         if emission == "auto":

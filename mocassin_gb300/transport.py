@@ -111,6 +111,8 @@ def library():
         lib.mc_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.mc_ctx_get_tuning.restype = C.c_int
         lib.mc_ctx_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        lib.mc_ctx_set_grain_opacity.restype = C.c_int
+        lib.mc_ctx_set_grain_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp, fp, fp, C.c_float]
         lib.mc_ctx_set_grain_physics.restype = C.c_int
         lib.mc_ctx_set_grain_physics.argtypes = [C.c_void_p, C.POINTER(abi.McGrainPhysics)]
         lib.mc_ctx_grain_state.restype = C.c_int
@@ -119,6 +121,8 @@ def library():
         lib.mc_ctx_dust_temperatures.argtypes = [C.c_void_p, C.c_int32, fp, fp, C.c_int32, fp, C.c_double, fp, dp]
         lib.mc_ctx_get_opacity.restype = C.c_int
         lib.mc_ctx_get_opacity.argtypes = [C.c_void_p, fp]
+        lib.mc_ctx_get_scattering.restype = C.c_int
+        lib.mc_ctx_get_scattering.argtypes = [C.c_void_p, fp]
         lib.mc_ctx_destroy.restype = None
         lib.mc_ctx_destroy.argtypes = [C.c_void_p]
         lib.mc_opacity_build.restype = C.c_int
@@ -433,6 +437,20 @@ class TransportContext:
                                                  float(scale), _fptr(out), C.byref(ms)))
         return out, ms.value
 
+    def set_grain_opacity(self, xs_ext, xs_sca, weight, ndust, t_sublime):
+        """The grains' rows of every opacity_from_state: per size, weight x
+        Ndust x xs_ext into the opacity and x xs_sca into the scattering
+        table, for the sizes below t_sublime (the last dust_temperatures)."""
+        if xs_ext is None:
+            _check(self.lib.mc_ctx_set_grain_opacity(self.handle, 0, None, None, None, None, 0.0))
+            return
+        ext = np.ascontiguousarray(xs_ext, dtype=np.float32)
+        sca = np.ascontiguousarray(xs_sca, dtype=np.float32)
+        w = np.ascontiguousarray(weight, dtype=np.float32)
+        nd = np.ascontiguousarray(ndust, dtype=np.float32)
+        _check(self.lib.mc_ctx_set_grain_opacity(self.handle, ext.shape[0], _fptr(ext), _fptr(sca), _fptr(w),
+                                                 _fptr(nd), float(t_sublime)))
+
     def set_grain_physics(self, grains):
         """Grains in the gas update (photoelectric heating and gas-grain
         collisions, update_mod.f90:527-930) from the description of
@@ -458,6 +476,11 @@ class TransportContext:
     def get_opacity(self):
         out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
         _check(self.lib.mc_ctx_get_opacity(self.handle, _fptr(out)))
+        return out
+
+    def get_scattering(self):
+        out = np.empty((self.neb.nbins, self.neb.ncells + 1), dtype=np.float32)
+        _check(self.lib.mc_ctx_get_scattering(self.handle, _fptr(out)))
         return out
 
     def set_fixed_opacity(self, den, xs):

@@ -147,3 +147,36 @@ def test_grain_physics_argument_checks(gpu_lib):
     with pytest.raises(transport.TransportError):
         ctx.grain_state()  # no update has run yet
     ctx.close()
+
+
+def test_sublimated_grains_leave_the_opacity_and_scattering(gpu_lib):
+    """The opacity rebuild adds each size bin's grains (weight x Ndust x
+    (abs + sca)) and rebuilds the scattering table from the same sizes, for
+    the sizes whose grain temperature is below the sublimation temperature
+    (iteration_mod.f90:193-210): against a float64 restatement, with a
+    threshold that half of the (size, cell) temperatures pass."""
+    neb, ctx, state, w, gp = _setup(CASES[0])
+    ctx.update_cells(w, 1e-9)
+    xs_abs, gw, _ = dust.grains(neb.nu)
+    td, _ = ctx.dust_temperatures(dust.absorption_weights(xs_abs), dust.emission_table(xs_abs, neb.nu), gw, 1e-9)
+    ext, sca, wgt = dust.grain_opacity(neb.nu)
+    lit = td[1:, 1:][td[1:, 1:] > 0]
+    tsub = float(np.median(lit))
+    ctx.set_grain_opacity(ext, sca, wgt, neb.ndust, tsub)
+    ions = _ions()
+    ctx.opacity_from_state(np.array(ions, dtype=np.int32), neb.xs, method="fp32")
+    op, sc = ctx.get_opacity().astype(np.float64), ctx.get_scattering().astype(np.float64)
+    X = ctx.get_cell_state()[2]
+    ctx.close()
+    den = balance.opacity_species(X, neb.hden.astype(np.float64), ions).astype(np.float64)
+    keep = td[1:] < tsub                                   # (sizes, cells)
+    assert 0.2 < keep[:, 1:].mean() < 0.8
+    dd = keep * wgt[:, None].astype(np.float64) * neb.ndust[None, :].astype(np.float64)
+    dd[:, 0] = 0.0
+    ref_op = (den.T @ neb.xs.astype(np.float64)).T + (dd.T @ ext.astype(np.float64)).T
+    ref_sc = (dd.T @ sca.astype(np.float64)).T
+    c = np.arange(1, neb.ncells + 1)
+    np.testing.assert_allclose(op[:, c], ref_op[:, c], rtol=2e-6, atol=1e-30)
+    np.testing.assert_allclose(sc[:, c], ref_sc[:, c], rtol=2e-6, atol=1e-30)
+    # with every size kept, the grains' rows add up to the grid's own dust opacity
+    assert np.allclose((wgt[:, None] * ext).sum(0), neb.dust_kappa, rtol=1e-5)
