@@ -426,6 +426,19 @@ mc_status mc_ctx_set_fixed_opacity(mc_ctx_t *ctx, int32_t nrows, const float *de
  * weight = grainAbun x grainWeight.  nsizes 0 removes them. */
 mc_status mc_ctx_set_grain_opacity(mc_ctx_t *ctx, int32_t nsizes, const float *xs_ext, const float *xs_sca,
                                    const float *weight, const float *ndust, float t_sublime);
+
+/* Resonance-line packets (energyPacketDriver, source/photon_mod.f90:180-266,
+ * which runs them when lgDust and convPercent >= resLinesTransfer): counts
+ * [Nc+1] = resLinePackets of each active cell (initResLinePackets,
+ * emission_mod.f90:150-245, stays with the caller).  Every later mc_ctx_run
+ * in the wave forms sends, after each star's packets, a block of "diffuse"
+ * packets with that star's deltaE: counts[cell] of them from the node
+ * (xAxis(ix), yAxis(iy), zAxis(iz)) of each cell, in the reference's loop
+ * order (x outer, z inner), each followed through its re-emissions.  Their
+ * draws come from Philox streams keyed by star index istar | 0x80.  Not with
+ * MC_RUN_FORM_PLAIN, replayed draws or more than 8 sources (MC_ERR_UNSUPPORTED).
+ * counts NULL (or all zero) turns them off. */
+mc_status mc_ctx_set_res_lines(mc_ctx_t *ctx, const int32_t *counts);
 mc_status mc_ctx_opacity_from_state(mc_ctx_t *ctx, int32_t nspecies, const int32_t *species, const float *xs,
                                     int32_t method, double *kernel_ms);
 

@@ -61,8 +61,9 @@ struct DevSource {
 };
 
 struct DevSources {
-  int nsrc;
-  long long total;
+  int nsrc;        // stars (entries 0..nsrc-1)
+  int nres;        // resonance-line blocks that follow them (0 or nsrc), one per star
+  long long total; // stellar packets (the resonance packets' ids follow)
   DevSource s[kMaxSources];
 };
 

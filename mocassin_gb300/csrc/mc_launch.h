@@ -23,6 +23,11 @@ cudaError_t launch_wave_sample_stellar_fp32(const WaveLaunch &L);
 cudaError_t launch_wave_sample_stellar_fp64(const WaveLaunch &L);
 cudaError_t launch_wave_sample_reemit_fp32(const WaveLaunch &L, unsigned int n_abs);
 cudaError_t launch_wave_sample_reemit_fp64(const WaveLaunch &L, unsigned int n_abs);
+// resonance-line packets into the absorbed list after round 0
+cudaError_t launch_wave_res_inject_fp32(const WaveLaunch &L, const uint32_t *cells, const long long *prefix,
+                                        int ncell);
+cudaError_t launch_wave_res_inject_fp64(const WaveLaunch &L, const uint32_t *cells, const long long *prefix,
+                                        int ncell);
 cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round);
 cudaError_t launch_wave_emit_fp64(const WaveLaunch &L, int round);
 cudaError_t launch_wave_march_fp32(const WaveLaunch &L);

@@ -181,6 +181,11 @@ struct mc_ctx {
   mcg::UpdArgs wave_args{};
   void *wave_scratch = nullptr;
   DBuf counters, src_cdf, replay;
+  // resonance-line packets (mc_ctx_set_res_lines): the cells that emit some,
+  // packed, in the reference's loop order, and the packets before each
+  DBuf res_cells, res_prefix;
+  int res_ncell = 0;
+  long long res_per_star = 0;
   // chosen form: march-indexed views and the sorted packet queue
   int identity = 1;
   long long ncell3 = 0;
@@ -372,6 +377,7 @@ mc_status make_sources(mc_ctx *c, const mc_source_t *src, int32_t nsrc, const mc
     return set_error(MC_ERR_ARG, "nsrc must be 1..%d (got %d)", mcg::kMaxSources, nsrc);
   std::vector<float> cdfs((size_t)nsrc * c->nb);
   S.nsrc = nsrc;
+  S.nres = 0;
   long long base = 0;
   for (int i = 0; i < nsrc; ++i) {
     const mc_source_t &x = src[i];
@@ -645,7 +651,9 @@ mc_status wave_setup(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &
   if (S.total >= 0xFFFFFFFFll) return set_error(MC_ERR_ARG, "2^32-1 or more packets in one call");
   if (g.nb > 0xFFFF) return set_error(MC_ERR_UNSUPPORTED, "nbins above 65535");
   if (c->nx > 1023 || c->ny > 1023 || c->nz > 1023) return set_error(MC_ERR_UNSUPPORTED, "grid axes above 1023");
-  mc_status st = wave_buffers(c, (size_t)S.total);
+  const long long all = S.total + (S.nres > 0 ? (long long)S.nres * S.s[S.nsrc].n : 0);
+  if (all >= 0xFFFFFFFFll) return set_error(MC_ERR_ARG, "2^32-1 or more packets in one call");
+  mc_status st = wave_buffers(c, (size_t)all);
   if (st) return st;
   L.g = g;
   L.S = S;
@@ -731,6 +739,11 @@ mc_status run_wave_graph(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSourc
     if (r == cudaSuccess) r = mcg::launch_wave_sort(L, (unsigned int)S.total);
     if (r == cudaSuccess) r = f64 ? mcg::launch_wave_emit_fp64(L, 0) : mcg::launch_wave_emit_fp32(L, 0);
     if (r == cudaSuccess) r = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
+    if (r == cudaSuccess && S.nres > 0)
+      r = f64 ? mcg::launch_wave_res_inject_fp64(L, c->res_cells.as<uint32_t>(), c->res_prefix.as<long long>(),
+                                                 c->res_ncell)
+              : mcg::launch_wave_res_inject_fp32(L, c->res_cells.as<uint32_t>(), c->res_prefix.as<long long>(),
+                                                 c->res_ncell);
     return r;
   };
   cudaError_t ce = round0();
@@ -839,6 +852,13 @@ mc_status run_wave(mc_ctx_t *c, const mcg::DevGrid &g, const mcg::DevSources &S,
     e = f64 ? mcg::launch_wave_march_fp64(L) : mcg::launch_wave_march_fp32(L);
     if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "march launch failed: %s", cudaGetErrorString(e));
     MC_CUDA(cudaEventRecord(c->evm1, c->stream));
+    if (round == 0 && S.nres > 0) {
+      e = f64 ? mcg::launch_wave_res_inject_fp64(L, c->res_cells.as<uint32_t>(), c->res_prefix.as<long long>(),
+                                                 c->res_ncell)
+              : mcg::launch_wave_res_inject_fp32(L, c->res_cells.as<uint32_t>(), c->res_prefix.as<long long>(),
+                                                 c->res_ncell);
+      if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "resonance-line launch failed: %s", cudaGetErrorString(e));
+    }
     struct { unsigned int a_count; int err; } hb{};
     MC_CUDA(cudaMemcpyAsync(&hb.a_count, w.a_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     MC_CUDA(cudaMemcpyAsync(&hb.err, &L.cnt->error_code, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -874,6 +894,24 @@ mc_status mc_ctx_run(mc_ctx_t *c, const mc_source_t *src, int32_t nsrc, const mc
   mcg::DevSources S{};
   mc_status st = make_sources(c, src, nsrc, o, S);
   if (st) return st;
+  if (c->res_per_star > 0) {
+    // a block of resonance-line packets after each star's (energyPacketDriver
+    // :180-266), with the star's deltaE and its own draw stream
+    if (o->rng != MC_RNG_PHILOX) return set_error(MC_ERR_UNSUPPORTED, "resonance-line packets draw from Philox only");
+    if (o->run_flags & MC_RUN_FORM_PLAIN)
+      return set_error(MC_ERR_UNSUPPORTED, "resonance-line packets need the wave form, not MC_RUN_FORM_PLAIN");
+    if (2 * nsrc > mcg::kMaxSources)
+      return set_error(MC_ERR_UNSUPPORTED, "resonance-line packets: at most %d sources", mcg::kMaxSources / 2);
+    if (S.total < 1) return set_error(MC_ERR_ARG, "resonance-line packets need stellar packets in the call");
+    S.nres = nsrc;
+    for (int i = 0; i < nsrc; ++i) {
+      mcg::DevSource &d = S.s[nsrc + i];
+      d = S.s[i];
+      d.k1 = (uint32_t)(o->seed >> 32) ^ ((o->iteration & 0xFFFFFFu) << 8) ^ ((uint32_t)(src[i].istar | 0x80) & 0xFFu);
+      d.n = c->res_per_star;
+      d.base = S.total + (long long)i * c->res_per_star;
+    }
+  }
   mcg::DevReplay rp{nullptr, 0};
   if (o->rng == MC_RNG_REPLAY) {
     if (!o->replay || o->replay_stride <= 0) return set_error(MC_ERR_ARG, "replay needs draws and a stride");
@@ -2541,6 +2579,41 @@ extern "C" mc_status mc_ctx_set_grain_opacity(mc_ctx_t *c, int32_t nsizes, const
   MC_CUDA(cudaStreamSynchronize(c->stream));
   c->go_n = nsizes;
   c->go_tsub = t_sublime;
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_set_res_lines(mc_ctx_t *c, const int32_t *counts) {
+  if (!c) return set_error(MC_ERR_ARG, "ctx is NULL");
+  c->res_per_star = 0;
+  c->res_ncell = 0;
+  if (!counts) return MC_OK;
+  const int nc1 = c->nc + 1;
+  long long tot = 0;
+  for (int i = 1; i < nc1; ++i) {
+    if (counts[i] < 0) return set_error(MC_ERR_ARG, "resonance-line packets: cell %d has %d", i, counts[i]);
+    tot += counts[i];
+  }
+  if (tot == 0) return MC_OK;
+  if (tot >= (1ll << 31)) return set_error(MC_ERR_ARG, "resonance-line packets: 2^31 or more per star");
+  std::vector<int32_t> act((size_t)c->nx * c->ny * c->nz);
+  MC_CUDA(cudaMemcpy(act.data(), c->active.p, act.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> cells;
+  std::vector<long long> prefix(1, 0);
+  for (int ix = 1; ix <= c->nx; ++ix)  // the reference's loop order: x outer, z inner
+    for (int iy = 1; iy <= c->ny; ++iy)
+      for (int iz = 1; iz <= c->nz; ++iz) {
+        const int a = act[(size_t)(ix - 1) + (size_t)c->nx * ((iy - 1) + (size_t)c->ny * (iz - 1))];
+        if (a <= 0 || a >= nc1 || counts[a] == 0) continue;
+        cells.push_back(mcg::pack_cell_host(ix, iy, iz));
+        prefix.push_back(prefix.back() + counts[a]);
+      }
+  mc_status st;
+  if ((st = put_buf(c->res_cells, cells.data(), cells.size() * sizeof(uint32_t), c->stream)) ||
+      (st = put_buf(c->res_prefix, prefix.data(), prefix.size() * sizeof(long long), c->stream)))
+    return st;
+  MC_CUDA(cudaStreamSynchronize(c->stream));
+  c->res_ncell = (int)cells.size();
+  c->res_per_star = prefix.back();
   return MC_OK;
 }
 

@@ -54,6 +54,12 @@ template <bool Replay> static cudaError_t emit_impl(const WaveLaunch &L, int rou
   wave_emit_kernel<float, Replay><<<L.num_sms * kGridPerSm, 256, 0, L.stream>>>(L.g, L.S, L.rp, L.w, round, L.cnt);
   return cudaGetLastError();
 }
+cudaError_t launch_wave_res_inject_fp32(const WaveLaunch &L, const uint32_t *cells, const long long *prefix,
+                                        int ncell) {
+  wave_res_inject_kernel<float><<<L.num_sms * kGridPerSm, 256, 0, L.stream>>>(L.g, L.S, L.w, cells, prefix, ncell);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round) {
   return L.rp.draws ? emit_impl<true>(L, round) : emit_impl<false>(L, round);
 }

@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(256) transport_plain_kernel(const __grid_const
   for (long long gp = (long long)blockIdx.x * blockDim.x + threadIdx.x; gp < S.total; gp += stride) {
     if (*(volatile int *)&cnt->error_code != 0) break;
     int s = 0;
-    while (s + 1 < S.nsrc && gp >= S.s[s + 1].base) ++s;
+    while (s + 1 < S.nsrc + S.nres && gp >= S.s[s + 1].base) ++s;
     const DevSource &src = S.s[s];
     History<Real, Layout> h(g, src, cnt, lc);
     h.gpacket = gp;

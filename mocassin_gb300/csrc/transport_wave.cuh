@@ -110,7 +110,7 @@ template <bool Replay> struct RStream {
 
 __device__ __forceinline__ int source_of(const DevSources &S, long long gp) {
   int s = 0;
-  while (s + 1 < S.nsrc && gp >= S.s[s + 1].base) ++s;
+  while (s + 1 < S.nsrc + S.nres && gp >= S.s[s + 1].base) ++s;
   return s;
 }
 
@@ -306,6 +306,50 @@ __global__ void __launch_bounds__(256) wave_sample_reemit_kernel(const __grid_co
   __syncthreads();
   for (int i = threadIdx.x; i < g.nb; i += blockDim.x)
     if (sh[i]) atomicAdd(&w.bin_count[i], sh[i]);
+}
+
+// Resonance-line packets (energyPacketDriver :180-266): after round 0 each
+// star's block of diffuse packets joins the absorbed list that round 1
+// re-emits, packet p of a block at the node (xAxis(ix), yAxis(iy),
+// zAxis(iz)) of its cell, with a fresh draw stream and no re-emission yet.
+// cells [ncell] packed, prefix [ncell + 1] the packets before each cell.
+template <typename Real>
+__global__ void __launch_bounds__(256) wave_res_inject_kernel(const __grid_constant__ DevGrid g,
+                                                             const __grid_constant__ DevSources S,
+                                                             const __grid_constant__ WaveGrid w,
+                                                             const uint32_t *cells, const long long *prefix,
+                                                             int ncell) {
+  const long long per = prefix[ncell], total = per * S.nres;
+  const unsigned int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < total; k0 += stride) {
+    const long long k = k0 + lane;
+    const bool mine = k < total;
+    const unsigned int m = __ballot_sync(0xffffffffu, mine);
+    unsigned int base = 0;
+    if (lane == 0) base = atomicAdd(w.a_count, (unsigned int)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!mine) continue;
+    const int b = (int)(k / per);
+    const long long p = k - (long long)b * per;
+    int lo = 0, hi = ncell - 1;  // the cell j with prefix[j] <= p < prefix[j + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= p) lo = mid;
+      else hi = mid - 1;
+    }
+    const unsigned int slot = base + lane;
+    int x, y, z;
+    unpack_cell(cells[lo], x, y, z);
+    w.a_id[slot] = (uint32_t)(S.s[S.nsrc + b].base + p);
+    w.a_cell[slot] = cells[lo];
+    w.a_words[slot] = 0u;
+    w.a_run[slot] = 0;
+    Real *ar = (Real *)w.a_r + 3 * (size_t)slot;
+    ar[0] = (Real)g.xa[x - 1];
+    ar[1] = (Real)g.ya[y - 1];
+    ar[2] = (Real)g.za[z - 1];
+  }
 }
 
 // ------------------------------------------------------------------ emit
@@ -668,7 +712,8 @@ template <typename Real, bool Fast, bool Dust, bool Replay> struct Marcher {
     refresh_hot();
   }
   __device__ __forceinline__ void refresh_hot() {
-    hot_ok = Fast && valid && nuP == hot_nu && (stellar || !(g.flags & MC_FLAG_DEBUG)) && source_of(S, id) < kHotSrc;
+    hot_ok = Fast && valid && nuP == hot_nu && (stellar || !(g.flags & MC_FLAG_DEBUG)) &&
+             source_of(S, id) < (S.nsrc < kHotSrc ? S.nsrc : kHotSrc);  // a star with a cube (not a resonance block)
   }
   // (re)start the ray at r0 = r with direction v
   __device__ void dda_init() {

@@ -13,6 +13,11 @@ namespace mcg {
 // CUDA graph.
 constexpr unsigned int kDeviceCount = 0xFFFFFFFFu;
 
+// a cell's (x, y, z) in one word, 10 bits each (the device's pack_cell)
+__host__ __device__ inline uint32_t pack_cell_host(int x, int y, int z) {
+  return (uint32_t)x | ((uint32_t)y << 10) | ((uint32_t)z << 20);
+}
+
 struct WaveGrid {
   // march-indexed views of the grid
   const float *opac;        // [nb][S] opacity

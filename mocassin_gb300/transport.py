@@ -111,6 +111,8 @@ def library():
         lib.mc_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.mc_ctx_get_tuning.restype = C.c_int
         lib.mc_ctx_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        lib.mc_ctx_set_res_lines.restype = C.c_int
+        lib.mc_ctx_set_res_lines.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         lib.mc_ctx_set_grain_opacity.restype = C.c_int
         lib.mc_ctx_set_grain_opacity.argtypes = [C.c_void_p, C.c_int32, fp, fp, fp, fp, C.c_float]
         lib.mc_ctx_set_grain_physics.restype = C.c_int
@@ -436,6 +438,17 @@ class TransportContext:
         _check(self.lib.mc_ctx_dust_temperatures(self.handle, nsizes, _fptr(w_abs), _fptr(em), em.shape[1], _fptr(gw),
                                                  float(scale), _fptr(out), C.byref(ms)))
         return out, ms.value
+
+    def set_res_lines(self, counts):
+        """Resonance-line packets per active cell [Nc+1] for every later run
+        (None: off); see mc_ctx_set_res_lines."""
+        if counts is None:
+            _check(self.lib.mc_ctx_set_res_lines(self.handle, None))
+            return
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        if c.shape != (self.neb.ncells + 1,):
+            raise ValueError("counts must have Nc+1 entries")
+        _check(self.lib.mc_ctx_set_res_lines(self.handle, c.ctypes.data_as(C.POINTER(C.c_int32))))
 
     def set_grain_opacity(self, xs_ext, xs_sca, weight, ndust, t_sublime):
         """The grains' rows of every opacity_from_state: per size, weight x

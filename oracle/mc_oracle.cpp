@@ -683,6 +683,29 @@ template <typename Real, typename Acc> class Runner {
     return false;
   }
 
+  // one resonance-line packet (energyPacketDriver :180-266): a "diffuse"
+  // packet emitted at the node of cell c0 (xAxis(ix), yAxis(iy), zAxis(iz)),
+  // followed through its re-emissions like any other history
+  void res_history(int64_t p, int64_t gp, const int c0[3]) {
+    gpacket = gp;
+    d = Draws();
+    d.k0 = k0;
+    d.k1 = k1;
+    d.packet = (uint64_t)p;
+    PType ptype = DIFFUSE;
+    V3<Real> position{P.xA[c0[0] - 1], P.yA[c0[1] - 1], P.zA[c0[2] - 1]};
+    int cell[3] = {c0[0], c0[1], c0[2]};
+    int64_t ncross = 0;
+    int i;
+    for (i = 1; i <= P.recursionLimit; ++i) {
+      bool rerun = energyPacketRun(ptype, position, cell, ncross);
+      if (d.exhausted) { P.fail(MC_ERR_REPLAY, gpacket); break; }
+      if (!rerun) break;
+    }
+    if (i >= P.recursionLimit) P.trapped.fetch_add(1, std::memory_order_relaxed);
+    P.crossings.fetch_add(ncross, std::memory_order_relaxed);
+  }
+
   // Key / replay row of this source, set once per source.
   uint32_t k0 = 0, k1 = 0;
   const double *replay = nullptr;
@@ -718,7 +741,7 @@ template <typename Real, typename Acc> class Runner {
 
 template <typename Real, typename Acc>
 int run(const mc_grid_t *g, const mc_source_t *src, int nsrc, const mc_run_opts_t *o,
-        double *jste, double *jdif, double *esc, mc_stats_t *st, int nthreads) {
+        double *jste, double *jdif, double *esc, mc_stats_t *st, int nthreads, const int32_t *res_counts) {
   Problem<Real, Acc> P;
   P.g = g;
   P.nx = g->nx; P.ny = g->ny; P.nz = g->nz; P.nc = g->ncells; P.nb = g->nbins;
@@ -752,6 +775,26 @@ int run(const mc_grid_t *g, const mc_source_t *src, int nsrc, const mc_run_opts_
   }
   if (P.debug && !P.jdif) return MC_ERR_ARG;
 
+  // resonance-line packets: the cell of each packet of a star's block, cells
+  // in the reference's loop order (x outer, z inner), resLinePackets(cell)
+  // packets each
+  std::vector<int> res_cell;
+  if (res_counts)
+    for (int ix = 1; ix <= P.nx; ++ix)
+      for (int iy = 1; iy <= P.ny; ++iy)
+        for (int iz = 1; iz <= P.nz; ++iz) {
+          const int a = g->active[(ix - 1) + (int64_t)P.nx * ((iy - 1) + (int64_t)P.ny * (iz - 1))];
+          if (a <= 0) continue;
+          for (int k = 0; k < res_counts[a]; ++k) {
+            res_cell.push_back(ix);
+            res_cell.push_back(iy);
+            res_cell.push_back(iz);
+          }
+        }
+  const int64_t nres = (int64_t)res_cell.size() / 3;
+  int64_t total_stellar = 0;
+  for (int s = 0; s < nsrc; ++s) total_stellar += src[s].n_packets;
+
   int64_t base = 0;
   double qphot = 0.0;
   for (int s = 0; s < nsrc; ++s) {
@@ -776,6 +819,21 @@ int run(const mc_grid_t *g, const mc_source_t *src, int nsrc, const mc_run_opts_
       qphot += R.qphot;
     }
     base += n;
+    if (nres > 0) {
+      // this star's block of resonance-line packets, after its own packets,
+      // drawn from the stream of star index istar | 0x80
+      uint32_t r0, r1;
+      stream_key(o->seed, o->iteration, S.istar | 0x80, r0, r1);
+      const int64_t rbase = total_stellar + (int64_t)s * nres;
+#pragma omp parallel
+      {
+        Runner<Real, Acc> R(P, S);
+        R.k0 = r0;
+        R.k1 = r1;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t p = 0; p < nres; ++p) R.res_history(p, rbase + p, &res_cell[3 * p]);
+      }
+    }
   }
   if (!direct) {
     for (int64_t i = 0; i < nj; ++i) jste[i] += (double)aj[i];
@@ -813,9 +871,23 @@ int oracle_transport_run(const mc_grid_t *g, const mc_source_t *src, int32_t nsr
   if (g->n_angle < 0 || g->n_angle > 2 || (g->n_angle > 0 && (!g->view_theta || !g->view_phi))) return MC_ERR_ARG;
   if (o->rng == MC_RNG_REPLAY && (!o->replay || o->replay_stride <= 0)) return MC_ERR_ARG;
   if (o->precision == MC_PREC_FP64)
-    return run<double, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads);
-  if (acc32) return run<float, float>(g, src, nsrc, o, jste, jdif, esc, st, nthreads);
-  return run<float, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads);
+    return run<double, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads, nullptr);
+  if (acc32) return run<float, float>(g, src, nsrc, o, jste, jdif, esc, st, nthreads, nullptr);
+  return run<float, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads, nullptr);
+}
+
+// The same with resonance-line packets: res_counts [Nc+1] = resLinePackets
+// per active cell, a block of them after each star's packets
+// (energyPacketDriver :180-266).  Philox draws only.
+int oracle_transport_run_res(const mc_grid_t *g, const mc_source_t *src, int32_t nsrc,
+                             const mc_run_opts_t *o, double *jste, double *jdif, double *esc,
+                             mc_stats_t *st, int32_t nthreads, const int32_t *res_counts) {
+  if (!g || !src || !o || !jste || nsrc < 0 || !res_counts) return MC_ERR_ARG;
+  if (o->rng != MC_RNG_PHILOX) return MC_ERR_ARG;
+  if (g->n_angle < 0 || g->n_angle > 2 || (g->n_angle > 0 && (!g->view_theta || !g->view_phi))) return MC_ERR_ARG;
+  if (o->precision == MC_PREC_FP64)
+    return run<double, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads, res_counts);
+  return run<float, double>(g, src, nsrc, o, jste, jdif, esc, st, nthreads, res_counts);
 }
 
 // Philox4x32-10 of one block, for the known-answer tests.

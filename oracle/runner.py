@@ -33,12 +33,14 @@ def library():
 
 
 def run(neb, n_packets=None, seed=1, iteration=1, precision="fp64", replay=None, threads=0, acc32=False,
-        recursion_limit=0, safe_limit=0, out=None, marshalled=None):
+        recursion_limit=0, safe_limit=0, out=None, marshalled=None, res_counts=None):
     """Oracle transport of all stars of ``neb``; returns (jste, jdif, escaped, stats).
 
     out: (jste, jdif, escaped) arrays of abi.estimator_arrays(neb) to zero
     and fill instead of new ones; marshalled: an abi.Marshalled(neb,
-    n_packets) to reuse (a timing loop keeps both out of its timed region)."""
+    n_packets) to reuse (a timing loop keeps both out of its timed region);
+    res_counts: resonance-line packets per active cell [Nc+1] (a block after
+    each star's packets, Philox draws)."""
     lib = library()
     m = marshalled if marshalled is not None else abi.Marshalled(neb, n_packets=n_packets)
     prec = abi.MC_PREC_FP64 if precision == "fp64" else abi.MC_PREC_FP32
@@ -54,8 +56,16 @@ def run(neb, n_packets=None, seed=1, iteration=1, precision="fp64", replay=None,
             jd.fill(0.0)
     st = abi.McStats()
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    rc = lib.oracle_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), dp(js), dp(jd), dp(es),
-                                  C.byref(st), int(threads), int(acc32))
+    if res_counts is None:
+        rc = lib.oracle_transport_run(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), dp(js), dp(jd), dp(es),
+                                      C.byref(st), int(threads), int(acc32))
+    else:
+        rcnt = np.ascontiguousarray(res_counts, dtype=np.int32)
+        if rcnt.shape != (neb.ncells + 1,):
+            raise ValueError("res_counts must have Nc+1 entries")
+        rc = lib.oracle_transport_run_res(C.byref(m.grid), m.sources, m.nsrc, C.byref(opts), dp(js), dp(jd),
+                                          dp(es), C.byref(st), int(threads),
+                                          rcnt.ctypes.data_as(C.POINTER(C.c_int32)))
     if rc != 0:
         raise RuntimeError("oracle failed with status %d (packet %d)" % (rc, st.error_packet))
     return js, jd, es, st.as_dict()

@@ -92,3 +92,24 @@ def test_packet_and_energy_conservation():
             assert abs(es.sum() + e_lines - lum) < 1e-9 * lum, spec.name
         assert np.all(js >= 0) and np.all(es >= 0)
         assert st["crossings"] > 0
+
+
+def test_resonance_packets_in_the_oracle():
+    """No resonance-line packets is the plain transport (to the rounding of
+    the threads' sums); each extra packet is one more history that ends as
+    a line, an escape or a trap."""
+    import numpy as np
+    from mocassin_gb300 import nebula
+    from oracle import runner
+    from tests import helpers
+    neb = nebula.build(nebula.small_cases()[3])
+    a = runner.run(neb, precision="fp64", seed=4)
+    b = runner.run(neb, precision="fp64", seed=4, res_counts=np.zeros(neb.ncells + 1, np.int32))
+    for k in ("crossings", "absorptions", "lines", "escaped", "trapped"):
+        assert a[3][k] == b[3][k]
+    assert helpers.rel_err(a[0], b[0]) < 1e-13
+    cnt = np.zeros(neb.ncells + 1, np.int32)
+    cnt[1:] = np.random.default_rng(1).integers(0, 3, neb.ncells)
+    c = runner.run(neb, precision="fp64", seed=4, res_counts=cnt)
+    ends = lambda s: s["lines"] + s["escaped"] + s["trapped"] + s["silent_exits"]
+    assert ends(c[3]) - ends(a[3]) == int(cnt.sum())
