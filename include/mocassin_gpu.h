@@ -537,6 +537,11 @@ mc_status mc_ctx_surrogate_params(mc_ctx_t *ctx, float *get, const float *set);
  * the first 41 columns count), and the outputs y [m][48]. */
 mc_status mc_ctx_surrogate_grads(mc_ctx_t *ctx, int32_t m, const float *x, const float *t, double *loss, float *grads,
                                  float *y);
+/* The network's outputs y [m][48] for m feature rows x [m][80] with the
+ * prediction's arithmetic (the four layers on tcgen05: BF16 operands, FP32
+ * accumulators in tensor memory), as mc_ctx_update_cells_warm computes them
+ * for every cell. */
+mc_status mc_ctx_surrogate_forward(mc_ctx_t *ctx, int32_t m, const float *x, float *y);
 
 /* Scheduling parameters of the persistent march (results do not depend on
  * them beyond the order of the FP64 sums): refill_min = free lanes a warp

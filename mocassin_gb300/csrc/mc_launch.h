@@ -159,6 +159,12 @@ cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const 
                             const float *w, bool wt, const float *bias, int act, float *c, int ldc, cudaStream_t s);
 cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
                              float *db, int num_sms, cudaStream_t s);
+// the forward layers on the tensor cores (tcgen05, BF16 operands, FP32
+// accumulators in TMEM), and the error flag of their bounded mbarrier waits
+// (1 when one gave up; reading it clears it)
+cudaError_t launch_mlp_forward_tc(int M, int N, int K, const float *a, int lda, const float *w, const float *bias,
+                                  int act, float *c, int ldc, int num_sms, cudaStream_t s);
+int mlp_tc_take_error();
 cudaError_t launch_mlp_loss(int M, int nt, int ld, const float *y, const float *tn, float *dy, double *loss,
                             cudaStream_t s);
 cudaError_t launch_mlp_adam(int n, float *w, const float *g, float *m1, float *m2, const int *dstep, int step0,

@@ -1775,6 +1775,8 @@ static mc_status update_cells_impl(mc_ctx_t *c, const float *w, double scale, do
   MC_CUDA(cudaMemcpyAsync(&hs, c->s_ustats.p, sizeof hs, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaMemcpyAsync(&herr, c->s_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
+  if (warm && mcg::mlp_tc_take_error() > 0)
+    return set_error(MC_ERR_TIMEOUT, "a tensor-core wait of the surrogate gave up");
   float m1 = 0.f, m2 = 0.f;
   cudaEventElapsedTime(&m1, e0, e1);
   cudaEventElapsedTime(&m2, e1, e2);
@@ -1901,20 +1903,23 @@ mc_status ensure(DBuf &b, size_t bytes) {
 }
 
 // forward pass of M rows: x [M][80] -> a1, a2, a3 [M][256] -> y [M][48]
-mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, float *a3, float *y) {
+// the four layers of M rows; tensor: on tcgen05 (the prediction over a
+// grid), else on the CUDA cores (training, whose steps of a few thousand
+// rows gain nothing from the tensor cores and keep the arithmetic the
+// measured networks were trained with)
+mc_status mlp_forward(mc_ctx_t *c, int M, const float *x, float *a1, float *a2, float *a3, float *y,
+                      bool tensor = false) {
   const float *W = c->m_w.as<float>();
   cudaStream_t s = c->stream;
-  cudaError_t e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpIn, x, kMlpIn, nullptr, true, W + mcg::kMlpW1, true,
-                                       W + mcg::kMlpB1, 1, a1, kMlpHid, s);
-  if (e == cudaSuccess)
-    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, a1, kMlpHid, nullptr, true, W + mcg::kMlpW2, true, W + mcg::kMlpB2,
-                             1, a2, kMlpHid, s);
-  if (e == cudaSuccess)
-    e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, a2, kMlpHid, nullptr, true, W + mcg::kMlpW3, true, W + mcg::kMlpB3,
-                             1, a3, kMlpHid, s);
-  if (e == cudaSuccess)
-    e = mcg::launch_mlp_gemm(M, kMlpOut, kMlpHid, a3, kMlpHid, nullptr, true, W + mcg::kMlpW4, true, W + mcg::kMlpB4,
-                             0, y, kMlpOut, s);
+  const int sm = c->num_sms;
+  auto layer = [&](int N, int K, const float *a, const float *w, const float *b, int act, float *o) {
+    return tensor ? mcg::launch_mlp_forward_tc(M, N, K, a, K, w, b, act, o, N, sm, s)
+                  : mcg::launch_mlp_gemm(M, N, K, a, K, nullptr, true, w, true, b, act, o, N, s);
+  };
+  cudaError_t e = layer(kMlpHid, kMlpIn, x, W + mcg::kMlpW1, W + mcg::kMlpB1, 1, a1);
+  if (e == cudaSuccess) e = layer(kMlpHid, kMlpHid, a1, W + mcg::kMlpW2, W + mcg::kMlpB2, 1, a2);
+  if (e == cudaSuccess) e = layer(kMlpHid, kMlpHid, a2, W + mcg::kMlpW3, W + mcg::kMlpB3, 1, a3);
+  if (e == cudaSuccess) e = layer(kMlpOut, kMlpHid, a3, W + mcg::kMlpW4, W + mcg::kMlpB4, 0, y);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp forward failed: %s", cudaGetErrorString(e));
   return MC_OK;
 }
@@ -1977,7 +1982,7 @@ mc_status surrogate_predict_state(mc_ctx_t *c) {
                                                  c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "features failed: %s", cudaGetErrorString(e));
   if ((st = mlp_forward(c, nc1, c->m_xi.as<float>(), c->m_h1.as<float>(), c->m_h2.as<float>(), c->m_h3.as<float>(),
-                        c->m_yi.as<float>())))
+                        c->m_yi.as<float>(), true)))
     return st;
   e = mcg::launch_mlp_apply(c->nc, c->s_mom.as<float>(), c->m_yi.as<float>(), c->m_tmean.as<float>(),
                             c->m_tstd.as<float>(), c->s_te.as<double>(), c->s_ne.as<double>(), c->s_X.as<double>(),
@@ -2144,6 +2149,7 @@ extern "C" mc_status mc_ctx_surrogate_train(mc_ctx_t *c, int32_t steps, int32_t 
   MC_CUDA(cudaEventRecord(e1, s));
   if (steps > 0) MC_CUDA(cudaMemcpyAsync(&last, c->m_loss.p, 8, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
+  if (mcg::mlp_tc_take_error() > 0) return set_error(MC_ERR_TIMEOUT, "a tensor-core wait of the surrogate gave up");
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
@@ -2205,7 +2211,26 @@ extern "C" mc_status mc_ctx_surrogate_grads(mc_ctx_t *c, int32_t m, const float 
   if (grads) MC_CUDA(cudaMemcpyAsync(grads, c->m_g.p, kMlpParams * 4, cudaMemcpyDeviceToHost, s));
   if (y) MC_CUDA(cudaMemcpyAsync(y, c->m_y.p, (size_t)m * kMlpOut * 4, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
+  if (mcg::mlp_tc_take_error() > 0) return set_error(MC_ERR_TIMEOUT, "a tensor-core wait of the surrogate gave up");
   if (loss) *loss = l / ((double)m * mcg::kMlpTargets);
+  return MC_OK;
+}
+
+extern "C" mc_status mc_ctx_surrogate_forward(mc_ctx_t *c, int32_t m, const float *x, float *y) {
+  if (!c || !c->m_ready || m < 1 || !x || !y) return set_error(MC_ERR_ARG, "bad surrogate forward arguments");
+  cudaStream_t s = c->stream;
+  DBuf dx, h1, h2, h3, dy;
+  MC_CUDA(dx.alloc((size_t)m * kMlpIn * 4));
+  MC_CUDA(h1.alloc((size_t)m * kMlpHid * 4));
+  MC_CUDA(h2.alloc((size_t)m * kMlpHid * 4));
+  MC_CUDA(h3.alloc((size_t)m * kMlpHid * 4));
+  MC_CUDA(dy.alloc((size_t)m * kMlpOut * 4));
+  MC_CUDA(cudaMemcpyAsync(dx.p, x, dx.bytes, cudaMemcpyHostToDevice, s));
+  mc_status st = mlp_forward(c, m, dx.as<float>(), h1.as<float>(), h2.as<float>(), h3.as<float>(), dy.as<float>(), true);
+  if (st) return st;
+  MC_CUDA(cudaMemcpyAsync(y, dy.p, dy.bytes, cudaMemcpyDeviceToHost, s));
+  MC_CUDA(cudaStreamSynchronize(s));
+  if (mcg::mlp_tc_take_error() > 0) return set_error(MC_ERR_TIMEOUT, "a tensor-core wait of the surrogate gave up");
   return MC_OK;
 }
 

@@ -6,11 +6,13 @@
 // Network: four layers, 80 -> 256 (ReLU) -> 256 (ReLU) -> 256 (ReLU) -> 48
 // (padded sizes; 68 features, 41 targets).  Arithmetic: each layer rounds its
 // operands to BF16 and accumulates in FP32 (the operand precision of a BF16
-// tensor-core product), weights kept in FP32 for Adam.  The layers run on
-// CUDA cores as tiled GEMMs: ~330 kFLOP per cell forward, a few ms for a
-// 101^3 grid.
+// tensor-core product), weights kept in FP32 for Adam.  The prediction over
+// a grid runs the four layers on the tensor cores (mlp_fwd_tc_kernel: 0.57
+// ms for the 227k cells of a 61^3 grid); training (steps of a few thousand
+// rows) runs them on CUDA cores as tiled GEMMs, ~330 kFLOP per row forward.
 //
 // Kernels
+//   mlp_fwd_tc_kernel  the forward layers on tcgen05 (below)
 //   mlp_gemm_kernel    C[m][n] = act(b[n] + sum_k A(m,k) B(k,n)) in 64 x 64
 //                      tiles, 16-deep K steps through shared memory, 4 x 4
 //                      outputs per thread; B is a layer's weights read as
@@ -32,6 +34,7 @@
 
 #include "mc_device.cuh"
 #include "mc_launch.h"
+#include "tc_util.cuh"
 
 namespace mcg {
 
@@ -330,7 +333,192 @@ __global__ void mlp_apply_kernel(int nc, const float *mom, const float *y, const
   }
 }
 
+// ---- the forward layers on tcgen05 ------------------------------------
+// out[m][n] = act(bias[n] + sum_k bf16(a[m*lda + k]) bf16(w[n*K + k])), the
+// same products as mlp_gemm_kernel's forward pass, with the sums in the
+// tensor cores' FP32 accumulators.  A persistent CTA of 256 threads per SM
+// keeps the layer's BF16 weights (N x K, K-major core matrices) in shared
+// memory and takes 128-row tiles of A in turn: the threads convert the
+// tile's FP32 rows (float4 loads, a warp covering 8 rows x 32 k so both the
+// loads and the 16-byte shared stores are conflict-free) into the K-major
+// BF16 layout, one thread issues the K / 16 MMAs (128 x N x 16) into one of
+// two TMEM accumulators, and while they run the threads drain the other
+// accumulator (the previous tile) through tcgen05.ld, bias, ReLU and the
+// stores.  Every mbarrier wait is bounded; a wait that gives up sets
+// g_mlp_tc_error and ends the CTA's loop.
+constexpr int kFwdM = 128, kFwdThreads = 256;
+
+__device__ int g_mlp_tc_error;
+
+__device__ __forceinline__ uint32_t mlp_pack_bf16x2(float a, float b) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+}
+
+// rows [r0, r0 + nrows) x K of src (row stride ld, rows >= rmax read as 0)
+// into BF16 K-major core matrices at dst
+__device__ __forceinline__ void mlp_stage_rows(unsigned char *dst, const float *src, long long ld, int r0, int nrows,
+                                               int rmax, int K, int warp, int lane) {
+  const int kgroups = (K + 31) / 32, total = (nrows / 8) * kgroups;
+  const int rr = lane >> 2, kc = lane & 3;
+  constexpr int kU = 8;  // warp steps whose loads are in flight together
+  for (int it0 = warp; it0 < total; it0 += kU * (kFwdThreads / 32)) {
+    float4 v[kU][2];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int it = it0 + u * (kFwdThreads / 32);
+      const int r = (it / kgroups) * 8 + rr, k = (it % kgroups) * 32 + kc * 8;
+      v[u][0] = v[u][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (it < total && r0 + r < rmax && k < K) {
+        const float4 *p = (const float4 *)(src + (long long)(r0 + r) * ld + k);
+        v[u][0] = __ldg(p);
+        v[u][1] = __ldg(p + 1);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int it = it0 + u * (kFwdThreads / 32);
+      const int r = (it / kgroups) * 8 + rr, k = (it % kgroups) * 32 + kc * 8;
+      if (it < total && k < K)
+        *(uint4 *)(dst + kmajor_off(r, k, K)) =
+            make_uint4(mlp_pack_bf16x2(v[u][0].x, v[u][0].y), mlp_pack_bf16x2(v[u][0].z, v[u][0].w),
+                       mlp_pack_bf16x2(v[u][1].x, v[u][1].y), mlp_pack_bf16x2(v[u][1].z, v[u][1].w));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1) mlp_fwd_tc_kernel(int M, int N, int K, const float *a, int lda,
+                                                                      const float *w, const float *bias, int act,
+                                                                      float *out, int ldo, int ncols) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char *sW = sm, *sA = sm + (size_t)N * K * 2;
+  uint64_t *bar = (uint64_t *)(sA + (size_t)kFwdM * K * 2);  // [2]: the accumulators' MMAs done
+  uint32_t *tslot = (uint32_t *)(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar + 1)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  // the layer's weights, once
+  mlp_stage_rows(sW, w, K, 0, (N + 7) / 8 * 8, N, K, warp, lane);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = mma_idesc(kFwdM, N);
+  const uint32_t lbo = 128, sbo = (uint32_t)(K / 8) * 128;
+  const int ntiles = (M + kFwdM - 1) / kFwdM;
+  uint32_t phase[2] = {0u, 0u};
+  bool failed = false;
+  int prev = -1;  // the tile whose accumulator is still to be drained
+  int i = 0;
+  auto drain = [&](int tile, int buf) {
+    // warp w: TMEM lanes 32 (w % 4) .., columns of half w / 4
+    const int q = warp & 3, half = warp >> 2;
+    const int r = tile * kFwdM + 32 * q + lane;
+    const int c_lo = half * ((N + 63) / 64) * 32, c_hi = min(N, c_lo + ((N + 63) / 64) * 32);
+    for (int c0 = c_lo; c0 < c_hi; c0 += 32) {
+      uint32_t v[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * (ncols / 2) + c0), v);
+      if (r < M) {
+        float *o = out + (long long)r * ldo;
+#pragma unroll
+        for (int u = 0; u < 32; u += 4) {
+          if (c0 + u >= N) break;
+          float x[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float t = __uint_as_float(v[u + e]) + (bias ? __ldg(bias + c0 + u + e) : 0.f);
+            x[e] = act == 1 ? (t > 0.f ? t : 0.f) : t;
+          }
+          *(float4 *)(o + c0 + u) = make_float4(x[0], x[1], x[2], x[3]);
+        }
+      }
+    }
+  };
+  for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x, ++i) {
+    const int buf = i & 1;
+    if (i > 0) {
+      // the A buffer is free once the previous tile's MMAs are done
+      const bool ok = mbar_wait(smem_addr(bar + (buf ^ 1)), phase[buf ^ 1]);
+      phase[buf ^ 1] ^= 1u;
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    mlp_stage_rows(sA, a, lda, tile * kFwdM, kFwdM, M, K, warp, lane);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t aa = smem_addr(sA), ww = smem_addr(sW), d = tmem + (uint32_t)(buf * (ncols / 2));
+      for (int st = 0; st < K / 16; ++st) {
+        const uint32_t ko = (uint32_t)st * 256;
+        umma_bf16(d, smem_desc(aa + ko, lbo, sbo), smem_desc(ww + ko, lbo, sbo), idesc, st > 0 ? 1u : 0u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_addr(bar + buf))
+                   : "memory");
+    }
+    // the previous tile's accumulator (its MMAs were waited for above)
+    if (prev >= 0) drain(prev, buf ^ 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    prev = tile;
+  }
+  if (!failed && prev >= 0) {
+    const int buf = (i - 1) & 1;
+    const bool ok = mbar_wait(smem_addr(bar + buf), phase[buf]);
+    if (__syncthreads_or(!ok)) failed = true;
+    else {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      drain(prev, buf);
+    }
+  }
+  if (failed && tid == 0) atomicExch(&g_mlp_tc_error, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+size_t mlp_fwd_smem(int N, int K) { return (size_t)N * K * 2 + (size_t)kFwdM * K * 2 + 64; }
+
 }  // namespace
+
+// the forward layers on tcgen05 (N, K multiples of 16, N <= 256, K <= 256,
+// lda and ldo multiples of 4); the kernel's shared memory is set by
+// mlp_prepare(), before any capture
+cudaError_t launch_mlp_forward_tc(int M, int N, int K, const float *a, int lda, const float *w, const float *bias,
+                                  int act, float *c, int ldc, int num_sms, cudaStream_t s) {
+  if (M < 1 || N < 16 || N > 256 || N % 16 || K < 16 || K > 256 || K % 16 || lda % 4 || ldc % 4)
+    return cudaErrorInvalidValue;
+  int ncols = 32;
+  while (ncols < 2 * N) ncols <<= 1;
+  const int ntiles = (M + kFwdM - 1) / kFwdM;
+  const int blocks = ntiles < num_sms ? ntiles : num_sms;
+  // at least 116 KB of shared memory: one CTA per SM, so the TMEM columns of
+  // co-resident CTAs never have to wait for each other
+  size_t sh = mlp_fwd_smem(N, K);
+  if (sh < 116 * 1024) sh = 116 * 1024;
+  mlp_fwd_tc_kernel<<<blocks, kFwdThreads, sh, s>>>(M, N, K, a, lda, w, bias, act, c, ldc, ncols);
+  return cudaGetLastError();
+}
+
+int mlp_tc_take_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_mlp_tc_error, sizeof v) != cudaSuccess) return -1;
+  if (v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(g_mlp_tc_error, &z, sizeof z);
+  }
+  return v;
+}
 
 cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const float *mask, bool round_a,
                             const float *w, bool wt, const float *bias, int act, float *c, int ldc, cudaStream_t s) {
@@ -380,7 +568,10 @@ cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dste
   return cudaGetLastError();
 }
 
-cudaError_t mlp_prepare() { return cudaSuccess; }
+cudaError_t mlp_prepare() {
+  return cudaFuncSetAttribute(mlp_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)mlp_fwd_smem(256, 256));
+}
 
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s) {
   mlp_stats_kernel<<<dim3(64, cols), 256, 0, s>>>(n, cols, a, sum, sq);

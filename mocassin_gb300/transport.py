@@ -408,6 +408,17 @@ class TransportContext:
         _check(self.lib.mc_ctx_surrogate_params(self.handle, _fptr(out), _fptr(s)))
         return out
 
+    def surrogate_forward(self, x):
+        """Outputs [m, 48] of the network for feature rows x [m, 80] on the
+        tensor cores (the arithmetic of the warm start's prediction)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((len(x), 48), dtype=np.float32)
+        self.lib.mc_ctx_surrogate_forward.restype = C.c_int
+        self.lib.mc_ctx_surrogate_forward.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_float),
+                                                      C.POINTER(C.c_float)]
+        _check(self.lib.mc_ctx_surrogate_forward(self.handle, len(x), _fptr(x), _fptr(y)))
+        return y
+
     def surrogate_grads(self, x, t):
         x = np.ascontiguousarray(x, dtype=np.float32)
         t = np.ascontiguousarray(t, dtype=np.float32)

@@ -209,3 +209,31 @@ def test_network_trained_on_other_models_warm_starts_a_new_one(gpu_lib):
     assert warm["hit"] == cold["hit"]
     assert warm["t_iterations"] < cold["t_iterations"], (cold["t_iterations"], warm["t_iterations"])
     print("pretrained warm start: T steps %d -> %d" % (cold["t_iterations"], warm["t_iterations"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rows", [300, 40000])
+def test_gpu_tensor_core_forward_matches_oracle(gpu_lib, rows):
+    """The prediction's forward on tcgen05 (mc_ctx_surrogate_forward) against
+    the oracle: 300 rows (a tile per CTA) and 40,000 rows (every CTA takes
+    several 128-row tiles in turn: both TMEM accumulators, the A buffer
+    refilled).  The tensor cores add the BF16 products in blocks of 16, in
+    another order than a sequential FP32 sum, so more hidden activations
+    land one BF16 step (2^-8) apart than on the CUDA cores: 97 % of the
+    outputs to 2e-5, all to 5e-3."""
+    neb = nebula.build(nebula.small_cases()[0])
+    ctx = transport.TransportContext(neb)
+    ctx.surrogate_init(seed=3, capacity=16)
+    p = _random_params(6)
+    ctx.surrogate_params(set=p)
+    rng = np.random.default_rng(7)
+    x = rng.normal(0, 1, (rows, O.NI)).astype(np.float32)
+    y = ctx.surrogate_forward(x)
+    ctx.close()
+    oy = O.forward(p, x)[1]
+    d = np.abs(y - oy)
+    rows_bad = np.mean(d > 5e-3, axis=1)
+    print("tensor-core forward, %d rows: %.4f within 2e-5, max %.2e, rows with an entry above 5e-3: %d" % (rows,
+          np.mean(d <= 2e-5 + 2e-5 * np.abs(oy)), d.max(), int((rows_bad > 0).sum())))
+    assert np.mean(d <= 2e-5 + 2e-5 * np.abs(oy)) >= 0.97
+    assert d.max() <= 5e-3, d.max()
