@@ -321,6 +321,25 @@ def converged_model(neb, args):
     out["speedup_parts"] = {"transport_per_iteration": per("plain", "transport_s") / per("chosen", "transport_s"),
                             "update_per_iteration": per("plain", "update_s") / per("chosen", "update_s"),
                             "warm_start_wall": out["chosen"]["wall_s"] / out["chosen_surrogate"]["wall_s"]}
+    if args.repeats > 1:
+        # the chosen form with and without the warm start, each run `repeats` times from the same initial
+        # state (the warm start's network trained anew each time: its training sums in a different order
+        # from run to run, so its spread is part of the warm start's)
+        recs = {n: [out[n]] + [_lambda_form(neb, n, args, rows)[0] for _ in range(args.repeats - 1)]
+                for n in ("chosen", "chosen_surrogate")}
+        rep = {"runs": args.repeats}
+        for n, rr in recs.items():
+            rep[n] = {}
+            for k in ("wall_s", "wall_to_dte_rule_s", "update_s", "transport_s", "iterations"):
+                v = np.array([r[k] for r in rr if r[k] is not None], dtype=float)
+                rep[n][k] = {"mean": float(v.mean()), "sd": float(v.std(ddof=1)) if len(v) > 1 else None,
+                             "n": int(len(v))}
+        a, b = rep["chosen"]["wall_s"], rep["chosen_surrogate"]["wall_s"]
+        rep["warm_start_wall_ratio"] = a["mean"] / b["mean"]
+        # difference of the means in units of its standard error (Welch)
+        se = np.sqrt((a["sd"] or 0.0) ** 2 / a["n"] + (b["sd"] or 0.0) ** 2 / b["n"])
+        rep["warm_start_gain_in_se"] = float((a["mean"] - b["mean"]) / se) if se > 0 else None
+        out["repeats"] = rep
     return out
 
 
@@ -429,6 +448,8 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--surrogate-rows", type=int, default=1_000_000,
                     help="batch cell states (FP64 update) the warm start is trained on; 0: the model's own")
+    ap.add_argument("--repeats", type=int, default=5,
+                    help="runs of the chosen form with and without the warm start (mean and sd of their times)")
     ap.add_argument("--breakdown", type=int, default=0,
                     help="only the Lambda forms, each run this many times: mean and sd of their times")
     ap.add_argument("--lambda-only", default="", choices=["", "chosen", "chosen_surrogate", "plain", "naive"],

@@ -319,6 +319,144 @@ __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real
   return cool;
 }
 
+// cel_cooling_smem in FP32 for an ion of N levels known at compile time:
+// every loop unrolled, so the rate matrix, the right-hand side and the
+// populations are registers (no per-thread matrix in local memory) and the
+// table reads take constant offsets.  The same operations in the same order
+// as cel_cooling_smem.
+template <int N>
+__device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float Te, float Ne, float up, int top_levels,
+                                                 float fscale, float *emis, float escale) {
+  const UpdTabs<float> &T = a.f;
+  if (emis) *emis = 0.f;
+  if (up != up) return 0.f;
+  const UpdCelT<float> &c = T.cel[k];
+  const int nt = c.nt;
+  const float *logt = T.logt + (size_t)k * kNT;
+  const float *g = T.g + (size_t)k * kNL, *e = T.e + (size_t)k * kNL;
+  const float *A = T.A + (size_t)k * kNL * kNL;
+  const float *qq = T.qq + (size_t)k * kNL * kNL * kNT, *q2 = T.q2 + (size_t)k * kNL * kNL * kNT;
+  const float sqrTe = sqrtf(Te), log10Te = log10f(Te);
+  float X[N][N], y[N];  // X[i][j] is row i + 1, column j + 1 of the 1-based system
+  float arec = 0.f;
+  const bool rec = c.br > 0.f;
+  if (rec) {
+    const float br = c.br, zz = c.zz;
+    const float tz = Te * 1.e-4f / (zz * zz), t4 = Te * 1.e-4f;
+    arec = 1.e-13f * br * zz * c.ar[0] * powf(tz, c.ar[1]) / (1.f + c.ar[2] * powf(tz, c.ar[3])) +
+           1.0e-12f * br * (c.ad[0] / t4 + c.ad[1] + c.ad[2] * t4 + c.ad[3] * t4 * t4) * powf(t4, -1.5f) *
+               expf(-c.ad[4] * 1.e4f / Te);
+  }
+#pragma unroll
+  for (int j = 0; j < N; ++j) X[0][j] = 1.f;
+  y[0] = 1.f;
+#pragma unroll
+  for (int i = 1; i < N; ++i) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) X[i][j] = 0.f;
+    y[i] = rec ? -Ne * up * arec : 0.f;
+  }
+  int klo = 0, khi = nt - 1;
+  const bool below = log10Te <= logt[0], above = log10Te >= logt[nt - 1];
+  if (nt > 2 && !below && !above) {
+    while (khi - klo > 1) {
+      const int m = (khi + klo) / 2;
+      if (logt[m] > log10Te) khi = m;
+      else klo = m;
+    }
+  }
+  const float h = logt[khi] - logt[klo];
+  const float aa = nt > 2 ? (logt[khi] - log10Te) / h : 0.f;
+  const float bb = nt > 2 ? (log10Te - logt[klo]) / h : 0.f;
+  const float ca = aa * aa * aa - aa, cb = bb * bb * bb - bb, h26 = h * h / 6.f;
+#pragma unroll
+  for (int lo = 1; lo < N; ++lo)
+#pragma unroll
+    for (int hi = lo + 1; hi <= N; ++hi) {
+      const float *yy = qq + ((size_t)lo * kNL + hi) * kNT;
+      float cs;
+      if (nt == 1) cs = yy[0];
+      else if (nt == 2) cs = yy[0] + (yy[1] - yy[0]) / (logt[1] - logt[0]) * (log10Te - logt[0]);
+      else if (below) cs = yy[0];
+      else if (above) cs = yy[nt - 1];
+      else {
+        const float *y2 = q2 + ((size_t)lo * kNL + hi) * kNT;
+        cs = aa * yy[klo] + bb * yy[khi] + (ca * y2[klo] + cb * y2[khi]) * h26;
+      }
+      const float qex = 8.63e-6f * cs * expf((e[lo] - e[hi]) * 1.4388463f / Te) / (g[lo] * sqrTe);
+      const float qde = 8.63e-6f * cs / (g[hi] * sqrTe);
+      const float Ahl = A[hi * kNL + lo];
+      X[hi - 1][lo - 1] += Ne * qex;
+      X[hi - 1][hi - 1] -= Ne * qde + Ahl;
+      if (lo >= 2) {
+        X[lo - 1][hi - 1] += Ne * qde + Ahl;
+        X[lo - 1][lo - 1] -= Ne * qex;
+      }
+    }
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) {
+    const float inv = 1.f / X[i][i];
+#pragma unroll
+    for (int kk = i + 1; kk < N; ++kk) {
+      const float f = X[kk][i] * inv;
+#pragma unroll
+      for (int j = i + 1; j < N; ++j) X[kk][j] = X[kk][j] - X[i][j] * f;
+      y[kk] = y[kk] - y[i] * f;
+    }
+  }
+  y[N - 1] = y[N - 1] / X[N - 1][N - 1];
+#pragma unroll
+  for (int kk = N - 2; kk >= 0; --kk) {
+#pragma unroll
+    for (int j = kk + 1; j < N; ++j) y[kk] = y[kk] - y[j] * X[kk][j];
+    y[kk] = y[kk] / X[kk][kk];
+  }
+  float sumN = 0.f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) sumN += y[i];
+  float cool = 0.f;
+  const int top = N < top_levels ? N : top_levels;
+  const float inv = 1.f / sumN;
+#pragma unroll
+  for (int i = 1; i <= N - 1; ++i)
+#pragma unroll
+    for (int j = i + 1; j <= N; ++j)
+      if (j <= top && A[j * kNL + i] != 0.f) {
+        const float line = A[j * kNL + i] * (e[j] - e[i]) * (y[j - 1] * inv);
+        if (!(fscale > 0.f)) cool += line;
+        else if (line * fscale > 1e-35f) cool += line * fscale;
+      }
+  if (emis) {
+    float em = 0.f;
+#pragma unroll
+    for (int i = 1; i <= N - 1; ++i)
+#pragma unroll
+      for (int j = i + 1; j <= N; ++j)
+        if (A[j * kNL + i] != 0.f) {
+          const float line = A[j * kNL + i] * (e[j] - e[i]) * (y[j - 1] * inv) * escale;
+          if (line > 1e-35f) em += line;
+        }
+    *emis = em;
+  }
+  return cool;
+}
+
+// the FP32 level populations of line ion k: the register form for the
+// level counts the line ions of the atomic data have (2, 3, 5, 6, 7, 9, 10,
+// 12, 13, 15), cel_cooling_smem on the scratch matrix M (L rows) otherwise
+__device__ __forceinline__ float cel_cooling_f32(const UpdArgs &a, int k, float Te, float Ne, float up, float *M, int L,
+                                                 int top_levels, float fscale, float *emis = nullptr,
+                                                 float escale = 0.f) {
+  switch (a.f.cel[k].nlev) {
+#define MC_CEL_CASE(n) \
+  case n: return cel_cooling_reg<n>(a, k, Te, Ne, up, top_levels, fscale, emis, escale);
+    MC_CEL_CASE(2) MC_CEL_CASE(3) MC_CEL_CASE(5) MC_CEL_CASE(6) MC_CEL_CASE(7) MC_CEL_CASE(9) MC_CEL_CASE(10)
+    MC_CEL_CASE(12) MC_CEL_CASE(13) MC_CEL_CASE(15)
+#undef MC_CEL_CASE
+    default: return cel_cooling_smem<float>(a, k, Te, Ne, up, M, L, top_levels, fscale, emis, escale);
+  }
+}
+
 template <typename Real, bool Fast>
 __global__ void __launch_bounds__(kW * 32) cell_update_kernel(const __grid_constant__ UpdArgs a) {
   extern __shared__ __align__(16) unsigned char cu_dyn[];

@@ -224,8 +224,8 @@ __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ W
     const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
     float x[kNL * kNL];
     float emis = 0.f;
-    const float cool = cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f, a.forb_out ? &emis : nullptr,
-                                               T.ab[C.e] * xi * 1.9865e9f);
+    const float cool = cel_cooling_f32(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f, a.forb_out ? &emis : nullptr,
+                                       T.ab[C.e] * xi * 1.9865e9f);
     w.cool[(size_t)k * (a.nc + 1) + c] = cool * T.ab[C.e] * xi * 1.9865e-16f;
     if (a.forb_out) a.forb_out[(size_t)k * (a.nc + 1) + c] = emis;
   }

@@ -157,8 +157,12 @@ constexpr int kMlpW1 = 0, kMlpB1 = kMlpW1 + kMlpHid * kMlpIn, kMlpW2 = kMlpB1 + 
               kMlpW4 = kMlpB3 + kMlpHid, kMlpB4 = kMlpW4 + kMlpOut * kMlpHid, kMlpParams = kMlpB4 + kMlpOut;
 cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const float *mask, bool round_a,
                             const float *w, bool wt, const float *bias, int act, float *c, int ldc, cudaStream_t s);
+// dW += dZ^T bf16(X) and db += column sums of dZ over M rows: per-split
+// partial sums in `scratch` (mlp_wgrad_scratch_floats of them), added in a
+// fixed order, so that training is reproducible
+size_t mlp_wgrad_scratch_floats(int M, int N, int K, int num_sms);
 cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
-                             float *db, int num_sms, cudaStream_t s);
+                             float *db, float *scratch, size_t scratch_floats, int num_sms, cudaStream_t s);
 // the forward layers on the tensor cores (tcgen05, BF16 operands, FP32
 // accumulators in TMEM), and the error flag of their bounded mbarrier waits
 // (1 when one gave up; reading it clears it)
@@ -174,10 +178,16 @@ cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dste
                               const float *fmean, const float *fstd, const float *tmean, const float *tstd, float *xb,
                               float *tb, cudaStream_t s);
 cudaError_t mlp_prepare();
+// per-column sums and sums of squares of n rows: kMlpStatBlocks partial
+// sums per column (sum[b * cols + col]), for the host to add in order
+constexpr int kMlpStatBlocks = 64;
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s);
+// appends the rows of the balanced hit cells in cell order; blk_counts holds
+// mlp_collect_blocks(num_sms) counts
+int mlp_collect_blocks(int num_sms);
 cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
                                const double *X, const int *flags, long long cap, unsigned long long *count, float *xs,
-                               float *ts, int num_sms, cudaStream_t s);
+                               float *ts, unsigned int *blk_counts, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_infer_features(int nc, const float *mom, long long ms, const double *hden, const float *fmean,
                                       const float *fstd, float *x, int num_sms, cudaStream_t s);
 cudaError_t launch_mlp_apply(int nc, const float *mom, const float *y, const float *tmean, const float *tstd, double *te,

@@ -138,6 +138,10 @@ struct mc_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_side0 = nullptr, ev_cdf = nullptr;
   bool cdf_pending = false;
+  // MC_RUN_HOST_ZEROED: the last call left the device estimators all zero
+  // (it cleared what it had made nonzero after downloading it), so the next
+  // one needs no full clear
+  bool est_zero = false;
   DBuf view;        // viewing-angle table (n_angle > 0)
   int n_angle = 0;
   // cell update: atomic tables, per-cell state and scratch
@@ -148,6 +152,8 @@ struct mc_ctx {
   int u_bal_z[7] = {}, u_bal_first[7] = {};
   // learned warm start: parameters, Adam state, training buffer, work arrays
   DBuf m_w, m_g, m_m1, m_m2, m_xs, m_ts, m_count, m_fmean, m_fstd, m_tmean, m_tstd, m_loss, m_dstep;
+  DBuf m_gscr;  // the weight gradients' per-split partial sums
+  DBuf m_ccnt;  // rows per block of the training-row collection
   DBuf m_xb, m_tb, m_a1, m_a2, m_a3, m_y, m_dy, m_d3, m_d2, m_d1, m_xi, m_h1, m_h2, m_h3, m_yi, m_te_prev, m_ne_prev, m_x_prev;
   long long m_cap = 0, m_n = 0;
   int m_step = 0, m_B = 0;
@@ -300,6 +306,14 @@ mc_status view_table(const mc_grid_t *g, mcg::DevGrid &d, std::vector<uint8_t> &
 // opac_row0 > 0: the opacity rows (frequency bins) below it are not copied:
 // the caller guarantees no packet marches there (the non-ionising bins of a
 // gas-only grid escape before any march).
+// Device view of a pinned (page-locked, mapped) host pointer, or nullptr
+// for pageable memory.
+void *pinned_view(const void *h) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t cdf_stream = nullptr,
                         int opac_row0 = 0) {
   const int nc1 = g->ncells + 1, nb = g->nbins;
@@ -1939,30 +1953,35 @@ mc_status mlp_backward(mc_ctx_t *c, int M, const float *x, const float *t) {
   if ((st = mlp_forward(c, M, x, a1, a2, a3, y))) return st;
   const float *W = c->m_w.as<float>();
   float *G = c->m_g.as<float>();
-  MC_CUDA(cudaMemsetAsync(G, 0, kMlpParams * sizeof(float), s));
   const int sm = c->num_sms;
+  const size_t nscr = std::max({mcg::mlp_wgrad_scratch_floats(M, kMlpOut, kMlpHid, sm),
+                                mcg::mlp_wgrad_scratch_floats(M, kMlpHid, kMlpHid, sm),
+                                mcg::mlp_wgrad_scratch_floats(M, kMlpHid, kMlpIn, sm)});
+  if ((st = ensure(c->m_gscr, nscr * sizeof(float)))) return st;
+  float *scr = c->m_gscr.as<float>();
+  MC_CUDA(cudaMemsetAsync(G, 0, kMlpParams * sizeof(float), s));
   cudaError_t e = mcg::launch_mlp_loss(M, mcg::kMlpTargets, kMlpOut, y, t, dy, c->m_loss.as<double>(), s);
   // layer 4 (linear): dW4 = dY^T a3, dA3 = dY W4
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpOut, kMlpHid, dy, nullptr, a3, G + mcg::kMlpW4, G + mcg::kMlpB4, sm, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpOut, kMlpHid, dy, nullptr, a3, G + mcg::kMlpW4, G + mcg::kMlpB4, scr, nscr, sm, s);
   if (e == cudaSuccess)
     e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpOut, dy, kMlpOut, nullptr, false, W + mcg::kMlpW4, false, nullptr, 0, d3,
                              kMlpHid, s);
   // layer 3 (ReLU): dZ3 = dA3 (a3 > 0)
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d3, a3, a2, G + mcg::kMlpW3, G + mcg::kMlpB3, sm, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d3, a3, a2, G + mcg::kMlpW3, G + mcg::kMlpB3, scr, nscr, sm, s);
   if (e == cudaSuccess)
     e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, d3, kMlpHid, a3, false, W + mcg::kMlpW3, false, nullptr, 0, d2,
                              kMlpHid, s);
   // layer 2 (ReLU): dZ2 = dA2 (a2 > 0)
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d2, a2, a1, G + mcg::kMlpW2, G + mcg::kMlpB2, sm, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpHid, d2, a2, a1, G + mcg::kMlpW2, G + mcg::kMlpB2, scr, nscr, sm, s);
   if (e == cudaSuccess)
     e = mcg::launch_mlp_gemm(M, kMlpHid, kMlpHid, d2, kMlpHid, a2, false, W + mcg::kMlpW2, false, nullptr, 0, d1,
                              kMlpHid, s);
   // layer 1 (ReLU): dZ1 = dA1 (a1 > 0)
   if (e == cudaSuccess)
-    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpIn, d1, a1, x, G + mcg::kMlpW1, G + mcg::kMlpB1, sm, s);
+    e = mcg::launch_mlp_wgrad(M, kMlpHid, kMlpIn, d1, a1, x, G + mcg::kMlpW1, G + mcg::kMlpB1, scr, nscr, sm, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "mlp backward failed: %s", cudaGetErrorString(e));
   return MC_OK;
 }
@@ -1996,16 +2015,21 @@ mc_status surrogate_normalise(mc_ctx_t *c) {
   const long long n = std::min(c->m_n, c->m_cap);
   if (n < 2) return set_error(MC_ERR_ARG, "the surrogate has fewer than 2 training rows");
   cudaStream_t s = c->stream;
+  // per-block partial sums, added here in block order (reproducible)
+  const size_t B = mcg::kMlpStatBlocks, ox = 0, qx = B * kMlpIn, ot = 2 * B * kMlpIn, qt = ot + B * kMlpOut;
   DBuf sums;
-  MC_CUDA(sums.alloc((size_t)4 * 128 * sizeof(double)));
-  MC_CUDA(cudaMemsetAsync(sums.p, 0, sums.bytes, s));
+  MC_CUDA(sums.alloc((qt + B * kMlpOut) * sizeof(double)));
   double *d = sums.as<double>();
-  cudaError_t e = mcg::launch_mlp_stats(n, kMlpIn, c->m_xs.as<float>(), d, d + 128, s);
-  if (e == cudaSuccess) e = mcg::launch_mlp_stats(n, kMlpOut, c->m_ts.as<float>(), d + 256, d + 384, s);
+  cudaError_t e = mcg::launch_mlp_stats(n, kMlpIn, c->m_xs.as<float>(), d + ox, d + qx, s);
+  if (e == cudaSuccess) e = mcg::launch_mlp_stats(n, kMlpOut, c->m_ts.as<float>(), d + ot, d + qt, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "stats failed: %s", cudaGetErrorString(e));
-  std::vector<double> h(4 * 128);
-  MC_CUDA(cudaMemcpyAsync(h.data(), d, sums.bytes, cudaMemcpyDeviceToHost, s));
+  std::vector<double> part(qt + B * kMlpOut), h(4 * 128, 0.0);
+  MC_CUDA(cudaMemcpyAsync(part.data(), d, sums.bytes, cudaMemcpyDeviceToHost, s));
   MC_CUDA(cudaStreamSynchronize(s));
+  for (size_t b = 0; b < B; ++b) {
+    for (int i = 0; i < kMlpIn; ++i) { h[i] += part[ox + b * kMlpIn + i]; h[128 + i] += part[qx + b * kMlpIn + i]; }
+    for (int o = 0; o < kMlpOut; ++o) { h[256 + o] += part[ot + b * kMlpOut + o]; h[384 + o] += part[qt + b * kMlpOut + o]; }
+  }
   std::vector<float> fm(kMlpIn), fs(kMlpIn), tm(kMlpOut), ts(kMlpOut);
   auto ms = [&](double sum, double sq, float &mean, float &sd) {
     const double m = sum / (double)n, v = std::max(sq / (double)n - m * m, 0.);
@@ -2079,10 +2103,12 @@ extern "C" mc_status mc_ctx_surrogate_collect(mc_ctx_t *c, int64_t *rows) {
   if (!c || !c->m_ready) return set_error(MC_ERR_ARG, "mc_ctx_surrogate_init has not been called");
   if (!c->s_mom.p || !c->s_ready) return set_error(MC_ERR_ARG, "no cell update to learn from");
   cudaStream_t s = c->stream;
+  mc_status st0;
+  if ((st0 = ensure(c->m_ccnt, (size_t)mcg::mlp_collect_blocks(c->num_sms) * sizeof(unsigned int)))) return st0;
   cudaError_t e = mcg::launch_mlp_collect(c->nc, c->s_mom.as<float>(), c->nc + 1, c->u_hden.as<double>(),
                                           c->s_te.as<double>(), c->s_X.as<double>(), c->s_flags.as<int>(), c->m_cap,
                                           c->m_count.as<unsigned long long>(), c->m_xs.as<float>(),
-                                          c->m_ts.as<float>(), c->num_sms, s);
+                                          c->m_ts.as<float>(), c->m_ccnt.as<unsigned int>(), c->num_sms, s);
   if (e != cudaSuccess) return set_error(MC_ERR_CUDA, "collect failed: %s", cudaGetErrorString(e));
   unsigned long long n = 0;
   MC_CUDA(cudaMemcpyAsync(&n, c->m_count.p, 8, cudaMemcpyDeviceToHost, s));
@@ -2740,11 +2766,16 @@ int first_marched_bin(const mc_grid_t *g) {
 
 // flag[row] = 1 when row `row` of a [rows][len] array holds a nonzero value
 // (grid: x tiles the row, y = row; flag zeroed before)
-__global__ void row_nonzero_kernel(const double *__restrict__ a, long long len, unsigned char *flag) {
+__global__ void row_nonzero_kernel(const double *__restrict__ a, long long len, unsigned char *flag,
+                                   float *__restrict__ narrow) {
   const double *r = a + (long long)blockIdx.y * len;
+  float *o = narrow ? narrow + (long long)blockIdx.y * len : nullptr;
   bool nz = false;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
-    nz |= r[i] != 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const double v = r[i];
+    nz |= v != 0.0;
+    if (o) o[i] = (float)v;
+  }
   if (__syncthreads_or(nz) && threadIdx.x == 0) flag[blockIdx.y] = 1;
 }
 
@@ -2785,24 +2816,28 @@ __global__ void scatter_pairs_kernel(const uint32_t *__restrict__ idx, const voi
   }
 }
 
-// Device view of a pinned (page-locked, mapped) host pointer, or nullptr
-// for pageable memory.
-void *pinned_view(void *h) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+// a[idx[k]] = 0 for the n compacted entries
+__global__ void zero_at_kernel(const uint32_t *__restrict__ idx, unsigned long long n, double *a) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x)
+    a[idx[k]] = 0.0;
 }
 
+
 // MC_RUN_HOST_ZEROED download of one estimator [rows][len] (FP64 on the
-// device; FP32 staged values when stage is given): the rows that hold a
-// nonzero value, in one copy per run of such rows.
-mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, long long rows, long long len) {
+// device; rounded to FP32 into `stage` in the same pass that finds the
+// nonzero rows, when stage is given): the rows that hold a nonzero value, in
+// one copy per run of such rows.
+// With rezero, the rows are cleared on the device once copied.
+mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, long long rows, long long len,
+                        bool rezero) {
   cudaStream_t s = c->stream;
   mc_status st;
   if (c->z_mask.bytes != (size_t)rows && (st = put_buf(c->z_mask, nullptr, (size_t)rows, s))) return st;
   MC_CUDA(cudaMemsetAsync(c->z_mask.p, 0, (size_t)rows, s));
   const unsigned int tiles = (unsigned int)std::max(1ll, std::min(64ll, len / 4096));
-  row_nonzero_kernel<<<dim3(tiles, (unsigned int)rows), 256, 0, s>>>(d.as<double>(), len, c->z_mask.as<unsigned char>());
+  row_nonzero_kernel<<<dim3(tiles, (unsigned int)rows), 256, 0, s>>>(d.as<double>(), len, c->z_mask.as<unsigned char>(),
+                                                                    stage ? stage->as<float>() : nullptr);
   MC_CUDA(cudaGetLastError());
   std::vector<unsigned char> mask((size_t)rows);
   MC_CUDA(cudaMemcpyAsync(mask.data(), c->z_mask.p, (size_t)rows, cudaMemcpyDeviceToHost, s));
@@ -2817,6 +2852,7 @@ mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, lo
     MC_CUDA(cudaMemcpyAsync((char *)h + r * len * elt, src + r * len * elt, (size_t)((e - r) * len) * elt,
                             cudaMemcpyDeviceToHost, s));
     c->xfer_d2h += (long long)((e - r) * len) * (long long)elt;
+    if (rezero) MC_CUDA(cudaMemsetAsync((char *)d.p + r * len * sizeof(double), 0, (size_t)((e - r) * len) * sizeof(double), s));
     r = e;
   }
   return MC_OK;
@@ -2826,7 +2862,7 @@ mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, lo
 // compacted on the device and scattered into the caller's array (by the
 // device into pinned memory, by the host otherwise); a dense copy when they
 // are too many for the pair buffers.
-mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32) {
+mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32, bool rezero) {
   cudaStream_t s = c->stream;
   mc_status st;
   const unsigned long long n = d.bytes / sizeof(double);
@@ -2852,9 +2888,15 @@ mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32) {
       MC_CUDA(cudaMemcpyAsync(h, c->stage_e.p, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     }
     c->xfer_d2h += (long long)(n * elt);
+    if (rezero) MC_CUDA(cudaMemsetAsync(d.p, 0, d.bytes, s));
     return MC_OK;
   }
   if (cnt == 0) return MC_OK;
+  if (rezero) {  // the pairs hold the values: the entries can be cleared now
+    zero_at_kernel<<<(unsigned int)std::min<unsigned long long>((unsigned long long)c->num_sms * 4, (cnt + 255) / 256),
+                     256, 0, s>>>(c->z_idx.as<uint32_t>(), cnt, d.as<double>());
+    MC_CUDA(cudaGetLastError());
+  }
   // the pairs cross to the host either way: written there by the device, or
   // copied and scattered by the host
   c->xfer_d2h += (long long)(cnt * (sizeof(uint32_t) + elt));
@@ -2950,12 +2992,14 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
   cudaStream_t s = c->stream;
   struct Item { void *h; DBuf *d; DBuf *stage; } items[3] = {
       {jste, &c->jste, &c->stage_j}, {jdif, &c->jdif, &c->stage_d}, {escaped, &c->esc, &c->stage_e}};
+  const bool already_zero = hostz && c->est_zero;
+  c->est_zero = false;
   for (auto &it : items) {
     if (!it.d->p) continue;
     const size_t n = it.d->bytes / sizeof(double);
     if (f32 && it.h && (st = put_buf(*it.stage, nullptr, n * sizeof(float), s))) return st;
     if (!it.h || zero) {
-      MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, s));
+      if (!already_zero) MC_CUDA(cudaMemsetAsync(it.d->p, 0, it.d->bytes, s));
     } else if (!f32) {
       MC_CUDA(cudaMemcpyAsync(it.d->p, it.h, it.d->bytes, cudaMemcpyHostToDevice, s));
       h2d += (long long)it.d->bytes;
@@ -2976,22 +3020,27 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     return r;
   };
   if (hostz) {
-    // only what the transport made nonzero goes back
+    // only what the transport made nonzero goes back, and is then cleared
+    // on the device (on an identity grid the march adds into these arrays
+    // directly), so that the next call starts from zero without a full clear
     const long long len = c->nc + 1;
+    bool all = c->identity;
     for (int k = 0; k < 2; ++k) {
       Item &it = items[k];
-      if (!it.h || !it.d->p) continue;
+      if (!it.d->p) continue;
+      if (!it.h) { all = false; continue; }
       const long long n = (long long)(it.d->bytes / sizeof(double));
-      if (f32) {
-        narrow_kernel<<<c->num_sms * 8, 256, 0, s>>>(it.d->as<double>(), it.stage->as<float>(), (size_t)n);
-        MC_CUDA(cudaGetLastError());
-      }
-      if ((st = download_rows(c, *it.d, f32 ? it.stage : nullptr, it.h, n / len, len))) return st;
+      if ((st = download_rows(c, *it.d, f32 ? it.stage : nullptr, it.h, n / len, len, c->identity))) return st;
     }
-    if (escaped && c->esc.p) {
-      if ((st = download_sparse(c, c->esc, escaped, f32))) return st;
+    if (c->esc.p) {
+      if (escaped) {
+        if ((st = download_sparse(c, c->esc, escaped, f32, c->identity))) return st;
+      } else {
+        all = false;
+      }
     }
     MC_CUDA(cudaStreamSynchronize(s));
+    c->est_zero = all;
     return counted(MC_OK);
   }
   if (!f32) {

@@ -111,10 +111,12 @@ __global__ void __launch_bounds__(256) mlp_gemm_kernel(int M, int N, int K, cons
   }
 }
 
-// dW[n][k] += sum_m dZ(m,n) bf16(X(m,k)), dZ(m,n) = dz[m*N + n] (zero where
-// mask[m*N + n] <= 0); tiles of 64 n x 64 k, rows split over blockIdx.z
+// sum_m dZ(m,n) bf16(X(m,k)), dZ(m,n) = dz[m*N + n] (zero where
+// mask[m*N + n] <= 0), over the rows of split blockIdx.z, into P[z][n][k];
+// tiles of 64 n x 64 k.  The splits are added in order by
+// mlp_grad_reduce_kernel (no atomics), so a training run is reproducible.
 __global__ void __launch_bounds__(256) mlp_wgrad_kernel(int M, int N, int K, const float *dz, const float *mask,
-                                                        const float *x, float *dW, int rows_per_split) {
+                                                        const float *x, float *P, int rows_per_split) {
   __shared__ float Zs[kTK][kTN + 4], Xs[kTK][kTN + 4];
   const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
   const int n0 = blockIdx.x * kTN, k0 = blockIdx.y * kTN;
@@ -163,22 +165,47 @@ __global__ void __launch_bounds__(256) mlp_wgrad_kernel(int M, int N, int K, con
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int k = k0 + tx * 4 + j;
-      if (k < K) atomicAdd(&dW[(size_t)n * K + k], acc[i][j]);
+      if (k < K) P[((size_t)blockIdx.z * N + n) * K + k] = acc[i][j];
     }
   }
 }
 
-// db[n] += sum_m dZ(m,n)
-__global__ void mlp_bgrad_kernel(int M, int N, const float *dz, const float *mask, float *db) {
-  const int n = blockIdx.x * 32 + (threadIdx.x & 31);
+// sum_m dZ(m,n) over the rows of block row blockIdx.y into Pb[y][n] (the
+// eight warps' sums added in order)
+__global__ void mlp_bgrad_kernel(int M, int N, const float *dz, const float *mask, float *Pb) {
+  __shared__ float part[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = blockIdx.x * 32 + lane;
   float acc = 0.f;
   if (n < N)
-    for (int m = blockIdx.y * 8 + (threadIdx.x >> 5); m < M; m += gridDim.y * 8) {
+    for (int m = blockIdx.y * 8 + warp; m < M; m += gridDim.y * 8) {
       float v = dz[(size_t)m * N + n];
       if (mask && !(mask[(size_t)m * N + n] > 0.f)) v = 0.f;
       acc += v;
     }
-  if (n < N) atomicAdd(&db[n], acc);
+  part[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && n < N) {
+    float t = 0.f;
+    for (int w = 0; w < 8; ++w) t += part[w][lane];
+    Pb[(size_t)blockIdx.y * N + n] = t;
+  }
+}
+
+// dW[i] += sum_z P[z][i] (i < NK) and db[n] += sum_y Pb[y][n], in order
+__global__ void mlp_grad_reduce_kernel(int NK, int splits, const float *P, float *dW, int N, int ysplits,
+                                       const float *Pb, float *db) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NK + N; i += gridDim.x * blockDim.x) {
+    float t = 0.f;
+    if (i < NK) {
+      for (int z = 0; z < splits; ++z) t += P[(size_t)z * NK + i];
+      dW[i] += t;
+    } else if (db) {
+      const int n = i - NK;
+      for (int y = 0; y < ysplits; ++y) t += Pb[(size_t)y * N + n];
+      db[n] += t;
+    }
+  }
 }
 
 // dY[m][o] = 2 (Y - Tn) / (M * nt) for o < nt; loss += sum (Y - Tn)^2
@@ -235,8 +262,12 @@ __global__ void mlp_gather_kernel(int B, long long n, uint32_t seed, const int *
   }
 }
 
-// per-column sums of the training buffer (FP64) for the normalisation
+// per-column sums of the training buffer (FP64) for the normalisation: the
+// partial sums of block x go to sum[x * cols + col] and sq[...], added in
+// order by the host
 __global__ void mlp_stats_kernel(long long n, int cols, const float *a, double *sum, double *sq) {
+  __shared__ double ps[8], pq[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int col = blockIdx.y; col < cols; col += gridDim.y) {
     double s = 0., s2 = 0.;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
@@ -248,10 +279,15 @@ __global__ void mlp_stats_kernel(long long n, int cols, const float *a, double *
       s += __shfl_xor_sync(0xffffffffu, s, o);
       s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
-    if ((threadIdx.x & 31) == 0) {
-      atomicAdd(&sum[col], s);
-      atomicAdd(&sq[col], s2);
+    if (lane == 0) { ps[warp] = s; pq[warp] = s2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0., t2 = 0.;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ps[w]; t2 += pq[w]; }
+      sum[(size_t)blockIdx.x * cols + col] = t;
+      sq[(size_t)blockIdx.x * cols + col] = t2;
     }
+    __syncthreads();
   }
 }
 
@@ -267,24 +303,76 @@ __device__ __forceinline__ void cell_features(const float *mom, long long ms, in
 
 __device__ __forceinline__ int stage_count(int e) { return e == 0 ? 2 : (e == 1 ? 3 : 7); }
 
-// appends (features, targets) of every hit cell to the training buffer
-__global__ void mlp_collect_kernel(int nc, const float *mom, long long ms, const double *hden, const double *te,
-                                   const double *X, const int *flags, long long cap, unsigned long long *count,
-                                   float *xs, float *ts) {
-  for (int c = 1 + blockIdx.x * blockDim.x + threadIdx.x; c <= nc; c += gridDim.x * blockDim.x) {
-    // only states the update balanced (no noTeBal, no noIonBal) teach the model
-    if (!(mom[c] > 0.f) || (flags[c] & 3)) continue;
-    const unsigned long long k = atomicAdd(count, 1ull);
-    if ((long long)k >= cap) continue;
-    float f[kMlpIn];
-    cell_features(mom, ms, c, hden, f);
-    for (int i = 0; i < kMlpIn; ++i) xs[k * kMlpIn + i] = f[i];
-    float *t = ts + k * kMlpOut;
-    t[0] = log10f((float)te[c]);
-    int o = 1;
-    for (int e = 0; e < 7; ++e)
-      for (int s = 1; s <= stage_count(e); ++s) t[o++] = log10f(fmaxf((float)X[((size_t)c * 7 + e) * 8 + s], 1e-20f));
-    for (; o < kMlpOut; ++o) t[o] = 0.f;
+// a cell whose state teaches the model: it has packets and the update
+// balanced it (no noTeBal, no noIonBal)
+__device__ __forceinline__ bool collect_hit(const float *mom, const int *flags, int c) {
+  return mom[c] > 0.f && !(flags[c] & 3);
+}
+
+// The training rows are appended in cell order (reproducible): block b owns
+// cells [1 + b chunk, 1 + (b+1) chunk), counts its rows first, then writes
+// them after the rows of the blocks before it.
+__global__ void mlp_collect_count_kernel(int nc, int chunk, const float *mom, const int *flags, unsigned int *cnt) {
+  const int c0 = 1 + blockIdx.x * chunk, c1 = min(nc + 1, c0 + chunk);
+  unsigned int n = 0;
+  for (int t0 = c0; t0 < c1; t0 += blockDim.x) {
+    const int c = t0 + threadIdx.x;
+    n += __syncthreads_count(c < c1 && collect_hit(mom, flags, c));
+  }
+  if (threadIdx.x == 0) cnt[blockIdx.x] = n;
+}
+
+// writes (features, targets) of the block's hit cells at count + (rows of
+// the blocks before) + (rank within the block); rows past cap are dropped
+__global__ void mlp_collect_kernel(int nc, int chunk, const float *mom, long long ms, const double *hden,
+                                   const double *te, const double *X, const int *flags, long long cap,
+                                   const unsigned long long *count, const unsigned int *cnt, float *xs, float *ts) {
+  __shared__ unsigned int wsum[32];
+  __shared__ unsigned long long sbase;
+  if (threadIdx.x == 0) {
+    unsigned long long b = *count;
+    for (int j = 0; j < (int)blockIdx.x; ++j) b += cnt[j];
+    sbase = b;
+  }
+  __syncthreads();
+  unsigned long long base = sbase;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int c0 = 1 + blockIdx.x * chunk, c1 = min(nc + 1, c0 + chunk);
+  for (int t0 = c0; t0 < c1; t0 += blockDim.x) {
+    const int c = t0 + threadIdx.x;
+    const bool hit = c < c1 && collect_hit(mom, flags, c);
+    const unsigned int bal = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    unsigned int off = __popc(bal & ((1u << lane) - 1u)), tot = 0;
+    for (int w = 0; w < nw; ++w) {
+      const unsigned int v = wsum[w];
+      off += w < warp ? v : 0u;
+      tot += v;
+    }
+    const unsigned long long k = base + off;
+    if (hit && (long long)k < cap) {
+      float f[kMlpIn];
+      cell_features(mom, ms, c, hden, f);
+      for (int i = 0; i < kMlpIn; ++i) xs[k * kMlpIn + i] = f[i];
+      float *t = ts + k * kMlpOut;
+      t[0] = log10f((float)te[c]);
+      int o = 1;
+      for (int e = 0; e < 7; ++e)
+        for (int s = 1; s <= stage_count(e); ++s) t[o++] = log10f(fmaxf((float)X[((size_t)c * 7 + e) * 8 + s], 1e-20f));
+      for (; o < kMlpOut; ++o) t[o] = 0.f;
+    }
+    base += tot;
+    __syncthreads();  // wsum is reused by the next tile
+  }
+}
+
+// count += the rows of every block
+__global__ void mlp_collect_total_kernel(int nblocks, const unsigned int *cnt, unsigned long long *count) {
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int j = 0; j < nblocks; ++j) t += cnt[j];
+    *count += t;
   }
 }
 
@@ -528,19 +616,38 @@ cudaError_t launch_mlp_gemm(int M, int N, int K, const float *a, int lda, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
-                             float *db, int num_sms, cudaStream_t s) {
-  if (M < 1 || N < 1 || K < 1) return cudaErrorInvalidValue;
+// row splits of the weight gradient: enough to fill the SMs twice, at least
+// 64 rows each; the rows per split (a multiple of kTK) in *per
+static int wgrad_splits(int M, int N, int K, int num_sms, int *per) {
   const int tiles = ((N + kTN - 1) / kTN) * ((K + kTN - 1) / kTN);
-  // enough row splits to fill the SMs twice, at least 64 rows each
   int splits = std::max(1, std::min((M + 63) / 64, (2 * num_sms + tiles - 1) / tiles));
-  const int per = ((M + splits - 1) / splits + kTK - 1) / kTK * kTK;
-  splits = (M + per - 1) / per;
-  mlp_wgrad_kernel<<<dim3((N + kTN - 1) / kTN, (K + kTN - 1) / kTN, splits), 256, 0, s>>>(M, N, K, dz, mask, x, dW,
+  *per = ((M + splits - 1) / splits + kTK - 1) / kTK * kTK;
+  return (M + *per - 1) / *per;
+}
+static int bgrad_splits(int M) { return std::max(1, std::min(64, (M + 255) / 256)); }
+
+size_t mlp_wgrad_scratch_floats(int M, int N, int K, int num_sms) {
+  int per = 0;
+  return (size_t)wgrad_splits(M, N, K, num_sms, &per) * N * K + (size_t)bgrad_splits(M) * N;
+}
+
+cudaError_t launch_mlp_wgrad(int M, int N, int K, const float *dz, const float *mask, const float *x, float *dW,
+                             float *db, float *scratch, size_t scratch_floats, int num_sms, cudaStream_t s) {
+  if (M < 1 || N < 1 || K < 1) return cudaErrorInvalidValue;
+  if (!scratch || scratch_floats < mlp_wgrad_scratch_floats(M, N, K, num_sms)) return cudaErrorInvalidValue;
+  int per = 0;
+  const int splits = wgrad_splits(M, N, K, num_sms, &per), ys = bgrad_splits(M);
+  float *P = scratch, *Pb = scratch + (size_t)splits * N * K;
+  mlp_wgrad_kernel<<<dim3((N + kTN - 1) / kTN, (K + kTN - 1) / kTN, splits), 256, 0, s>>>(M, N, K, dz, mask, x, P,
                                                                                           per);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || !db) return e;
-  mlp_bgrad_kernel<<<dim3((N + 31) / 32, std::max(1, std::min(64, (M + 255) / 256))), 256, 0, s>>>(M, N, dz, mask, db);
+  if (e != cudaSuccess) return e;
+  if (db) {
+    mlp_bgrad_kernel<<<dim3((N + 31) / 32, ys), 256, 0, s>>>(M, N, dz, mask, Pb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  const int n = N * K + N;
+  mlp_grad_reduce_kernel<<<std::min((n + 255) / 256, num_sms * 4), 256, 0, s>>>(N * K, splits, P, dW, N, ys, Pb, db);
   return cudaGetLastError();
 }
 
@@ -574,14 +681,24 @@ cudaError_t mlp_prepare() {
 }
 
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s) {
-  mlp_stats_kernel<<<dim3(64, cols), 256, 0, s>>>(n, cols, a, sum, sq);
+  mlp_stats_kernel<<<dim3(kMlpStatBlocks, cols), 256, 0, s>>>(n, cols, a, sum, sq);
   return cudaGetLastError();
 }
 
+int mlp_collect_blocks(int num_sms) { return num_sms * 4; }
+
 cudaError_t launch_mlp_collect(int nc, const float *mom, long long ms, const double *hden, const double *te,
                                const double *X, const int *flags, long long cap, unsigned long long *count, float *xs,
-                               float *ts, int num_sms, cudaStream_t s) {
-  mlp_collect_kernel<<<num_sms * 4, 256, 0, s>>>(nc, mom, ms, hden, te, X, flags, cap, count, xs, ts);
+                               float *ts, unsigned int *blk_counts, int num_sms, cudaStream_t s) {
+  const int nb = mlp_collect_blocks(num_sms);
+  const int chunk = (nc + nb - 1) / nb;
+  if (nc < 1) return cudaSuccess;
+  mlp_collect_count_kernel<<<nb, 256, 0, s>>>(nc, chunk, mom, flags, blk_counts);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mlp_collect_kernel<<<nb, 256, 0, s>>>(nc, chunk, mom, ms, hden, te, X, flags, cap, count, blk_counts, xs, ts);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  mlp_collect_total_kernel<<<1, 32, 0, s>>>(nb, blk_counts, count);
   return cudaGetLastError();
 }
 

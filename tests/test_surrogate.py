@@ -237,3 +237,55 @@ def test_gpu_tensor_core_forward_matches_oracle(gpu_lib, rows):
           np.mean(d <= 2e-5 + 2e-5 * np.abs(oy)), d.max(), int((rows_bad > 0).sum())))
     assert np.mean(d <= 2e-5 + 2e-5 * np.abs(oy)) >= 0.97
     assert d.max() <= 5e-3, d.max()
+
+
+@pytest.mark.gpu
+def test_training_is_reproducible(gpu_lib):
+    """Two trainings from the same rows, seed and initial weights give the
+    same weights bit for bit: the gradients' row splits, the bias sums and
+    the normalisation statistics are added in a fixed order."""
+    rng = np.random.default_rng(7)
+    x = rng.normal(0, 1, (20_000, O.NI)).astype(np.float32)
+    t = rng.normal(0, 1, (20_000, O.NO)).astype(np.float32)
+    neb = nebula.build(nebula.small_cases()[0])
+    out = []
+    for _ in range(2):
+        ctx = transport.TransportContext(neb)
+        ctx.surrogate_init(seed=5, capacity=len(x))
+        ctx.surrogate_load(x, t)
+        loss, _ = ctx.surrogate_train(steps=40, batch=4096, lr=2e-3, seed=3)
+        out.append((loss, ctx.surrogate_params()))
+        ctx.close()
+    # the reported loss is an FP64 sum over the rows in no set order
+    assert abs(out[0][0] - out[1][0]) <= 1e-12 * abs(out[0][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.gpu
+def test_collected_rows_follow_cell_order(gpu_lib):
+    """surrogate_collect appends one row per cell that received packets and
+    that the update balanced (Te and ions), in increasing cell order: row k's
+    first target is log10 Te of the k-th such cell, and collecting twice
+    appends the same rows again."""
+    neb = _clumpy(n=21, packets=400_000)
+    ctx = transport.TransportContext(neb)
+    ctx.set_update_tables(balance.tables(), neb.hden, balance.abundances())
+    te, ne, X = balance.initial_state(neb)
+    ctx.set_cell_state(te, ne, X)
+    w = balance.moment_weights(neb.xs, neb.nu, _ions())
+    ctx.surrogate_init(seed=2, capacity=50_000)
+    ctx.run(seed=11, precision="fp32", zero_first=True)
+    ctx.update_cells(w, 1e-9, precision="fp32")
+    ctx.surrogate_collect()
+    ctx.surrogate_collect()
+    x, t = ctx.surrogate_rows()
+    st = ctx.get_cell_state()
+    ctx.close()
+    te_c, niter, flags = st[0], st[4], st[5]
+    cells = np.nonzero((niter > 0) & ((flags & 3) == 0))[0]
+    cells = cells[cells >= 1]
+    n = len(cells)
+    assert n > 100 and len(x) == 2 * n
+    np.testing.assert_allclose(t[:n, 0], np.log10(te_c[cells].astype(np.float32)), rtol=0, atol=2e-6)
+    np.testing.assert_array_equal(x[n:], x[:n])
+    np.testing.assert_array_equal(t[n:], t[:n])
