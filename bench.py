@@ -443,7 +443,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-opacity", action="store_true")
     ap.add_argument("--lambda-max", type=int, default=12, help="Lambda iterations at most per form (0: skip)")
-    ap.add_argument("--batch-models", type=int, default=16,
+    ap.add_argument("--batch-models", type=int, default=64,
                     help="batched serving: models of the 64-model batch to serve (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--surrogate-rows", type=int, default=1_000_000,

@@ -322,8 +322,9 @@ __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real
 // cel_cooling_smem in FP32 for an ion of N levels known at compile time:
 // every loop unrolled, so the rate matrix, the right-hand side and the
 // populations are registers (no per-thread matrix in local memory) and the
-// table reads take constant offsets.  The same operations in the same order
-// as cel_cooling_smem.
+// table reads take constant offsets.  The same solve as cel_cooling_smem,
+// with the rate factors 8.63e-6 / (g sqrt Te) and 1.4388463 / Te formed
+// once per level (a few FP32 roundings apart from dividing per transition).
 template <int N>
 __device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float Te, float Ne, float up, int top_levels,
                                                  float fscale, float *emis, float escale) {
@@ -369,6 +370,13 @@ __device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float 
   const float aa = nt > 2 ? (logt[khi] - log10Te) / h : 0.f;
   const float bb = nt > 2 ? (log10Te - logt[klo]) / h : 0.f;
   const float ca = aa * aa * aa - aa, cb = bb * bb * bb - bb, h26 = h * h / 6.f;
+  // the per-level factors of the rates, one division per level instead of
+  // two per transition: 8.63e-6 / (g sqrt(Te)), and hc/k / Te
+  const float ic = 1.4388463f / Te;
+  const float i2 = nt == 2 ? (log10Te - logt[0]) / (logt[1] - logt[0]) : 0.f;
+  float ig[N + 1];
+#pragma unroll
+  for (int l = 1; l <= N; ++l) ig[l] = 8.63e-6f / (g[l] * sqrTe);
 #pragma unroll
   for (int lo = 1; lo < N; ++lo)
 #pragma unroll
@@ -376,15 +384,15 @@ __device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float 
       const float *yy = qq + ((size_t)lo * kNL + hi) * kNT;
       float cs;
       if (nt == 1) cs = yy[0];
-      else if (nt == 2) cs = yy[0] + (yy[1] - yy[0]) / (logt[1] - logt[0]) * (log10Te - logt[0]);
+      else if (nt == 2) cs = yy[0] + (yy[1] - yy[0]) * i2;
       else if (below) cs = yy[0];
       else if (above) cs = yy[nt - 1];
       else {
         const float *y2 = q2 + ((size_t)lo * kNL + hi) * kNT;
         cs = aa * yy[klo] + bb * yy[khi] + (ca * y2[klo] + cb * y2[khi]) * h26;
       }
-      const float qex = 8.63e-6f * cs * expf((e[lo] - e[hi]) * 1.4388463f / Te) / (g[lo] * sqrTe);
-      const float qde = 8.63e-6f * cs / (g[hi] * sqrTe);
+      const float qex = cs * expf((e[lo] - e[hi]) * ic) * ig[lo];
+      const float qde = cs * ig[hi];
       const float Ahl = A[hi * kNL + lo];
       X[hi - 1][lo - 1] += Ne * qex;
       X[hi - 1][hi - 1] -= Ne * qde + Ahl;

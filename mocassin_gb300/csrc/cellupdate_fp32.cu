@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "cellupdate.cuh"
+#include "tc_util.cuh"
 
 namespace mcg {
 
@@ -159,7 +160,9 @@ __global__ void grain_flux_kernel(const __grid_constant__ WaveArgs w) {
     for (int r = ty; r < 32; r += 8) {
       const int b = b0 + r, c = c0 + tx;
       float v = 0.f;
-      if (b < nb && c < nc1) v = (float)(g.jste[(size_t)b * nc1 + c] * g.jscale * g.inv_hnu[b]);
+      // FP32 form: Jste rounded by integer operations, times the bin's
+      // jscale / (hcRyd nu) in FP32 (no FP64 arithmetic per element)
+      if (b < nb && c < nc1) v = f64_to_f32_rn(g.jste[(size_t)b * nc1 + c]) * (float)(g.jscale * g.inv_hnu[b]);
       tile[r][tx] = v;
     }
     __syncthreads();

@@ -19,6 +19,7 @@
 
 #include "../../include/mocassin_gpu.h"
 #include "mc_device.cuh"
+#include "tc_util.cuh"
 #include "mc_launch.h"
 #include "wave_types.cuh"
 
@@ -66,6 +67,14 @@ struct DBuf {
   }
   template <typename T> T *as() const { return (T *)p; }
 };
+
+// (re)allocates b to at least `bytes` (contents not kept)
+mc_status ensure(DBuf &b, size_t bytes) {
+  if (b.p && b.bytes >= bytes) return MC_OK;
+  if (b.p) { cudaFree(b.p); b.p = nullptr; b.bytes = 0; }
+  MC_CUDA(b.alloc(bytes));
+  return MC_OK;
+}
 
 }  // namespace
 
@@ -142,6 +151,8 @@ struct mc_ctx {
   // (it cleared what it had made nonzero after downloading it), so the next
   // one needs no full clear
   bool est_zero = false;
+  unsigned long long *h_cnt = nullptr;  // pinned: the compacted escape count
+  cudaEvent_t ev_done = nullptr;        // the transport's end, for the side stream
   DBuf view;        // viewing-angle table (n_angle > 0)
   int n_angle = 0;
   // cell update: atomic tables, per-cell state and scratch
@@ -354,6 +365,12 @@ mc_status upload_arrays(mc_ctx *c, const mc_grid_t *g, bool first, cudaStream_t 
   if (g->g_sca && (st = put(c->gsca, g->g_sca, (size_t)nb * sizeof(float)))) return st;
   if (g->rec_pdf) {
     const cudaStream_t cs = cdf_stream ? cdf_stream : s;
+    if (cs != s && c->ev_side0) {
+      // the recPDF copy starts once the opacity rows are up: round 0 needs
+      // them, and the two copies would share the host link
+      MC_CUDA(cudaEventRecord(c->ev_side0, s));
+      MC_CUDA(cudaStreamWaitEvent(cs, c->ev_side0, 0));
+    }
     c->xfer_h2d += (long long)plane;
     if (first || !c->rec_raw.p) {
       if ((st = upload(c->rec_raw, g->rec_pdf, plane, cs))) return st;
@@ -1233,7 +1250,9 @@ void mc_ctx_destroy(mc_ctx_t *c) {
   if (c->side) cudaStreamSynchronize(c->side);
   if (c->ev_side0) cudaEventDestroy(c->ev_side0);
   if (c->ev_cdf) cudaEventDestroy(c->ev_cdf);
+  if (c->ev_done) cudaEventDestroy(c->ev_done);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->h_cnt) cudaFreeHost(c->h_cnt);
   cudaStream_t s = c->stream;
   delete c;  // frees the device buffers
   if (s) cudaStreamDestroy(s);
@@ -1353,6 +1372,8 @@ extern "C" mc_status mc_ctx_dust_temperatures(mc_ctx_t *c, int32_t nsizes, const
   MC_CUDA(dg.alloc((size_t)nsizes * sizeof(float)));
   if (!dt.p) MC_CUDA(dt.alloc((size_t)nout * nc1 * sizeof(float)));
   c->d_nsizes = nsizes;
+  // cell 0 (outside the grid) is never written by the kernel: it stays 0
+  MC_CUDA(cudaMemsetAsync(dt.p, 0, dt.bytes, c->stream));
   MC_CUDA(err.alloc(sizeof(int)));
   cudaStream_t s = c->stream;
   MC_CUDA(cudaMemcpyAsync(dw.p, w.data(), dw.bytes, cudaMemcpyHostToDevice, s));
@@ -1909,12 +1930,6 @@ using mcg::kMlpHid;
 using mcg::kMlpOut;
 using mcg::kMlpParams;
 
-mc_status ensure(DBuf &b, size_t bytes) {
-  if (b.p && b.bytes >= bytes) return MC_OK;
-  if (b.p) { cudaFree(b.p); b.p = nullptr; b.bytes = 0; }
-  MC_CUDA(b.alloc(bytes));
-  return MC_OK;
-}
 
 // forward pass of M rows: x [M][80] -> a1, a2, a3 [M][256] -> y [M][48]
 // the four layers of M rows; tensor: on tcgen05 (the prediction over a
@@ -2751,7 +2766,7 @@ __global__ void widen_kernel(const float *__restrict__ in, double *__restrict__ 
 }
 __global__ void narrow_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+    out[i] = mcg::f64_to_f32_rn(in[i]);
 }
 
 // The first frequency bin a packet can march in: on a gas-only grid the
@@ -2774,7 +2789,7 @@ __global__ void row_nonzero_kernel(const double *__restrict__ a, long long len, 
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
     const double v = r[i];
     nz |= v != 0.0;
-    if (o) o[i] = (float)v;
+    if (o) o[i] = mcg::f64_to_f32_rn(v);
   }
   if (__syncthreads_or(nz) && threadIdx.x == 0) flag[blockIdx.y] = 1;
 }
@@ -2798,7 +2813,7 @@ __global__ void compact_nonzero_kernel(const double *__restrict__ a, unsigned lo
       const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
       if (slot < cap) {
         idx[slot] = (uint32_t)i;
-        if (f32) ((float *)val)[slot] = (float)v;
+        if (f32) ((float *)val)[slot] = mcg::f64_to_f32_rn(v);
         else ((double *)val)[slot] = v;
       }
     }
@@ -2862,8 +2877,10 @@ mc_status download_rows(mc_ctx *c, const DBuf &d, const DBuf *stage, void *h, lo
 // compacted on the device and scattered into the caller's array (by the
 // device into pinned memory, by the host otherwise); a dense copy when they
 // are too many for the pair buffers.
-mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32, bool rezero) {
-  cudaStream_t s = c->stream;
+// The compaction and the count's copy are queued on stream s by
+// sparse_begin, which returns at once; sparse_end waits for the count and
+// queues the rest on the same stream.
+mc_status sparse_begin(mc_ctx *c, const DBuf &d, bool f32, cudaStream_t s) {
   mc_status st;
   const unsigned long long n = d.bytes / sizeof(double);
   const unsigned long long cap = std::min<unsigned long long>(n, 1ull << 24);
@@ -2874,11 +2891,22 @@ mc_status download_sparse(mc_ctx *c, const DBuf &d, void *h, bool f32, bool reze
   compact_nonzero_kernel<<<c->num_sms * 8, 256, 0, s>>>(d.as<double>(), n, c->z_idx.as<uint32_t>(), c->z_val.p,
                                                          f32 ? 1 : 0, cap, c->z_cnt.as<unsigned long long>());
   MC_CUDA(cudaGetLastError());
-  unsigned long long cnt = 0;
-  MC_CUDA(cudaMemcpyAsync(&cnt, c->z_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  if (!c->h_cnt && cudaHostAlloc((void **)&c->h_cnt, sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    c->h_cnt = nullptr;
+    return set_error(MC_ERR_CUDA, "pinned count allocation failed");
+  }
+  MC_CUDA(cudaMemcpyAsync(c->h_cnt, c->z_cnt.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  return MC_OK;
+}
+
+mc_status sparse_end(mc_ctx *c, const DBuf &d, void *h, bool f32, bool rezero, cudaStream_t s) {
+  const unsigned long long n = d.bytes / sizeof(double);
+  const unsigned long long cap = std::min<unsigned long long>(n, 1ull << 24);
   MC_CUDA(cudaStreamSynchronize(s));
+  const unsigned long long cnt = *c->h_cnt;
   const size_t elt = f32 ? sizeof(float) : sizeof(double);
-  c->xfer_d2h += (long long)sizeof cnt;
+  c->xfer_d2h += (long long)sizeof(unsigned long long);
   if (cnt > cap) {
     if (!f32) {
       MC_CUDA(cudaMemcpyAsync(h, d.p, d.bytes, cudaMemcpyDeviceToHost, s));
@@ -3025,6 +3053,16 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     // directly), so that the next call starts from zero without a full clear
     const long long len = c->nc + 1;
     bool all = c->identity;
+    // the escapes are compacted on the side stream while the Jste rows are
+    // scanned and copied on the main one
+    cudaStream_t es = s;
+    if (c->esc.p && escaped && c->side) {
+      if (!c->ev_done) MC_CUDA(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));
+      MC_CUDA(cudaEventRecord(c->ev_done, s));
+      MC_CUDA(cudaStreamWaitEvent(c->side, c->ev_done, 0));
+      es = c->side;
+    }
+    if (c->esc.p && escaped && (st = sparse_begin(c, c->esc, f32, es))) return st;
     for (int k = 0; k < 2; ++k) {
       Item &it = items[k];
       if (!it.d->p) continue;
@@ -3034,11 +3072,12 @@ mc_status transport_run_impl(const mc_grid_t *g, const mc_source_t *src, int32_t
     }
     if (c->esc.p) {
       if (escaped) {
-        if ((st = download_sparse(c, c->esc, escaped, f32, c->identity))) return st;
+        if ((st = sparse_end(c, c->esc, escaped, f32, c->identity, es))) return st;
       } else {
         all = false;
       }
     }
+    MC_CUDA(cudaStreamSynchronize(es));
     MC_CUDA(cudaStreamSynchronize(s));
     c->est_zero = all;
     return counted(MC_OK);

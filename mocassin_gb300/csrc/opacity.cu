@@ -223,6 +223,153 @@ __global__ void __launch_bounds__(128, 4) opacity_tc_kernel(const __grid_constan
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOpN));
 }
 
+// opacity_pipe_kernel: the same contraction with the epilogue overlapped.
+// A persistent CTA of 8 warps holds one 128-bin tile of XS (hi/lo) and walks
+// 128-cell tiles: two A buffers and two TMEM accumulators, so the MMAs of
+// tile i run while the threads store tile i - 1 (each warp 32 cells x 64
+// bins, coalesced along cells) and load the densities of tile i + 1.  The
+// MMAs of a tile are those of opacity_tc_kernel in the same order.
+constexpr int kOpPThreads = 256;
+
+__global__ void __launch_bounds__(kOpPThreads, 2) opacity_pipe_kernel(const __grid_constant__ OpacityTcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int K = a.K;
+  const uint32_t tile_bytes = (uint32_t)kOpM * K * 2;  // 128 x K bf16
+  unsigned char *sBhi = sm, *sBlo = sm + tile_bytes;
+  auto sA = [&](int b) { return sm + (2u + 2u * (uint32_t)b) * tile_bytes; };  // hi, then lo
+  uint64_t *mdone = (uint64_t *)(sm + 6 * tile_bytes);
+  uint32_t *tslot = (uint32_t *)(mdone + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nvt = (a.nb + kOpN - 1) / kOpN, ntiles = (a.nc1 + kOpM - 1) / kOpM;
+  // block -> (bin tile, first cell tile, stride): the blocks of a bin tile
+  // take its cell tiles in turn
+  const int per = (int)gridDim.x / nvt;  // blocks per bin tile (the launch makes gridDim a multiple of nvt)
+  const int vt = (int)blockIdx.x / per, t0 = (int)blockIdx.x % per;
+  const int v0 = vt * kOpN;
+  for (int i = tid; i < kOpN * K; i += blockDim.x) {
+    const int r = i / K, k = i % K;
+    const int v = v0 + r;
+    const float x = (k < a.nspecies && v < a.nb) ? __ldg(a.xs + (long long)k * a.nb + v) : 0.f;
+    __nv_bfloat16 hi, lo;
+    split_bf16(x, hi, lo);
+    *(__nv_bfloat16 *)(sBhi + kmajor_off(r, k, K)) = hi;
+    *(__nv_bfloat16 *)(sBlo + kmajor_off(r, k, K)) = lo;
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mdone + i)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(2 * kOpN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = mma_idesc(kOpM, kOpN);
+  const uint32_t lbo = 128, sbo = (uint32_t)(K / 8) * 128;
+  const int mytiles = t0 < ntiles ? (ntiles - 1 - t0) / per + 1 : 0;
+  uint32_t ph = 0u;  // bit b: the next phase of mdone[b]
+  bool ok = true, failed = false;
+  int last_b = -1;
+  uint32_t last_ph = 0u, cph = 0u;  // thread 0: the last commit and the next commit phases (bit b)
+
+  // stores tile i from accumulator i & 1 once its MMAs are done
+  auto epilogue = [&](int i) {
+    const int b = i & 1;
+    ok = mbar_wait(smem_addr(mdone + b), (ph >> b) & 1u) && ok;
+    ph ^= 1u << b;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int q = warp & 3, h = warp >> 2;
+    const int c = (t0 + i * per) * kOpM + q * 32 + lane;
+    const float f = (a.ff && c < a.nc1 && v0 == 0 && h == 0) ? __ldg(a.ff + c) : 0.f;
+    for (int j0 = 0; j0 < kOpN / 2; j0 += 32) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)b * kOpN + (uint32_t)(h * (kOpN / 2) + j0), r);
+      if (c < a.nc1) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int v = v0 + h * (kOpN / 2) + j0 + j;
+          if (v < a.nb) {
+            float x = __uint_as_float(r[j]);
+            if (v == 0) x += f;
+            a.out[(long long)v * a.nc1 + c] = x;
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  };
+
+  for (int i = 0; i < mytiles; ++i) {
+    const int b = i & 1, c0 = (t0 + i * per) * kOpM;
+    // A = den^T of this tile into buffer b (free: the epilogue of tile i - 2,
+    // which waited for its MMAs, ran in the previous step)
+    {
+      const int r = tid & (kOpM - 1), kh = tid >> 7;  // cell row, species half
+      const int c = c0 + r;
+      const int kb = kh * (kOpKMax / 2);
+      float x[kOpKMax / 2];
+#pragma unroll
+      for (int k = 0; k < kOpKMax / 2; ++k)
+        x[k] = (kb + k < a.nspecies && c < a.nc1) ? __ldg(a.den + (long long)(kb + k) * a.nc1 + c) : 0.f;
+#pragma unroll
+      for (int kc = 0; kc < kOpKMax / 16; ++kc) {
+        if (kb + kc * 8 >= K) break;
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) pack_split(x[kc * 8 + 2 * j], x[kc * 8 + 2 * j + 1], hw[j], lw[j]);
+        const uint32_t off = kmajor_off(r, kb + kc * 8, K);
+        *(uint4 *)(sA(b) + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *(uint4 *)(sA(b) + tile_bytes + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    failed = __syncthreads_or(!ok);
+    if (failed) break;
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + (uint32_t)b * kOpN;
+      const uint32_t ah = smem_addr(sA(b)), al = ah + tile_bytes, bh = smem_addr(sBhi), bl = smem_addr(sBlo);
+      int first = 1;
+      for (int s = 0; s < K / 16; ++s) {
+        const uint32_t ko = (uint32_t)s * 256;
+        const uint64_t dAh = smem_desc(ah + ko, lbo, sbo), dAl = smem_desc(al + ko, lbo, sbo);
+        const uint64_t dBh = smem_desc(bh + ko, lbo, sbo), dBl = smem_desc(bl + ko, lbo, sbo);
+        umma_bf16(d, dAh, dBh, idesc, first ? 0u : 1u);
+        first = 0;
+        umma_bf16(d, dAh, dBl, idesc, 1u);
+        umma_bf16(d, dAl, dBh, idesc, 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_addr(mdone + b))
+                   : "memory");
+      last_b = b;
+      last_ph = (cph >> b) & 1u;
+      cph ^= 1u << b;
+    }
+    // the previous tile's stores overlap this tile's MMAs
+    if (i >= 1) epilogue(i - 1);
+  }
+  if (!failed && mytiles > 0) {
+    epilogue(mytiles - 1);
+    failed = __syncthreads_or(!ok);
+  } else {
+    __syncthreads();
+  }
+  if (failed && tid == 0) atomicExch(a.error, (int)MC_ERR_TIMEOUT);
+  if (tid == 0 && last_b >= 0) (void)mbar_wait(smem_addr(mdone + last_b), last_ph);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kOpN));
+}
+
+size_t opacity_pipe_smem(int K) { return (size_t)6 * kOpM * K * 2 + 64; }
+
 size_t opacity_tc_smem(int K) { return (size_t)4 * kOpM * K * 2 + 64; }
 
 cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const float *den, const float *xs,
@@ -242,6 +389,20 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
   a.K = ((nspecies + 15) / 16) * 16;
   a.nb = nb;
   a.den = den; a.xs = xs; a.ff = ff; a.out = out; a.error = error;
+  if (a.K <= kOpKMax) {
+    // the pipelined kernel: two CTAs per SM (2 x 256 TMEM columns), the
+    // blocks split evenly over the bin tiles
+    const size_t shp = opacity_pipe_smem(a.K);
+    cudaError_t e = cudaFuncSetAttribute(opacity_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shp);
+    if (e != cudaSuccess) return e;
+    const int nvt = (nb + kOpN - 1) / kOpN;
+    const int ntiles = (nc1 + kOpM - 1) / kOpM;
+    int per = (2 * num_sms) / nvt;
+    if (per > ntiles) per = ntiles;
+    if (per < 1) per = 1;
+    opacity_pipe_kernel<<<nvt * per, kOpPThreads, shp, stream>>>(a);
+    return cudaGetLastError();
+  }
   const size_t sh = opacity_tc_smem(a.K);
   cudaError_t e = cudaFuncSetAttribute(opacity_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
   if (e != cudaSuccess) return e;

@@ -75,6 +75,24 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// (float)d, rounded to nearest even, by integer operations on the IEEE-754
+// layouts (GB300 runs FP64 arithmetic and FP64 -> FP32 conversions at a
+// small fraction of its FP32 rate): for results that are normal floats;
+// zeros, subnormal or overflowing results, infinities and NaNs take the
+// conversion instruction.
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((u >> 52) & 0x7ff) - 1023 + 127;  // the float's biased exponent
+  if (e <= 0 || e >= 255) return (float)d;
+  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;  // 52 mantissa bits
+  const uint32_t keep = (uint32_t)(m >> 29), rest = (uint32_t)(m & 0x1FFFFFFFull);
+  const uint32_t up = (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+  // a carry out of the mantissa moves into the exponent, as rounding does
+  const uint32_t bits = ((uint32_t)(u >> 32) & 0x80000000u) | (((uint32_t)e << 23) + keep + up);
+  if (((bits >> 23) & 0xFFu) == 0xFFu) return (float)d;  // rounded up to infinity
+  return __uint_as_float(bits);
+}
+
 // Two packed BF16 (hi, lo) words of x0, x1.
 __device__ __forceinline__ void pack_split(float x0, float x1, uint32_t &hw, uint32_t &lw) {
   __nv_bfloat16 h0, l0, h1, l1;

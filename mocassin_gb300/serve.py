@@ -154,10 +154,24 @@ class ModelServer:
                 self.peak_models = max(self.peak_models, self._resident_models)
                 lis = []
                 try:
-                    for neb in nebs:
+                    # the group's models are set up (context, tables, tuning) on the pool's threads at once
+                    def setup(neb):
                         li = iterate.LambdaIteration(neb, form="wave", update=self.update)
-                        lis.append(li)
-                        self._tune(li, neb, "wave")
+                        try:
+                            self._tune(li, neb, "wave")
+                        except Exception:
+                            li.close()
+                            raise
+                        return li
+                    futs = [pool.submit(setup, neb) for neb in nebs]
+                    err = None
+                    for f in futs:
+                        try:
+                            lis.append(f.result())
+                        except Exception as exc:
+                            err = err or exc
+                    if err is not None:
+                        raise err
                     t0 = time.perf_counter()
                     lat = [[] for _ in lis]
                     cross = [0] * len(lis)

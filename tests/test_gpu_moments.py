@@ -55,3 +55,24 @@ def test_host_weight_table_matches_the_oracle_formula():
     neb = nebula.build(nebula.small_cases()[0])
     np.testing.assert_allclose(rates.photo_weights(neb.xs, neb.nu),
                                rates_oracle.photo_weights(neb.xs, neb.nu), rtol=1e-7)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nout", [16, 67])
+def test_moments_of_a_grid_of_many_tiles(gpu_lib, nout):
+    """A 41^3 grid (539 tiles of 128 cells): the persistent CTAs take
+    several tiles each (the accumulator reused from tile to tile), and two
+    calls give the same sums."""
+    import dataclasses
+    neb = nebula.build(dataclasses.replace(nebula.clumpy61(300_000), name="clumpy41", n=41))
+    ctx = transport.TransportContext(neb)
+    ctx.run(seed=5, precision="fp32")
+    js, _, _ = ctx.download()
+    w = np.random.default_rng(100 + nout).lognormal(0, 2, (neb.nbins, nout)).astype(np.float32)
+    got, _ = ctx.jste_moments(w, 0.25)
+    again, _ = ctx.jste_moments(w, 0.25)
+    ctx.close()
+    ref = rates_oracle.moments(js, w, 0.25)
+    err = np.abs(got.astype(np.float64) - ref)
+    assert np.all(err <= TOL * np.abs(ref) + 1e-300), float((err / (np.abs(ref) + 1e-300)).max())
+    np.testing.assert_array_equal(got, again)

@@ -3,6 +3,8 @@
 FP32 CUDA-core path: 2e-6 relative per element.  Tensor-core path (tcgen05,
 two-term split BF16, FP32 accumulate): 3e-5 relative per element (all terms
 are non-negative, so the missing lo*lo term bounds the error by ~1.5e-5).
+The 70001-cell shape gives each CTA of the pipelined kernel several cell
+tiles (its double-buffered accumulators and overlapped stores).
 """
 import numpy as np
 import pytest
@@ -32,7 +34,8 @@ def _check(got, ref, tol):
 
 
 @pytest.mark.parametrize("method", ["fp32", "bf16x3"])
-@pytest.mark.parametrize("shape", [(16, 128, 128), (37, 1, 600), (37, 1000, 600), (47, 4097, 257), (64, 300, 33)])
+@pytest.mark.parametrize("shape", [(16, 128, 128), (37, 1, 600), (37, 1000, 600), (47, 4097, 257), (64, 300, 33),
+                                   (48, 70001, 600)])
 def test_opacity_matches_oracle(gpu_lib, method, shape):
     k, nc1, nb = shape
     den, xs, ff = _case(k, nc1, nb, seed=nc1 + nb)
