@@ -319,24 +319,89 @@ __device__ Real cel_cooling_smem(const UpdArgs &a, int k, Real Te, Real Ne, Real
   return cool;
 }
 
+// The tables of one line ion as cel_cooling_reg reads them: straight from
+// the device tables (CelTabGlobal), or from a warp's staged copy in shared
+// memory (CelTabStaged: the N (N - 1) / 2 transitions' collision-strength
+// rows, kNT apart, and A values packed by transition index).  Both give the
+// same values.
+struct CelTabGlobal {
+  const float *logt_, *g_, *e_, *A, *qq, *q2;
+  __device__ __forceinline__ CelTabGlobal(const UpdTabs<float> &T, int k)
+      : logt_(T.logt + (size_t)k * kNT), g_(T.g + (size_t)k * kNL), e_(T.e + (size_t)k * kNL),
+        A(T.A + (size_t)k * kNL * kNL), qq(T.qq + (size_t)k * kNL * kNL * kNT), q2(T.q2 + (size_t)k * kNL * kNL * kNT) {}
+  __device__ __forceinline__ const float *logt() const { return logt_; }
+  __device__ __forceinline__ const float *g() const { return g_; }
+  __device__ __forceinline__ const float *e() const { return e_; }
+  template <int N> __device__ __forceinline__ float a(int lo, int hi) const { return A[hi * kNL + lo]; }
+  template <int N> __device__ __forceinline__ const float *y(int lo, int hi) const {
+    return qq + ((size_t)lo * kNL + hi) * kNT;
+  }
+  template <int N> __device__ __forceinline__ const float *y2(int lo, int hi) const {
+    return q2 + ((size_t)lo * kNL + hi) * kNT;
+  }
+};
+
+// index of transition (lo, hi), 1 <= lo < hi <= N, in lo-major order
+__host__ __device__ constexpr int cel_pair(int lo, int hi, int N) { return (lo - 1) * (2 * N - lo) / 2 + (hi - lo - 1); }
+
+constexpr int kCelMaxPairs = 15 * 14 / 2;  // the register form's largest ion
+// floats of one warp's staged tables: logt, g, e, A by transition, two rows
+// of kNT collision strengths per transition
+constexpr int kCelStage = kNT + 2 * kNL + kCelMaxPairs + 2 * kCelMaxPairs * kNT;
+
+// one base pointer: every table sits at a fixed offset from it
+struct CelTabStaged {
+  const float *s;
+  int nt;
+  static constexpr int kG = kNT, kE = kNT + kNL, kA = kNT + 2 * kNL, kQ = kA + kCelMaxPairs,
+                       kQ2 = kQ + kCelMaxPairs * kNT;
+  __device__ __forceinline__ CelTabStaged(const float *s_, int nt_) : s(s_), nt(nt_) {}
+  __device__ __forceinline__ const float *logt() const { return s; }
+  __device__ __forceinline__ const float *g() const { return s + kG; }
+  __device__ __forceinline__ const float *e() const { return s + kE; }
+  template <int N> __device__ __forceinline__ float a(int lo, int hi) const { return s[kA + cel_pair(lo, hi, N)]; }
+  template <int N> __device__ __forceinline__ const float *y(int lo, int hi) const {
+    return s + kQ + cel_pair(lo, hi, N) * kNT;
+  }
+  template <int N> __device__ __forceinline__ const float *y2(int lo, int hi) const {
+    return s + kQ2 + cel_pair(lo, hi, N) * kNT;
+  }
+};
+
+// the warp copies line ion k's tables (N levels, nt temperatures) into s
+__device__ __forceinline__ void cel_stage(const UpdTabs<float> &T, int k, int N, int nt, float *s, int lane) {
+  const CelTabGlobal G(T, k);
+  float *logt = s, *g = s + CelTabStaged::kG, *e = s + CelTabStaged::kE, *A = s + CelTabStaged::kA;
+  float *qq = s + CelTabStaged::kQ, *q2 = s + CelTabStaged::kQ2;
+  if (lane < nt) logt[lane] = G.logt()[lane];
+  if (lane <= N) { g[lane] = G.g()[lane]; e[lane] = G.e()[lane]; }
+  int p = 0;
+  for (int lo = 1; lo < N; ++lo)
+    for (int hi = lo + 1; hi <= N; ++hi, ++p) {
+      if (lane == 0) A[p] = G.A[hi * kNL + lo];
+      if (lane < nt) {
+        const size_t row = ((size_t)lo * kNL + hi) * kNT + lane;
+        qq[p * kNT + lane] = G.qq[row];
+        q2[p * kNT + lane] = G.q2[row];
+      }
+    }
+}
+
 // cel_cooling_smem in FP32 for an ion of N levels known at compile time:
 // every loop unrolled, so the rate matrix, the right-hand side and the
 // populations are registers (no per-thread matrix in local memory) and the
 // table reads take constant offsets.  The same solve as cel_cooling_smem,
 // with the rate factors 8.63e-6 / (g sqrt Te) and 1.4388463 / Te formed
 // once per level (a few FP32 roundings apart from dividing per transition).
-template <int N>
-__device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float Te, float Ne, float up, int top_levels,
-                                                 float fscale, float *emis, float escale) {
+template <int N, typename Tab>
+__device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, const Tab &tb, float Te, float Ne, float up,
+                                                 int top_levels, float fscale, float *emis, float escale) {
   const UpdTabs<float> &T = a.f;
   if (emis) *emis = 0.f;
   if (up != up) return 0.f;
   const UpdCelT<float> &c = T.cel[k];
   const int nt = c.nt;
-  const float *logt = T.logt + (size_t)k * kNT;
-  const float *g = T.g + (size_t)k * kNL, *e = T.e + (size_t)k * kNL;
-  const float *A = T.A + (size_t)k * kNL * kNL;
-  const float *qq = T.qq + (size_t)k * kNL * kNL * kNT, *q2 = T.q2 + (size_t)k * kNL * kNL * kNT;
+  const float *logt = tb.logt(), *g = tb.g(), *e = tb.e();
   const float sqrTe = sqrtf(Te), log10Te = log10f(Te);
   float X[N][N], y[N];  // X[i][j] is row i + 1, column j + 1 of the 1-based system
   float arec = 0.f;
@@ -381,19 +446,19 @@ __device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float 
   for (int lo = 1; lo < N; ++lo)
 #pragma unroll
     for (int hi = lo + 1; hi <= N; ++hi) {
-      const float *yy = qq + ((size_t)lo * kNL + hi) * kNT;
+      const float *yy = tb.template y<N>(lo, hi);
       float cs;
       if (nt == 1) cs = yy[0];
       else if (nt == 2) cs = yy[0] + (yy[1] - yy[0]) * i2;
       else if (below) cs = yy[0];
       else if (above) cs = yy[nt - 1];
       else {
-        const float *y2 = q2 + ((size_t)lo * kNL + hi) * kNT;
+        const float *y2 = tb.template y2<N>(lo, hi);
         cs = aa * yy[klo] + bb * yy[khi] + (ca * y2[klo] + cb * y2[khi]) * h26;
       }
       const float qex = cs * expf((e[lo] - e[hi]) * ic) * ig[lo];
       const float qde = cs * ig[hi];
-      const float Ahl = A[hi * kNL + lo];
+      const float Ahl = tb.template a<N>(lo, hi);
       X[hi - 1][lo - 1] += Ne * qex;
       X[hi - 1][hi - 1] -= Ne * qde + Ahl;
       if (lo >= 2) {
@@ -428,36 +493,47 @@ __device__ __forceinline__ float cel_cooling_reg(const UpdArgs &a, int k, float 
 #pragma unroll
   for (int i = 1; i <= N - 1; ++i)
 #pragma unroll
-    for (int j = i + 1; j <= N; ++j)
-      if (j <= top && A[j * kNL + i] != 0.f) {
-        const float line = A[j * kNL + i] * (e[j] - e[i]) * (y[j - 1] * inv);
+    for (int j = i + 1; j <= N; ++j) {
+      const float Aji = tb.template a<N>(i, j);
+      if (j <= top && Aji != 0.f) {
+        const float line = Aji * (e[j] - e[i]) * (y[j - 1] * inv);
         if (!(fscale > 0.f)) cool += line;
         else if (line * fscale > 1e-35f) cool += line * fscale;
       }
+    }
   if (emis) {
     float em = 0.f;
 #pragma unroll
     for (int i = 1; i <= N - 1; ++i)
 #pragma unroll
-      for (int j = i + 1; j <= N; ++j)
-        if (A[j * kNL + i] != 0.f) {
-          const float line = A[j * kNL + i] * (e[j] - e[i]) * (y[j - 1] * inv) * escale;
+      for (int j = i + 1; j <= N; ++j) {
+        const float Aji = tb.template a<N>(i, j);
+        if (Aji != 0.f) {
+          const float line = Aji * (e[j] - e[i]) * (y[j - 1] * inv) * escale;
           if (line > 1e-35f) em += line;
         }
+      }
     *emis = em;
   }
   return cool;
 }
 
-// the FP32 level populations of line ion k: the register form for the
-// level counts the line ions of the atomic data have (2, 3, 5, 6, 7, 9, 10,
-// 12, 13, 15), cel_cooling_smem on the scratch matrix M (L rows) otherwise
-__device__ __forceinline__ float cel_cooling_f32(const UpdArgs &a, int k, float Te, float Ne, float up, float *M, int L,
-                                                 int top_levels, float fscale, float *emis = nullptr,
+// whether line ion k has a register form (the level counts the line ions of
+// the atomic data have: 2, 3, 5, 6, 7, 9, 10, 12, 13, 15)
+__device__ __forceinline__ bool cel_has_reg(int n) {
+  return n == 2 || n == 3 || n == 5 || n == 6 || n == 7 || n == 9 || n == 10 || n == 12 || n == 13 || n == 15;
+}
+
+// the FP32 level populations of line ion k with the tables tb: the register
+// form for its level count, cel_cooling_smem on the device tables and the
+// scratch matrix M (L rows) otherwise
+template <typename Tab>
+__device__ __forceinline__ float cel_cooling_f32(const UpdArgs &a, int k, const Tab &tb, float Te, float Ne, float up,
+                                                 float *M, int L, int top_levels, float fscale, float *emis = nullptr,
                                                  float escale = 0.f) {
   switch (a.f.cel[k].nlev) {
 #define MC_CEL_CASE(n) \
-  case n: return cel_cooling_reg<n>(a, k, Te, Ne, up, top_levels, fscale, emis, escale);
+  case n: return cel_cooling_reg<n>(a, k, tb, Te, Ne, up, top_levels, fscale, emis, escale);
     MC_CEL_CASE(2) MC_CEL_CASE(3) MC_CEL_CASE(5) MC_CEL_CASE(6) MC_CEL_CASE(7) MC_CEL_CASE(9) MC_CEL_CASE(10)
     MC_CEL_CASE(12) MC_CEL_CASE(13) MC_CEL_CASE(15)
 #undef MC_CEL_CASE

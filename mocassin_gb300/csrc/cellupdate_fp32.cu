@@ -46,6 +46,7 @@ struct WaveArgs {
   float *gpf;            // [nc+1][nbp] grains: each cell's photon flux Jste x scale / (hcRyd nu) per bin
   int *act[2];        // active lists
   int *count;         // [2] their lengths
+  unsigned int *cel_ctr;  // the level-population kernel's task counter (reset each T step)
 };
 
 __device__ __forceinline__ float &XS(const WaveArgs &w, int slot, int c) {
@@ -214,21 +215,44 @@ __global__ void __launch_bounds__(128) wave_grain_kernel(const __grid_constant__
 // length of the largest ion (mat_rows): the fewer bytes a thread touches, the
 // more of the resident threads' matrices stay in the L1.
 __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ WaveArgs w, int cur) {
+  extern __shared__ float cel_stage_smem[];
   const UpdArgs &a = w.a;
   const UpdTabs<float> &T = a.f;
   const int n = w.count[cur];
-  const long long total = (long long)n * a.ncel;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
-       q += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(q / n), c = w.act[cur][q % n];
+  const int lane = threadIdx.x & 31;
+  // tasks of 32 active cells of one line ion, ion-major, handed out by a
+  // counter: the warps move through the list together, so a warp's next
+  // task is mostly of the ion whose tables it has staged
+  const unsigned int nchunk = (unsigned int)(n + 31) / 32u;
+  const unsigned int total = nchunk * (unsigned int)a.ncel;
+  float *stage = cel_stage_smem + (threadIdx.x >> 5) * kCelStage;
+  int staged = -1;
+  float x[kNL * kNL];
+  while (true) {
+    unsigned int t = 0;
+    if (lane == 0) t = atomicAdd(w.cel_ctr, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= total) break;
+    const int k = (int)(t / nchunk), ci = (int)(t % nchunk) * 32 + lane;
     const UpdCelT<float> &C = T.cel[k];
+    const bool reg = cel_has_reg(C.nlev);
+    if (reg && k != staged) {
+      __syncwarp();
+      cel_stage(T, k, C.nlev, C.nt, stage, lane);
+      __syncwarp();
+      staged = k;
+    }
+    if (ci >= n) continue;
+    const int c = w.act[cur][ci];
     const float Te = w.Te[c], Ne = w.Ne[c];
     const float xi = XS(w, C.e * kNX + C.ion, c);
     const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
-    float x[kNL * kNL];
     float emis = 0.f;
-    const float cool = cel_cooling_f32(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f, a.forb_out ? &emis : nullptr,
-                                       T.ab[C.e] * xi * 1.9865e9f);
+    const float es = T.ab[C.e] * xi * 1.9865e9f;
+    const float cool = reg ? cel_cooling_f32(a, k, CelTabStaged(stage, C.nt), Te, Ne, up, x, a.mat_rows, 10, 0.f,
+                                             a.forb_out ? &emis : nullptr, es)
+                           : cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f,
+                                                     a.forb_out ? &emis : nullptr, es);
     w.cool[(size_t)k * (a.nc + 1) + c] = cool * T.ab[C.e] * xi * 1.9865e-16f;
     if (a.forb_out) a.forb_out[(size_t)k * (a.nc + 1) + c] = emis;
   }
@@ -352,12 +376,19 @@ __global__ void __launch_bounds__(128) wave_therm_kernel(const __grid_constant__
   }
 }
 
-__global__ void wave_reset_kernel(int *count, int slot) { count[slot] = 0; }
+__global__ void wave_reset_kernel(int *count, int slot, unsigned int *cel_ctr) {
+  count[slot] = 0;
+  *cel_ctr = 0u;
+}
 
 }  // namespace
 
 // blocks per SM of the level-population kernels: as many as are resident
 int cel_blocks_per_sm() { return 32; }
+// wave_cel_kernel: 2 blocks of 4 warps per SM (255 registers), each warp
+// with its staged tables in shared memory
+constexpr int kCelBlocksPerSm = 2;
+static size_t cel_smem() { return (size_t)4 * kCelStage * sizeof(float); }
 
 // shared memory of wave_grain_kernel: per warp the cell's photon flux per
 // bin and each size's two suffix sums over the bins above grainVn
@@ -372,7 +403,9 @@ cudaError_t cell_update_fp32_prepare(const UpdArgs &a) {
                                          (int)grain_smem(a.g));
     if (e != cudaSuccess) return e;
   }
-  return cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaError_t e = cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cel_smem());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 size_t cell_update_fp32_scratch(int nc, int ncel, int nsizes, int nb) {
@@ -398,13 +431,14 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
   w.flags = (int *)take(nc1 * sizeof(int));
   w.act[0] = (int *)take(nc1 * sizeof(int));
   w.act[1] = (int *)take(nc1 * sizeof(int));
-  w.count = (int *)take(2 * sizeof(int));
+  w.count = (int *)take(4 * sizeof(int));  // two list lengths, the task counter
+  w.cel_ctr = (unsigned int *)(w.count + 2);
   if (a.g.nsizes > 0) {
     w.gheat = (float *)take(nc1 * sizeof(float));
     w.gcool = (float *)take(nc1 * sizeof(float));
     w.gpf = (float *)take(nc1 * (size_t)((a.g.nb + 1) & ~1) * sizeof(float));
   }
-  cudaError_t e = cudaMemsetAsync(w.count, 0, 2 * sizeof(int), stream);
+  cudaError_t e = cudaMemsetAsync(w.count, 0, 4 * sizeof(int), stream);
   if (e != cudaSuccess) return e;
   const int blocks = num_sms * 8;
   wave_init_kernel<<<blocks, 256, 0, stream>>>(w);
@@ -413,10 +447,10 @@ cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms
   const int steps = a.x_prev ? 26 : 25;
   for (int t = 0; t < steps; ++t) {
     const int cur = t & 1;
-    wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1);
+    wave_reset_kernel<<<1, 1, 0, stream>>>(w.count, cur ^ 1, w.cel_ctr);
     wave_ion_kernel<<<blocks * 2, kIonThreads, 4 * kNB * kIonThreads * sizeof(float), stream>>>(w, cur);
     if (a.g.nsizes > 0) wave_grain_kernel<<<blocks, 128, grain_smem(a.g), stream>>>(w, cur);
-    wave_cel_kernel<<<num_sms * cel_blocks_per_sm(), 128, 0, stream>>>(w, cur);
+    wave_cel_kernel<<<num_sms * kCelBlocksPerSm, 128, cel_smem(), stream>>>(w, cur);
     wave_therm_kernel<<<blocks, 128, 0, stream>>>(w, cur);
   }
   return cudaGetLastError();

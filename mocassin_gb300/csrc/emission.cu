@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) emission_forb_kernel(const __grid_constan
     const float up = C.ion < kNS ? (float)Xc[C.e * kNX + C.ion + 1] / xi : 0.f;
     float x[kNL * kNL];
     forb[(size_t)k * (nc + 1) + c] =
-        cel_cooling_f32(a, k, Te, Ne, up, x, a.mat_rows, kNL, T.ab[C.e] * xi * 1.9865e9f);
+        cel_cooling_f32(a, k, CelTabGlobal(T, k), Te, Ne, up, x, a.mat_rows, kNL, T.ab[C.e] * xi * 1.9865e9f);
   }
 }
 
