@@ -378,15 +378,18 @@ def batched_models(args):
         srv.submit(sp)
     rep = srv.run()
     rep["batch"] = "%d of the 64-model batch (seed 1)" % len(specs)
-    # the same requests served in lockstep: the group's transports in one
-    # mc_batch_run per Lambda iteration (one march launch per round)
+    # the same requests served in lockstep: groups of 16 models, each group's
+    # transports in one mc_batch_run per Lambda iteration (one march launch
+    # per round), two groups in flight (one's transports overlap the other's
+    # updates)
     lk = serve.ModelServer(memory_budget=200e9, workers=args.batch_workers, iterations=3,
-                           autotune_packets=200_000, lockstep=True, group=len(specs))
+                           autotune_packets=200_000, lockstep=True, group=16, lanes=2)
     for sp in specs:
         lk.submit(sp)
     lrep = lk.run()
     rep["lockstep"] = {k: lrep[k] for k in ("models", "errors", "wall_s", "crossings_per_s", "latency_ms_p50",
                                             "latency_ms_p99", "peak_resident_models", "mode")}
+    rep["lockstep"]["groups"] = "16 models per group, 2 groups in flight"
     rep["one_launch_transport"] = batch_launch_transport(specs)
     return rep
 

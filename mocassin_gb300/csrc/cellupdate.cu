@@ -86,8 +86,7 @@ cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int nu
   // grains: each warp stages its cell's photon flux per bin in shared memory
   const size_t sh = a.g.nsizes > 0 ? (size_t)kW * a.g.nb * sizeof(double) : 0;
   if (sh > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(cell_update_kernel<double, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    cudaError_t e = raise_smem_limit((const void *)cell_update_kernel<double, false>, sh);
     if (e != cudaSuccess) return e;
   }
   cell_update_kernel<double, false><<<blocks, kW * 32, sh, stream>>>(a);

@@ -399,11 +399,10 @@ static size_t grain_smem(const GrainArgs &g) {
 
 cudaError_t cell_update_fp32_prepare(const UpdArgs &a) {
   if (a.g.nsizes > 0) {
-    cudaError_t e = cudaFuncSetAttribute(wave_grain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)grain_smem(a.g));
+    cudaError_t e = raise_smem_limit((const void *)wave_grain_kernel, (int)grain_smem(a.g));
     if (e != cudaSuccess) return e;
   }
-  cudaError_t e = cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cel_smem());
+  cudaError_t e = raise_smem_limit((const void *)wave_cel_kernel, (int)cel_smem());
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(wave_cel_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }

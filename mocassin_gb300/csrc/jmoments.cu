@@ -211,7 +211,7 @@ cudaError_t launch_jmoments(int nc1, int nb, int nout, const double *J, const fl
   a.N = ((nout + 15) / 16) * 16;
   a.J = J; a.W = W; a.scale = scale; a.out = out; a.error = error;
   const size_t sh = (size_t)2 * kJM * kJK * 2 + (size_t)2 * a.N * kJK * 2 + 64;
-  cudaError_t e = cudaFuncSetAttribute(jmoment_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaError_t e = raise_smem_limit((const void *)jmoment_tc_kernel, (int)sh);
   if (e != cudaSuccess) return e;
   // the whole carveout as shared memory, so several CTAs (each holding at
   // most 128 of the SM's 512 TMEM columns) share an SM and overlap their

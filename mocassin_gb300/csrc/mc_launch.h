@@ -50,6 +50,12 @@ cudaError_t launch_wave_fold(const double *src, double *dst, const int32_t *lin2
 cudaError_t launch_wave_expand(const float *src, float *dst, const int32_t *lin2cell, long long ncell3, int nc1,
                                int nb, cudaStream_t stream);
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` and never
+// lowers it: several host threads (one context and stream per model) launch
+// the same kernels with their own sizes, and a limit one thread sets must not
+// fall below what another thread's launch needs.
+cudaError_t raise_smem_limit(const void *func, size_t bytes);
+
 // Opacity contraction: method 0 = FP32 CUDA cores, 1 = tcgen05 split BF16.
 cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const float *den, const float *xs,
                            const float *ff, float *out, int *error, int num_sms, cudaStream_t stream);

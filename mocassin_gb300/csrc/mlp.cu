@@ -676,8 +676,7 @@ cudaError_t launch_mlp_gather(int B, long long n, uint32_t seed, const int *dste
 }
 
 cudaError_t mlp_prepare() {
-  return cudaFuncSetAttribute(mlp_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)mlp_fwd_smem(256, 256));
+  return raise_smem_limit((const void *)mlp_fwd_tc_kernel, (int)mlp_fwd_smem(256, 256));
 }
 
 cudaError_t launch_mlp_stats(long long n, int cols, const float *a, double *sum, double *sq, cudaStream_t s) {

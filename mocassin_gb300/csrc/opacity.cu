@@ -376,7 +376,7 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
                            const float *ff, float *out, int *error, int num_sms, cudaStream_t stream) {
   if (method == 0) {
     const size_t sh = (size_t)nspecies * nb * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(opacity_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    cudaError_t e = raise_smem_limit((const void *)opacity_fp32_kernel, (int)sh);
     if (e != cudaSuccess) return e;
     const long long want = (nc1 + 255) / 256;
     const int blocks = (int)(want < num_sms * 4 ? want : num_sms * 4);
@@ -393,7 +393,7 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
     // the pipelined kernel: two CTAs per SM (2 x 256 TMEM columns), the
     // blocks split evenly over the bin tiles
     const size_t shp = opacity_pipe_smem(a.K);
-    cudaError_t e = cudaFuncSetAttribute(opacity_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shp);
+    cudaError_t e = raise_smem_limit((const void *)opacity_pipe_kernel, (int)shp);
     if (e != cudaSuccess) return e;
     const int nvt = (nb + kOpN - 1) / kOpN;
     const int ntiles = (nc1 + kOpM - 1) / kOpM;
@@ -404,7 +404,7 @@ cudaError_t launch_opacity(int method, int nc1, int nspecies, int nb, const floa
     return cudaGetLastError();
   }
   const size_t sh = opacity_tc_smem(a.K);
-  cudaError_t e = cudaFuncSetAttribute(opacity_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaError_t e = raise_smem_limit((const void *)opacity_tc_kernel, (int)sh);
   if (e != cudaSuccess) return e;
   const int nvt = (nb + kOpN - 1) / kOpN;
   const int ntiles = (nc1 + kOpM - 1) / kOpM;

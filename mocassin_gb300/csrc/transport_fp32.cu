@@ -1,3 +1,5 @@
+#include <mutex>
+#include <unordered_map>
 // FP32 instantiation of the plain transport (contraction allowed).
 #include "mc_launch.h"
 #include "transport_plain.cuh"
@@ -28,7 +30,7 @@ static const int kGridPerSm = 4;
 template <bool Replay> static cudaError_t sample_stellar_impl(const WaveLaunch &L) {
   auto k = wave_sample_stellar_kernel<float, Replay>;
   const size_t sh = (size_t)L.g.nb * (1 + L.S.nsrc) * sizeof(unsigned int);
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaError_t e = raise_smem_limit((const void *)k, (int)sh);
   if (e != cudaSuccess) return e;
   k<<<L.num_sms * kGridPerSm, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, L.cnt);
   return cudaGetLastError();
@@ -40,7 +42,7 @@ cudaError_t launch_wave_sample_stellar_fp32(const WaveLaunch &L) {
 template <bool Replay> static cudaError_t sample_reemit_impl(const WaveLaunch &L, unsigned int n) {
   auto k = wave_sample_reemit_kernel<float, Replay>;
   const size_t sh = (size_t)L.g.nb * sizeof(unsigned int);
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaError_t e = raise_smem_limit((const void *)k, (int)sh);
   if (e != cudaSuccess) return e;
   const unsigned int blocks = (unsigned int)min((long long)L.num_sms * kGridPerSm, (n + 255ll) / 256 + 1);
   k<<<blocks, 256, sh, L.stream>>>(L.g, L.S, L.rp, L.w, n, L.cnt);
@@ -67,7 +69,7 @@ cudaError_t launch_wave_emit_fp32(const WaveLaunch &L, int round) {
 template <bool Dust, bool Replay> static cudaError_t march_impl(const WaveLaunch &L) {
   auto k = wave_march_kernel<float, true, Dust, Replay>;
   const size_t sh = march_smem_bytes<float>(L.g.nx, L.g.ny, L.g.nz, 256 / 32);
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaError_t e = raise_smem_limit((const void *)k, (int)sh);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, sh);
@@ -78,7 +80,7 @@ template <bool Dust, bool Replay> static cudaError_t march_impl(const WaveLaunch
 }
 template <bool Dust> static cudaError_t march_batch_blocks(size_t smem, int num_sms, int *blocks) {
   auto k = wave_march_batch_kernel<float, true, Dust>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void *)k, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
@@ -104,6 +106,17 @@ cudaError_t launch_wave_march_fp32(const WaveLaunch &L) {
   const bool dust = L.g.flags & MC_FLAG_DUST;
   if (L.rp.draws) return dust ? march_impl<true, true>(L) : march_impl<false, true>(L);
   return dust ? march_impl<true, false>(L) : march_impl<false, false>(L);
+}
+
+cudaError_t raise_smem_limit(const void *func, size_t bytes) {
+  static std::mutex m;
+  static std::unordered_map<const void *, size_t> limits;
+  std::lock_guard<std::mutex> lock(m);
+  size_t &cur = limits[func];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
 }
 
 }  // namespace mcg

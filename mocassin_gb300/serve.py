@@ -16,7 +16,9 @@ order, up to ``group`` of them and the memory budget) and advances the
 group one Lambda iteration at a time: the group's transports are one
 mc_batch_run (the rounds of all its models in step, one persistent march
 launch per round), then every model's cell update, opacity and emission
-CDFs run at once, one thread per model of the group.
+CDFs run at once, one thread per model of the group.  ``lanes`` groups are
+in flight at once (one thread each), so one group's transports overlap
+another group's updates.
 
 Reported: wall time, aggregate cell crossings per second, the p50 / p99 of
 the per-iteration latency, the peak number of resident models and bytes.
@@ -50,8 +52,9 @@ def device_bytes(neb):
 
 class ModelServer:
     def __init__(self, memory_budget=200e9, workers=4, iterations=3, form="graph", update="fp32",
-                 autotune_packets=0, lockstep=False, group=16):
+                 autotune_packets=0, lockstep=False, group=16, lanes=1):
         self.lockstep = bool(lockstep)
+        self.lanes = int(lanes)
         self.group = int(group)
         self.budget = float(memory_budget)
         self.workers = int(workers)
@@ -133,77 +136,102 @@ class ModelServer:
 
     def _run_lockstep(self):
         todo = list(self.requests)
-        # one thread per model of a group: every model's update, opacity and
-        # CDFs run at once on their own streams after the batched transport
-        with ThreadPoolExecutor(max(1, self.workers, self.group)) as pool:
-            i = 0
-            while i < len(todo):
-                t_req = time.perf_counter()
-                group = todo[i:i + self.group]
-                nebs = list(pool.map(lambda r: nebula.build(r[0]), group))
-                take, total = 0, 0
-                for neb in nebs:  # the group's models that fit in the budget (at least one)
-                    nb = device_bytes(neb)
-                    if take and total + nb > self.budget:
-                        break
-                    take, total = take + 1, total + nb
-                group, nebs = group[:take], nebs[:take]
-                i += take
-                self._admit(total)
-                self._resident_models += take - 1
-                self.peak_models = max(self.peak_models, self._resident_models)
-                lis = []
+        nxt = [0]
+        take_lock = threading.Lock()
+
+        def lane():
+            # one thread per model of a group: every model's update, opacity
+            # and CDFs run at once on their own streams after the batched
+            # transport
+            with ThreadPoolExecutor(max(1, self.workers, self.group)) as pool:
+                while True:
+                    with take_lock:
+                        if nxt[0] >= len(todo):
+                            return
+                        group = todo[nxt[0]:nxt[0] + self.group]
+                        nxt[0] += len(group)
+                    self._serve_group(group, pool)
+
+        # `lanes` groups in flight: one group's transports overlap another's updates
+        threads = [threading.Thread(target=lane) for _ in range(max(1, self.lanes))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+
+    def _serve_group(self, group, pool):
+        t_req = time.perf_counter()
+        nebs = list(pool.map(lambda r: nebula.build(r[0]), group))
+        while group:
+            # the group's models that fit in the budget (at least one); the rest form the next group
+            take, total = 0, 0
+            for neb in nebs:
+                nb = device_bytes(neb)
+                if take and total + nb > self.budget:
+                    break
+                take, total = take + 1, total + nb
+            self._serve_admitted(group[:take], nebs[:take], total, pool, t_req)
+            group, nebs = group[take:], nebs[take:]
+
+    def _serve_admitted(self, group, nebs, total, pool, t_req):
+        take = len(group)
+        self._admit(total)
+        with self._lock:
+            self._resident_models += take - 1
+            self.peak_models = max(self.peak_models, self._resident_models)
+        lis = []
+        try:
+            # the group's models are set up (context, tables, tuning) on the pool's threads at once
+            def setup(neb):
+                li = iterate.LambdaIteration(neb, form="wave", update=self.update)
                 try:
-                    # the group's models are set up (context, tables, tuning) on the pool's threads at once
-                    def setup(neb):
-                        li = iterate.LambdaIteration(neb, form="wave", update=self.update)
-                        try:
-                            self._tune(li, neb, "wave")
-                        except Exception:
-                            li.close()
-                            raise
-                        return li
-                    futs = [pool.submit(setup, neb) for neb in nebs]
-                    err = None
-                    for f in futs:
-                        try:
-                            lis.append(f.result())
-                        except Exception as exc:
-                            err = err or exc
-                    if err is not None:
-                        raise err
-                    t0 = time.perf_counter()
-                    lat = [[] for _ in lis]
-                    cross = [0] * len(lis)
-                    last = [None] * len(lis)
-                    for it in range(max(r[1] for r in group)):
-                        live = [k for k, r in enumerate(group) if it < r[1]]
-                        # mc_batch_run takes gas-only or dusty grids, not both
-                        for dusty in (False, True):
-                            ks = [k for k in live if bool(lis[k].dust is not None) == dusty]
-                            if not ks:
-                                continue
-                            recs = iterate.batched_step([lis[k] for k in ks],
-                                                        [model_seed(group[k][0].name, it) for k in ks], pool=pool)
-                            for k, rec in zip(ks, recs):
-                                lat[k].append(rec["wall_s"])
-                                cross[k] += rec["crossings"]
-                                last[k] = rec
-                    t1 = time.perf_counter()
-                    for k, (spec, iters) in enumerate(group):
-                        self.results.append({"model": spec.name, "cells": nebs[k].ncells,
-                                             "packets": int(sum(nebs[k].n_packets)), "iterations": iters,
-                                             "latency_s": lat[k], "crossings": cross[k],
-                                             "converged_pct": last[k]["converged_pct"] if last[k] else None,
-                                             "run_s": t1 - t0, "queue_s": t0 - t_req,
-                                             "bytes": device_bytes(nebs[k])})
-                except Exception as exc:  # reported, the next group goes on
-                    self.errors.append("%s: %s" % (",".join(r[0].name for r in group), exc))
-                finally:
-                    for li in lis:
-                        li.close()
-                    self._resident_models -= take - 1
-                    self._release(total)
+                    self._tune(li, neb, "wave")
+                except Exception:
+                    li.close()
+                    raise
+                return li
+            futs = [pool.submit(setup, neb) for neb in nebs]
+            err = None
+            for f in futs:
+                try:
+                    lis.append(f.result())
+                except Exception as exc:
+                    err = err or exc
+            if err is not None:
+                raise err
+            t0 = time.perf_counter()
+            lat = [[] for _ in lis]
+            cross = [0] * len(lis)
+            last = [None] * len(lis)
+            for it in range(max(r[1] for r in group)):
+                live = [k for k, r in enumerate(group) if it < r[1]]
+                # mc_batch_run takes gas-only or dusty grids, not both
+                for dusty in (False, True):
+                    ks = [k for k in live if bool(lis[k].dust is not None) == dusty]
+                    if not ks:
+                        continue
+                    recs = iterate.batched_step([lis[k] for k in ks],
+                                                [model_seed(group[k][0].name, it) for k in ks], pool=pool)
+                    for k, rec in zip(ks, recs):
+                        lat[k].append(rec["wall_s"])
+                        cross[k] += rec["crossings"]
+                        last[k] = rec
+            t1 = time.perf_counter()
+            for k, (spec, iters) in enumerate(group):
+                self.results.append({"model": spec.name, "cells": nebs[k].ncells,
+                                     "packets": int(sum(nebs[k].n_packets)), "iterations": iters,
+                                     "latency_s": lat[k], "crossings": cross[k],
+                                     "converged_pct": last[k]["converged_pct"] if last[k] else None,
+                                     "run_s": t1 - t0, "queue_s": t0 - t_req,
+                                     "bytes": device_bytes(nebs[k])})
+        except Exception as exc:  # reported, the next group goes on
+            self.errors.append("%s: %s" % (",".join(r[0].name for r in group), exc))
+        finally:
+            for li in lis:
+                li.close()
+            with self._lock:
+                self._resident_models -= take - 1
+            self._release(total)
 
     def run(self):
         """Serves every submitted request; returns the report."""

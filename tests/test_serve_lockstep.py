@@ -80,3 +80,39 @@ def test_memory_budget_splits_groups_and_kinds_batch_apart(monkeypatch):
     rep = srv.run()
     assert rep["models"] == 2
     assert sorted(c[1] for c in calls) == [[False], [True]]
+
+
+def test_two_lanes_serve_groups_at_once(monkeypatch):
+    """With lanes=2 two groups are in flight: every request is served once,
+    each group steps its own models, and the resident count returns to 0."""
+    import threading
+    import time
+    calls = []
+    inflight, peak = [0], [0]
+    lock = threading.Lock()
+    _FakeModel.made = []
+    monkeypatch.setattr(iterate, "LambdaIteration", _FakeModel)
+    step = _fake_step(calls)
+
+    def slow_step(models, seeds, pool=None):
+        with lock:
+            inflight[0] += 1
+            peak[0] = max(peak[0], inflight[0])
+        time.sleep(0.05)
+        try:
+            return step(models, seeds, pool)
+        finally:
+            with lock:
+                inflight[0] -= 1
+
+    monkeypatch.setattr(iterate, "batched_step", slow_step)
+    gas = [s for s in nebula.small_cases() if not s.dust]
+    srv = serve.ModelServer(iterations=2, lockstep=True, group=1, lanes=2)
+    for s in gas[:4]:
+        srv.submit(s)
+    rep = srv.run()
+    assert rep["errors"] == [] and rep["models"] == 4 and rep["iterations"] == 8
+    assert sorted(r["model"] for r in srv.results) == sorted(s.name for s in gas[:4])
+    assert peak[0] == 2 and len(calls) == 8
+    assert srv._resident == 0 and srv._resident_models == 0
+    assert all(m.closed for m in _FakeModel.made)
