@@ -570,7 +570,8 @@ def main():
         in_bytes = kk * (neb.ncells + 1) * 4
         flops = 2.0 * (neb.ncells + 1) * kk * neb.nbins
         t = res["bf16x3"] / 1e3
-        opac = {"kernel": "opacity_tc_kernel (tcgen05 kind::f16, split BF16 x3, FP32 accumulate)",
+        opac = {"kernel": "opacity_pipe_kernel (tcgen05 kind::f16, split BF16 x3, FP32 accumulate, stores of a tile "
+                          "overlapping the next tile's MMAs)",
                 "species": kk, "ms": res["bf16x3"], "fp32_cuda_core_ms": res["fp32"],
                 "achieved_gbs": (out_bytes + in_bytes) / t / 1e9, "frac_of_hbm": (out_bytes + in_bytes) / t / 1e9 / measured_peak()[0],
                 "useful_tflops": flops / t / 1e12, "tensor_tflops_issued": 3 * flops * (((kk + 15) // 16) * 16 / kk) / t / 1e12,
