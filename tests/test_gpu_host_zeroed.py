@@ -69,3 +69,33 @@ def test_gas_grid_reads_no_opacity_row_below_the_ionisation_edge(gpu_lib):
             np.testing.assert_allclose(got[0], ref[0], rtol=1e-12, atol=0)
             np.testing.assert_allclose(got[2], ref[2], rtol=1e-12, atol=0)
         assert np.isfinite(got[0]).all() and got[3]["crossings"] == ref[3]["crossings"]
+
+
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+def test_new_opacity_reaches_the_next_calls_march(gpu_lib, pinned):
+    """A second drop-in call of the same grid shape keeps the device buffers
+    of the first and uploads only the opacity rows a packet can march in:
+    with another opacity it gives the transport of that opacity (the FP64
+    plain form is the reference: the same draws, counters and sums to
+    1e-12)."""
+    neb = nebula.build(CASES[1])
+    js, es, keep = _arrays(neb, np.float64, pinned)
+    transport.energy_packet_driver(neb, precision="fp64", seed=71, jste=js, escaped=es, host_zeroed=True,
+                                   form="graph")
+    op = np.ascontiguousarray(neb.opacity * 3.0)
+    if pinned:
+        import torch
+        top = torch.from_numpy(op).pin_memory()
+        op = top.numpy()
+    neb.opacity = op
+    js2, es2, keep2 = _arrays(neb, np.float64, pinned)
+    _, _, _, st = transport.energy_packet_driver(neb, precision="fp64", seed=72, jste=js2, escaped=es2,
+                                                 host_zeroed=True, form="graph")
+    rj, re_ = helpers.zeros_like_estimators(neb)[::2]
+    _, _, _, ref = transport.energy_packet_driver(neb, precision="fp64", seed=72, jste=rj, escaped=re_,
+                                                  zero_first=True, form="plain")
+    for k in ("crossings", "absorptions", "escaped"):
+        assert st[k] == ref[k], (k, st[k], ref[k])
+    np.testing.assert_allclose(js2, rj, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(es2, re_, rtol=1e-12, atol=0)
+    del keep, keep2
