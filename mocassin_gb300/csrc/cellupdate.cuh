@@ -352,10 +352,9 @@ constexpr int kCelStage = kNT + 2 * kNL + kCelMaxPairs + 2 * kCelMaxPairs * kNT;
 // one base pointer: every table sits at a fixed offset from it
 struct CelTabStaged {
   const float *s;
-  int nt;
   static constexpr int kG = kNT, kE = kNT + kNL, kA = kNT + 2 * kNL, kQ = kA + kCelMaxPairs,
                        kQ2 = kQ + kCelMaxPairs * kNT;
-  __device__ __forceinline__ CelTabStaged(const float *s_, int nt_) : s(s_), nt(nt_) {}
+  __device__ __forceinline__ explicit CelTabStaged(const float *s_) : s(s_) {}
   __device__ __forceinline__ const float *logt() const { return s; }
   __device__ __forceinline__ const float *g() const { return s + kG; }
   __device__ __forceinline__ const float *e() const { return s + kE; }

@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128) wave_cel_kernel(const __grid_constant__ W
     const float up = C.ion < kNS ? XS(w, C.e * kNX + C.ion + 1, c) / xi : 0.f;
     float emis = 0.f;
     const float es = T.ab[C.e] * xi * 1.9865e9f;
-    const float cool = reg ? cel_cooling_f32(a, k, CelTabStaged(stage, C.nt), Te, Ne, up, x, a.mat_rows, 10, 0.f,
+    const float cool = reg ? cel_cooling_f32(a, k, CelTabStaged(stage), Te, Ne, up, x, a.mat_rows, 10, 0.f,
                                              a.forb_out ? &emis : nullptr, es)
                            : cel_cooling_smem<float>(a, k, Te, Ne, up, x, a.mat_rows, 10, 0.f,
                                                      a.forb_out ? &emis : nullptr, es);
@@ -383,8 +383,6 @@ __global__ void wave_reset_kernel(int *count, int slot, unsigned int *cel_ctr) {
 
 }  // namespace
 
-// blocks per SM of the level-population kernels: as many as are resident
-int cel_blocks_per_sm() { return 32; }
 // wave_cel_kernel: 2 blocks of 4 warps per SM (255 registers), each warp
 // with its staged tables in shared memory
 constexpr int kCelBlocksPerSm = 2;

@@ -144,7 +144,6 @@ cudaError_t launch_cell_update(const UpdArgs &a, int fp32, void *scratch, int nu
 cudaError_t launch_cell_update_fp32(const UpdArgs &a, void *scratch, int num_sms, cudaStream_t stream);
 // sets the cache preference of the FP32 form's kernels (before a capture)
 cudaError_t cell_update_fp32_prepare(const UpdArgs &a);
-int cel_blocks_per_sm();
 size_t cell_update_fp32_scratch(int nc, int ncel, int nsizes, int nb);
 cudaError_t launch_update_stats(int nc, const int *conv, const int *niter, const int *flags, const double *dte,
                                 UpdStatsDev *s, int num_sms, cudaStream_t stream);
