@@ -272,7 +272,7 @@ def _lambda_form(neb, name, args, rows):
     return rec, state
 
 
-def converged_model(neb, args):
+def converged_model(neb, args, keep=None):
     """Wall time to a converged model: Lambda iterations (transport, cell
     update, opacity and emission-CDF rebuild) until 95 % of the cells have
     |dX(H0)/X(H0)| <= 5 % (the reference's minConvergence / XHILimit), for
@@ -293,6 +293,8 @@ def converged_model(neb, args):
         x, t, info = iterate.training_rows(nebula.batch64(), max_rows=args.surrogate_rows)
         rows = (x, t)
         out["surrogate_dataset"] = info
+    if keep is not None:
+        keep["rows"] = rows
     states = {}
     for name in LAMBDA_FORMS:
         out[name], states[name] = _lambda_form(neb, name, args, rows)
@@ -341,6 +343,53 @@ def converged_model(neb, args):
         rep["warm_start_gain_in_se"] = float((a["mean"] - b["mean"]) / se) if se > 0 else None
         out["repeats"] = rep
     return out
+
+
+LAMBDA_KEYS = ("wall_s", "iterations", "converged", "converged_pct", "dte_lt_1pc_pct", "wall_to_dte_rule_s",
+               "transport_s", "update_s", "t_steps_per_cell", "warm_fallback_pct")
+
+
+def other_workloads(args, rows):
+    """The other benchmark workloads, one record each: the octant 21^3 of
+    the reference's CPU-runnable case, the dusty 81^3 and the two-star 101^3
+    of the learned warm start.  The transport's crossings/s (graph form,
+    FP32 march, device time of 3 steps after 2 warm-up steps) and the wall
+    time to a converged model of the chosen form (and, on the two-star grid,
+    with the warm start trained on the batch's FP64 cell states as for the
+    main workload)."""
+    out = {}
+    for name, warm in (("octant21", False), ("dusty81", False), ("twostar101", True)):
+        try:
+            out[name] = _workload_record(name, warm, args, rows)
+        except Exception as exc:  # reported in the record; the bench line still prints
+            out[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+    return out
+
+
+def _workload_record(name, warm, args, rows):
+    """One workload of other_workloads."""
+    from mocassin_gb300 import nebula, transport
+    neb = nebula.build(workload(name))
+    ctx = transport.TransportContext(neb)
+    try:
+        for k in range(2):
+            ctx.run(seed=900 + k, precision="fp32", zero_first=True, form="graph")
+        sts = [ctx.run(seed=910 + k, precision="fp32", zero_first=True, form="graph") for k in range(3)]
+    finally:
+        ctx.close()
+    cross = sum(st["crossings"] for st in sts)
+    ms = sum(st["kernel_ms"] for st in sts)
+    rec = {"workload": neb.spec.name, "cells": neb.ncells, "packets_per_step": int(sum(neb.n_packets)),
+           "crossings_per_step": cross / len(sts), "step_ms": ms / len(sts),
+           "crossings_per_s": cross / (ms / 1e3) if ms > 0 else None,
+           "transport": "graph form, FP32 march, FP64 sums; device time of the whole call"}
+    if args.lambda_max > 0:
+        forms = ("chosen", "chosen_surrogate") if warm and rows is not None else ("chosen",)
+        rec["converged_model"] = {}
+        for f in forms:
+            r = _lambda_form(neb, f, args, rows)[0]
+            rec["converged_model"][f] = {k: r[k] for k in LAMBDA_KEYS if k in r}
+    return rec
 
 
 def breakdown(neb, args, runs):
@@ -451,6 +500,8 @@ def main():
     ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--surrogate-rows", type=int, default=1_000_000,
                     help="batch cell states (FP64 update) the warm start is trained on; 0: the model's own")
+    ap.add_argument("--no-other-workloads", dest="other_workloads", action="store_false",
+                    help="skip the octant 21^3, dusty 81^3 and two-star 101^3 records")
     ap.add_argument("--repeats", type=int, default=5,
                     help="runs of the chosen form with and without the warm start (mean and sd of their times)")
     ap.add_argument("--breakdown", type=int, default=0,
@@ -675,8 +726,11 @@ def main():
         line["opacity_build"] = opac
     if moments:
         line["jste_moments"] = moments
+    keep = {}
     if args.lambda_max > 0 and rank == 0:
-        line["converged_model"] = converged_model(neb, args)
+        line["converged_model"] = converged_model(neb, args, keep)
+    if args.other_workloads and rank == 0 and ws == 1:
+        line["other_workloads"] = other_workloads(args, keep.get("rows"))
     if args.batch_models > 0 and rank == 0:
         line["batched_models"] = batched_models(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
