@@ -28,8 +28,11 @@
  *  - Every entry point returns an mc_status (0 = MC_OK).  The reference's
  *    fatal "print*; stop" insanity checks become error codes; the text of the
  *    last error of the calling thread is returned by mc_last_error().
- *  - One host thread per process drives the library (the reference is one
- *    thread per MPI rank).  Calls are not re-entrant on one context.
+ *  - The Fortran driver calls from one host thread (the reference is one
+ *    thread per MPI rank).  Several host threads may drive the library at
+ *    once, each on its own context (mc_ctx_t; the batch server does so):
+ *    calls are not re-entrant on one context, and the drop-in calls
+ *    (mc_transport_run / _f32) share one cached context and serialise on it.
  */
 #ifndef MOCASSIN_GPU_H
 #define MOCASSIN_GPU_H
