@@ -695,7 +695,8 @@ def main():
                    "scatter of the nonzero escapedPackets entries, FP64 sums rounded once on the device; the "
                    "caller's estimators zeroed between calls outside the timed region, as the Fortran driver "
                    "zeroes them before each iteration; device buffers kept between calls of the same grid "
-                   "shape); bytes are those the call reports having copied"}
+                   "shape, the entries a call made nonzero cleared on the device once copied); bytes are those "
+                   "the call reports having copied"}
 
     peak, peak_kind = measured_peak()
     # dominant kernel: the march (its own CUDA events on the library stream)
